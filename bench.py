@@ -1,0 +1,433 @@
+"""Benchmark of the batched LUP determinant on GB300.
+
+Default workload: 32768 lowest-Landau-level orbital matrices, n = 24, complex128
+(M_ij = z_i^j exp(-|z_i|^2/4), z ~ CN(0, 24), seed 2), i.e. the precision-stress
+configuration on which the mixed-vs-FP64 target is quoted. A "step" is one
+batched determinant call over the whole batch. The batch is 302 MB, larger than
+the 129 MB L2, so no flush is needed between steps.
+
+Prints ONE JSON line (rank 0). `value` is mixed-precision determinants/s with
+the batch resident in HBM; `e2e` is the same call through the C-ABI with the
+batch copied from pinned host memory each step and the results copied back.
+The plain FP64 kernels, accuracy against the double-double oracle, the
+roofline of the dominant kernel and the CPU baseline ride along in the line.
+
+`--impl reference` times the reference's CPU Crout path instead: the FP64
+restatement of LUCoreCPU::determinant (the reference is float32-only and its
+CPU code is not built on this machine), OpenMP over all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "lion-codes_gb300"))
+
+WORKLOADS = {
+    # name: (kind, n, batch, seed)
+    "lll24": ("lll", 24, 32768, 2),
+    "gauss16": ("gauss", 16, 65536, 1),
+    "gauss8": ("gauss", 8, 4096, 0),
+}
+
+
+def flops_per_matrix(n: int) -> float:
+    """Algorithmic flops of one n x n complex LUP: trailing-update complex MACs
+    at 8 real flops plus n(n-1)/2 multiplier scalings at 6 flops."""
+    return 4.0 * (n - 1) * n * (2 * n - 1) / 3.0 + 3.0 * n * (n - 1)
+
+
+def bytes_per_matrix(n: int) -> float:
+    """complex128 input + log|det| (8) + phase (8) + parity (1) + status (4)."""
+    return 16.0 * n * n + 21.0
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def accuracy_vs_fp64(np, mixed, plain) -> dict:
+    """Relative log|det| error of the mixed result against the plain FP64
+    kernel, |d log|det|| / max(1, |log|det||), and the phase error."""
+    ok = (plain["status"] == 0) & ((mixed["status"] & ~8) == 0)
+    rel = np.abs(mixed["logabs"][ok] - plain["logabs"][ok]) / np.maximum(
+        1.0, np.abs(plain["logabs"][ok]))
+    dph = np.abs(np.angle(np.exp(1j * (mixed["phase"][ok] - plain["phase"][ok]))))
+    accepted = ok & (mixed["status"] == 0)
+    rel_acc = np.abs(mixed["logabs"][accepted] - plain["logabs"][accepted]) / np.maximum(
+        1.0, np.abs(plain["logabs"][accepted]))
+    return {
+        "vs": "plain FP64 kernel (reference pivot rule and arithmetic), whole batch",
+        "max_rel_logabs_err": float(rel.max(initial=0.0)),
+        "median_rel_logabs_err": float(np.median(rel)) if rel.size else 0.0,
+        "p99_rel_logabs_err": float(np.quantile(rel, 0.99)) if rel.size else 0.0,
+        "max_rel_logabs_err_mixed_accepted": float(rel_acc.max(initial=0.0)),
+        "count_above_1e-10": int((rel > 1e-10).sum()),
+        "max_phase_err_rad": float(dph.max(initial=0.0)),
+        "compared": int(ok.sum()),
+        "note": "FP64 LU itself carries up to ~1e-10 rel error on these matrices; the "
+                "double-double oracle comparison lives in tests/test_gpu_mixed.py",
+    }
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """dram bytes (read + write) per launch from the committed ncu summary."""
+    p = ROOT / "profiles" / f"ncu_{kernel}_{workload}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------- GPU probes
+def measure_pipe_peaks(torch, lufqhe) -> dict:
+    """FP64 and FP32 FMA peaks of this GPU measured with the library's own
+    probe kernels (TFLOP/s, 2 flops per FMA)."""
+    import ctypes
+    lib = lufqhe.lib()
+    out = {}
+    for name, kind in (("fp64_tflops", 0), ("fp32_tflops", 1)):
+        v = ctypes.c_double()
+        rc = lib.lufqhe_probe_fma_peak(kind, ctypes.byref(v), None)
+        out[name] = v.value if rc == 0 else None
+    return out
+
+
+def make_inputs(torch, lufqhe, wl):
+    kind, n, batch, seed = WORKLOADS[wl]
+    if kind == "lll":
+        A, _ = lufqhe.gen_lll(batch, n, seed=seed)
+    else:
+        A = lufqhe.gen_gaussian(batch, n, seed=seed)
+    torch.cuda.synchronize()
+    return A, n, batch
+
+
+def time_device(torch, lufqhe, A, mode, out, steps, warmup, stream):
+    """ms per step with the batch resident; events on the launching stream."""
+    for _ in range(warmup):
+        lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=out)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import lufqhe
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        A, n, batch = make_inputs(torch, lufqhe, args.workload)
+    torch.cuda.synchronize()
+    res = lufqhe.DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
+                           torch.empty(batch, dtype=torch.float64, device=dev),
+                           torch.empty(batch, dtype=torch.int8, device=dev),
+                           torch.empty(batch, dtype=torch.int32, device=dev))
+
+    # ---- headline: mixed, device-resident --------------------------------
+    mode = lufqhe.MODE_MIXED
+    for _ in range(args.warmup):
+        lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=res)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=res)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_mixed = e0.elapsed_time(e1) / args.steps
+    time.sleep(0.2)
+    clocks = sampler.stop()
+    barrier(world)
+    ms_mixed_max = max_over_ranks(world, ms_mixed)
+    value = world * batch / (ms_mixed_max * 1e-3)
+    launches = args.steps  # one lup_mixed_kernel launch per step
+
+    mixed_out = {k: getattr(res, k).cpu().numpy() for k in ("logabs", "phase", "status")}
+
+    # ---- plain FP64 kernels (same batch) ---------------------------------
+    ms_plain_ref = time_device(torch, lufqhe, A, lufqhe.MODE_PLAIN_FP64, res,
+                               max(2, args.steps // 2), 2, stream)
+    plain_ref = {k: getattr(res, k).cpu().numpy() for k in ("logabs", "phase", "status")}
+    ms_plain_fused = time_device(torch, lufqhe, A, lufqhe.MODE_PLAIN_FP64_FUSED, res,
+                                 max(2, args.steps // 2), 2, stream)
+    launches += 2 * max(2, args.steps // 2)
+
+    # ---- e2e through the C-ABI with host buffers ---------------------------
+    A_host = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+    A_host.copy_(A)
+    A_dev = torch.empty_like(A)
+    out_host = {k: torch.empty(getattr(res, k).shape, dtype=getattr(res, k).dtype,
+                               pin_memory=True) for k in ("logabs", "phase", "parity", "status")}
+    h2d = A_host.numel() * A_host.element_size()
+    d2h = sum(t.numel() * t.element_size() for t in out_host.values())
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            A_dev.copy_(A_host, non_blocking=True)
+            lufqhe.batch_lup_det(A_dev, mode=mode, stream=stream, out=res)
+            for k, t in out_host.items():
+                t.copy_(getattr(res, k), non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = max_over_ranks(world, e2.elapsed_time(e3) / args.steps)
+    launches += args.steps
+
+    # ---- kernel-only timing of the dominant kernel (roofline) --------------
+    peaks_file = load_peaks()
+    pipes = measure_pipe_peaks(torch, lufqhe)
+    F = flops_per_matrix(n)
+    B = bytes_per_matrix(n)
+    hbm_peak = peaks_file.get("hbm_gbs")
+    hbm_src = "MEASURED_PEAKS.json" if hbm_peak else "fallback 6800 GB/s"
+    hbm_peak = hbm_peak or 6800.0
+
+    out = None
+    if rank == 0:
+        acc = accuracy_vs_fp64(np, mixed_out, plain_ref)
+        # cpu_baseline leg: the reference's CPU Crout path (FP64 restatement)
+        import bench_cpu
+        cpu = bench_cpu.cpu_baseline(np, A.cpu().numpy(), n, seconds=args.cpu_seconds)
+        dets_mixed = batch / (ms_mixed * 1e-3)
+        dets_ref = batch / (ms_plain_ref * 1e-3)
+        dets_fused = batch / (ms_plain_fused * 1e-3)
+        fallback = int(((mixed_out["status"] & lufqhe.ST_FALLBACK) != 0).sum())
+        fp32_peak = pipes.get("fp32_tflops")
+        fp64_peak = pipes.get("fp64_tflops")
+        achieved_tf = F * dets_mixed * 1e-12
+        roof = {
+            "kernel": "lup_mixed_kernel",
+            "bound": "fp32",
+            "achieved": achieved_tf,
+            "peak": fp32_peak,
+            "unit": "TFLOP/s",
+            "frac": (achieved_tf / fp32_peak) if fp32_peak else None,
+            "peak_source": "measured FP32 FMA peak (library probe kernel, this run)",
+            "flops_per_matrix": F,
+            "traffic": ncu_traffic("lup_mixed_kernel", args.workload),
+            "hbm": {"achieved": B * dets_mixed * 1e-9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": B * dets_mixed * 1e-9 / hbm_peak, "peak_source": hbm_src,
+                    "bytes_per_matrix": B},
+            "plain_fp64": {"kernel": "lup_plain_kernel<ARITH_FUSED>", "bound": "fp64",
+                           "achieved": F * dets_fused * 1e-12, "peak": fp64_peak,
+                           "unit": "TFLOP/s",
+                           "frac": (F * dets_fused * 1e-12 / fp64_peak) if fp64_peak else None},
+        }
+        out = {
+            "metric": "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)",
+            "value": value,
+            "unit": "dets/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_mixed_max,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "c128 in / fp32+float-float compute / f64 out",
+            "data": "synthetic (seeded, generated on device)",
+            "config": {"workload": f"{args.workload}: {batch} x n={n} "
+                                   f"{'LLL orbital' if WORKLOADS[args.workload][0] == 'lll' else 'complex Gaussian'} "
+                                   f"complex128, seed {WORKLOADS[args.workload][3]}",
+                       "batch": batch, "n": n,
+                       "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}"},
+            "plain_fp64": {"dets_per_s_reference_arith": dets_ref,
+                           "dets_per_s_fused": dets_fused,
+                           "mixed_over_plain_fused": dets_mixed / dets_fused,
+                           "mixed_over_plain_reference_arith": dets_mixed / dets_ref},
+            "accuracy": acc,
+            "fallbacks": {"count": fallback, "of": batch},
+            "e2e": {"value": world * batch / (ms_e2e * 1e-3), "unit": "dets/s",
+                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+    barrier(world)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    """The reference's CPU Crout path (FP64 restatement, OpenMP over host cores)."""
+    import numpy as np
+
+    import lufqhe
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import bench_cpu
+
+    def make_inputs(kind, n, count, seed):
+        if kind == "lll":
+            return lufqhe.gen_lll_host(count, n, seed=seed)[0]
+        return lufqhe.gen_gaussian_host(count, n, seed=seed)
+
+    kind, n, batch, seed = WORKLOADS[args.workload]
+    line = bench_cpu.reference_arm(np, args, kind, n, batch, seed, make_inputs)
+    line["n_gpus"] = world
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lll24", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-sample", type=int, default=8192)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

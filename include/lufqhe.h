@@ -1,0 +1,150 @@
+/*
+ * lufqhe: batched LUP determinants of small complex matrices on GB300 (sm_103a).
+ *
+ * C-ABI drop-in for the GPU batch-LUP call of lion-codes' LU-fqhe application.
+ * Every entry point takes plain pointers and sizes; no C++ or framework types
+ * cross the boundary. Device pointers are CUDA device addresses; `stream` is a
+ * cudaStream_t passed as an opaque pointer (NULL = legacy default stream).
+ * Calls are asynchronous on `stream` unless stated, re-entrant, and safe to
+ * issue concurrently on different streams: all geometry travels as kernel
+ * arguments (the reference keeps it in __constant__ memory set by
+ * cudaMemcpyToSymbol, LU-fqhe/src/LUCoreGPU.cu:33,53-76, which races when two
+ * host threads share a device with different n).
+ *
+ * Matrix layout (the reference's, LU-fqhe/src/LUCoreCPU.cu:85 and
+ * LU-fqhe/inc/LUCoreGPU.h:24-40): matrix b starts at element b*n*lda, row i at
+ * element i*lda, entries are interleaved (re, im) complex128 ("double2") or
+ * complex64 ("float2"). lda is the reference's loadSize (= n, or p2Above(n)
+ * with __PADDED__, LU-fqhe/src/RunInfo.cpp:72-76).
+ *
+ * Outputs per matrix (all optional except logabs):
+ *   logabs  log|det A|                      (float64)
+ *   phase   arg det A in (-pi, pi], permutation sign included  (float64)
+ *   parity  number of row swaps mod 2       (int8)
+ *   status  LUFQHE_ST_* flags, 0 = ok       (int32)
+ * Errors are returned, never exit(): the reference exits on a too-large grid
+ * (LU-fqhe/src/LUCoreGPU.cu:102-105) and on a near-zero row
+ * (LU-fqhe/src/LUCoreCPU.cu:158).
+ */
+#ifndef LUFQHE_H_
+#define LUFQHE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---- */
+#define LUFQHE_SUCCESS 0
+#define LUFQHE_ERR_INVALID_ARG (-1)
+#define LUFQHE_ERR_UNSUPPORTED_N (-2)
+#define LUFQHE_ERR_CUDA (-3)
+#define LUFQHE_ERR_UNSUPPORTED_MODE (-4)
+#define LUFQHE_ERR_BUSY (-5)
+#define LUFQHE_ERR_TIMEOUT (-6)
+#define LUFQHE_ERR_NO_MEMORY (-7)
+
+/* ---- per-matrix status flags ---- */
+#define LUFQHE_ST_SCALE_TINY 1 /* a row's max |Re| < 1e-24: the reference exits here (LUCoreCPU.cu:158) */
+#define LUFQHE_ST_SINGULAR 2   /* exact zero pivot: logabs = -inf, phase = 0 */
+#define LUFQHE_ST_NONFINITE 4  /* NaN/Inf in the input: logabs = phase = NaN */
+#define LUFQHE_ST_FALLBACK 8   /* mixed mode: refactorised in FP64 (result is the FP64 one) */
+
+/* ---- element types ---- */
+#define LUFQHE_C128 0
+#define LUFQHE_C64 1
+
+/* ---- methods ---- */
+/* FP64 LUP with the reference's pivot rule (implicit row scaling, pivot on
+ * |Re|/scale, ties to the last row) and the reference's arithmetic: every
+ * product and sum rounded separately, one division per multiplier. The
+ * L\U factors are bit-identical to the reference's CPU Crout restated in FP64. */
+#define LUFQHE_MODE_PLAIN_FP64 0
+/* Same pivot rule with fused multiply-adds and one reciprocal per column. */
+#define LUFQHE_MODE_PLAIN_FP64_FUSED 1
+/* FP32 complex LUP after power-of-two equilibration, FP64-accurate residual
+ * R = PA - LU (float-float on FP32 pipes), log det(I + U^-1 L^-1 R) correction,
+ * FP64 log|det|/phase accumulation, and a full FP64 refactorisation for any
+ * matrix whose correction norm exceeds the threshold (status FALLBACK). */
+#define LUFQHE_MODE_MIXED 2
+
+/* Largest n the batched entry points accept. */
+#define LUFQHE_MAX_N 64
+
+/*
+ * Batched determinant. Replaces LUCoreGPU::CALL
+ * (LU-fqhe/inc/LUCoreGPU.h:47, LU-fqhe/src/LUCoreGPU.cu:38-106): device batch
+ * pointer, n and batch count in; per-matrix determinant out. The input is not
+ * modified. Asynchronous on `stream`; no host synchronisation.
+ */
+int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int dtype, int mode,
+                         double *d_logabs, double *d_phase, int8_t *d_parity, int32_t *d_status,
+                         void *stream);
+
+/*
+ * In-place variant: overwrites each matrix with its L\U factors (unit-lower L
+ * below the diagonal, U on and above it, rows in pivoted order) exactly as the
+ * reference kernel leaves global memory (LU-fqhe/src/LUCoreGPU.cu:318-377).
+ * Plain modes only; complex128 only.
+ */
+int lufqhe_batch_lup_factor_inplace(void *d_A, int n, int lda, long long batch, int mode,
+                                    double *d_logabs, double *d_phase, int8_t *d_parity,
+                                    int32_t *d_status, void *stream);
+
+/*
+ * Reference-shaped call: LUCoreGPU::CALL with WRITE_DET (and PERFORM_PROD when
+ * pair_product != 0), LU-fqhe/src/LUCoreGPU.cu:384-435. For every matrix the
+ * complex determinant is written into its element (0,0); with pair_product,
+ * element (0,0) of matrix 2i receives det(A_2i)*det(A_2i+1). The rest of each
+ * matrix is left as L\U factors. complex128, plain FP64 reference arithmetic.
+ * A determinant outside the FP64 range becomes +-inf / 0 as the reference's
+ * direct product would.
+ */
+int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, int load_size,
+                          int pair_product, void *stream);
+
+/* ---- on-device synthetic inputs (seeded; identical on every device) ---- */
+/* i.i.d. complex Gaussian entries, Re and Im ~ N(0, sigma^2/2). */
+int lufqhe_gen_gaussian(double *d_A, int n, int lda, long long batch, unsigned long long seed,
+                        double sigma, void *stream);
+/* Lowest-Landau-level orbital matrices M_ij = z_i^j exp(-|z_i|^2/4),
+ * z_i complex Gaussian with E|z|^2 = sigma^2 (d_z receives the z_i, may be NULL). */
+int lufqhe_gen_lll(double *d_A, double *d_z, int n, int lda, long long batch,
+                   unsigned long long seed, double sigma, void *stream);
+
+/* Same generators on the host (bit-identical draws; libm's exp/sin/cos/log may
+ * differ from the device's in the last place). */
+int lufqhe_gen_gaussian_host(double *A, int n, int lda, long long batch, unsigned long long seed,
+                             double sigma);
+int lufqhe_gen_lll_host(double *A, double *z, int n, int lda, long long batch,
+                        unsigned long long seed, double sigma);
+
+/* ---- options (process-wide, read when a call is issued) ---- */
+/* ||E||_F above which the mixed mode refactorises a matrix in FP64 (default
+ * 0.1; 0 sends every matrix to the FP64 path, +inf disables the fallback
+ * except for zero or non-finite FP32 pivots). */
+#define LUFQHE_OPT_MIXED_THRESHOLD 1
+int lufqhe_set_option(int option, double value);
+double lufqhe_get_option(int option);
+
+/* ---- measurement ---- */
+/* Measured FMA-pipe peak of the current device in TFLOP/s (2 flops per FMA):
+ * kind 0 = FP64, kind 1 = FP32. Synchronises `stream`. No counterpart in the
+ * reference; it supplies the roofline denominators of the benchmark. */
+int lufqhe_probe_fma_peak(int kind, double *tflops, void *stream);
+
+/* ---- misc ---- */
+/* Bytes of device workspace a call needs (0 for the batched entry points). */
+size_t lufqhe_workspace_bytes(int n, long long batch, int mode);
+/* Text for the last error on the calling host thread. */
+const char *lufqhe_last_error(void);
+/* Library version as "major.minor.patch". */
+const char *lufqhe_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUFQHE_H_ */

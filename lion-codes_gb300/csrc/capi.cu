@@ -1,0 +1,184 @@
+// extern "C" entry points of liblufqhe: argument checks, dispatch, errors.
+
+#include <cstdarg>
+#include <cstdio>
+#include <cmath>
+#include <cstring>
+
+#include "lufqhe_internal.cuh"
+
+namespace lufqhe {
+
+namespace {
+thread_local char g_err[512] = "";
+
+struct DeviceProps {
+  int dev = -1;
+  int sms = 0;
+  size_t smem_optin = 0;
+};
+thread_local DeviceProps g_props;
+
+const DeviceProps &props() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (g_props.dev != dev) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
+      g_props.dev = dev;
+      g_props.sms = p.multiProcessorCount;
+      g_props.smem_optin = p.sharedMemPerBlockOptin;
+    }
+  }
+  return g_props;
+}
+}  // namespace
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return LUFQHE_SUCCESS;
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  return LUFQHE_ERR_CUDA;
+}
+
+int device_sm_count() {
+  int s = props().sms;
+  return s > 0 ? s : 1;
+}
+
+size_t device_smem_optin() { return props().smem_optin; }
+
+}  // namespace lufqhe
+
+using namespace lufqhe;
+
+namespace {
+
+int check_common(const void *A, int n, int lda, long long batch, const double *logabs,
+                 const char *fn) {
+  if (!A || !logabs || n < 1 || lda < n || batch < 0) {
+    set_error("%s: invalid argument (A=%p logabs=%p n=%d lda=%d batch=%lld)", fn, A,
+              (const void *)logabs, n, lda, batch);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (n > LUFQHE_MAX_N) {
+    set_error("%s: n=%d exceeds the supported maximum %d", fn, n, LUFQHE_MAX_N);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) {
+    set_error("%s: A must be 16-byte aligned", fn);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  return LUFQHE_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int dtype,
+                                    int mode, double *d_logabs, double *d_phase,
+                                    int8_t *d_parity, int32_t *d_status, void *stream) {
+  int rc = check_common(d_A, n, lda, batch, d_logabs, "lufqhe_batch_lup_det");
+  if (rc) return rc;
+  if (dtype != LUFQHE_C128) {
+    set_error("lufqhe_batch_lup_det: dtype %d not supported (complex128 only)", dtype);
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const double2 *A = reinterpret_cast<const double2 *>(d_A);
+  switch (mode) {
+    case LUFQHE_MODE_PLAIN_FP64:
+      return launch_plain(A, nullptr, n, lda, batch, ARITH_REF, d_logabs, d_phase, d_parity,
+                          d_status, s);
+    case LUFQHE_MODE_PLAIN_FP64_FUSED:
+      return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, d_logabs, d_phase, d_parity,
+                          d_status, s);
+    case LUFQHE_MODE_MIXED:
+      return launch_mixed(A, n, lda, batch, d_logabs, d_phase, d_parity, d_status, s);
+    default:
+      set_error("lufqhe_batch_lup_det: unknown mode %d", mode);
+      return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+}
+
+extern "C" int lufqhe_batch_lup_factor_inplace(void *d_A, int n, int lda, long long batch,
+                                               int mode, double *d_logabs, double *d_phase,
+                                               int8_t *d_parity, int32_t *d_status,
+                                               void *stream) {
+  int rc = check_common(d_A, n, lda, batch, d_logabs, "lufqhe_batch_lup_factor_inplace");
+  if (rc) return rc;
+  if (mode != LUFQHE_MODE_PLAIN_FP64 && mode != LUFQHE_MODE_PLAIN_FP64_FUSED) {
+    set_error("lufqhe_batch_lup_factor_inplace: mode %d has no in-place form", mode);
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  double2 *A = reinterpret_cast<double2 *>(d_A);
+  return launch_plain(A, A, n, lda, batch,
+                      mode == LUFQHE_MODE_PLAIN_FP64 ? ARITH_REF : ARITH_FUSED, d_logabs,
+                      d_phase, d_parity, d_status, (cudaStream_t)stream);
+}
+
+extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, int load_size,
+                                     int pair_product, void *stream) {
+  if (!d_matrices || n_mat < 0 || mat_side < 1 || load_size < mat_side) {
+    set_error("lufqhe_lucoregpu_call: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (mat_side > LUFQHE_MAX_N) {
+    set_error("lufqhe_lucoregpu_call: matSide=%d exceeds %d", mat_side, LUFQHE_MAX_N);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  if (n_mat == 0) return LUFQHE_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  // Per-matrix results live in stream-ordered temporaries; the reference keeps
+  // them in the matrices themselves (element (0,0)), which is also the output here.
+  void *tmp = nullptr;
+  size_t bytes = (size_t)n_mat * (2 * sizeof(double) + sizeof(int32_t));
+  int rc = check_cuda(cudaMallocAsync(&tmp, bytes, s), "cudaMallocAsync");
+  if (rc) return rc;
+  double *la = static_cast<double *>(tmp);
+  double *ph = la + n_mat;
+  int32_t *st = reinterpret_cast<int32_t *>(ph + n_mat);
+  double2 *A = reinterpret_cast<double2 *>(d_matrices);
+  rc = launch_plain(A, A, mat_side, load_size, n_mat, ARITH_REF, la, ph, nullptr, st, s);
+  if (!rc) rc = launch_write_det(A, mat_side, load_size, n_mat, la, ph, st, pair_product, s);
+  int rc2 = check_cuda(cudaFreeAsync(tmp, s), "cudaFreeAsync");
+  return rc ? rc : rc2;
+}
+
+namespace lufqhe {
+extern float g_mixed_theta;
+}
+
+extern "C" int lufqhe_set_option(int option, double value) {
+  if (option == LUFQHE_OPT_MIXED_THRESHOLD) {
+    if (!(value >= 0.0)) {
+      set_error("lufqhe_set_option: threshold must be >= 0");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_mixed_theta = (float)value;
+    return LUFQHE_SUCCESS;
+  }
+  set_error("lufqhe_set_option: unknown option %d", option);
+  return LUFQHE_ERR_INVALID_ARG;
+}
+
+extern "C" double lufqhe_get_option(int option) {
+  if (option == LUFQHE_OPT_MIXED_THRESHOLD) return (double)g_mixed_theta;
+  return NAN;
+}
+
+extern "C" size_t lufqhe_workspace_bytes(int n, long long batch, int mode) {
+  (void)n;
+  (void)batch;
+  (void)mode;
+  return 0;
+}
+
+extern "C" const char *lufqhe_last_error(void) { return g_err; }
+
+extern "C" const char *lufqhe_version(void) { return "0.1.0"; }

@@ -1,0 +1,150 @@
+// Plain FP64 batched complex LUP determinant.
+//
+// One warp factorises one matrix at a time, looping over the batch with a
+// grid stride. The matrix sits in shared memory (row stride n+1 complex so a
+// column read by 32 lanes hits 32 different banks); the right-looking update
+// of the (n-1-j)^2 trailing block is spread over all 32 lanes, so the FP64
+// pipe runs with full lanes until the block is smaller than a warp. The
+// factorisation itself (pivot rule, arithmetic) lives in lup_fp64.cuh.
+// The determinant is returned in log-polar form: the reference multiplies the
+// diagonal directly (LU-fqhe/src/LUCoreCPU.cu:256-265), which overflows for
+// lowest-Landau-level matrices.
+
+#include <cmath>
+
+#include "lup_fp64.cuh"
+
+namespace lufqhe {
+
+namespace {
+
+constexpr int kMaxWarpsPlain = 8;
+
+template <int ARITH>
+__global__ void __launch_bounds__(kMaxWarpsPlain * 32)
+    lup_plain_kernel(const double2 *__restrict__ A, double2 *__restrict__ Aout, int n, int lda,
+                     long long batch, double *__restrict__ logabs, double *__restrict__ phase,
+                     int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int lds = n + 1;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
+  double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
+                                            (size_t)warps * n * lds) +
+                 warp * n;
+  const int nn = n * n;
+
+  for (long long b = (long long)blockIdx.x * warps + warp; b < batch;
+       b += (long long)gridDim.x * warps) {
+    __syncwarp();
+    int par = 0;
+    int st = load_matrix_fp64(A + (size_t)b * n * lda, n, lda, M, lds, lane)
+                 ? LUFQHE_ST_NONFINITE
+                 : 0;
+    if (!st) st = lup_fp64_warp<ARITH>(M, lds, hold, n, lane, &par);
+
+    double la, ph;
+    if (st == 0) {
+      logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+    } else if (st == LUFQHE_ST_SINGULAR) {
+      la = -INFINITY;
+      ph = 0.0;
+    } else {
+      la = NAN;
+      ph = NAN;
+      par = 0;
+    }
+
+    if (Aout && (st == 0 || st == LUFQHE_ST_SINGULAR)) {
+      double2 *dst = Aout + (size_t)b * n * lda;
+      BlockWalk w(lane, n);
+      for (int e = lane; e < nn; e += 32) {
+        dst[(size_t)w.i * lda + w.k] = M[w.i * lds + w.k];
+        w.next(n);
+      }
+    }
+    if (lane == 0) {
+      logabs[b] = la;
+      if (phase) phase[b] = ph;
+      if (parity) parity[b] = (int8_t)par;
+      if (status) status[b] = st;
+    }
+  }
+}
+
+// Writes exp(logabs + i*phase) into element (0,0); with pair_product the even
+// matrix of each pair gets the product of the pair's determinants
+// (LU-fqhe/src/LUCoreGPU.cu:403-435).
+__global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
+                                 const double *logabs, const double *phase,
+                                 const int32_t *status, int pair_product) {
+  long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double la = logabs[b], ph = phase[b];
+  if (pair_product && (b % 2 == 0) && b + 1 < batch) {
+    la += logabs[b + 1];
+    ph += phase[b + 1];
+  }
+  double2 v;
+  if (la != la || ph != ph) {
+    v = make_double2(NAN, NAN);
+  } else {
+    double m = exp(la);
+    double s, c;
+    sincos(ph, &s, &c);
+    v = make_double2(m * c, m * s);
+  }
+  A[(size_t)b * n * lda] = v;
+}
+
+}  // namespace
+
+size_t plain_smem_per_warp(int n) {
+  return (size_t)n * (n + 1) * sizeof(double2) + (size_t)n * sizeof(double);
+}
+
+int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,
+                 double *logabs, double *phase, int8_t *parity, int32_t *status,
+                 cudaStream_t stream) {
+  if (batch == 0) return LUFQHE_SUCCESS;
+  const size_t per_warp = plain_smem_per_warp(n);
+  const size_t optin = device_smem_optin();
+  int warps = (int)(optin / per_warp);
+  if (warps > 4) warps = 4;
+  if (warps < 1) {
+    set_error("n=%d needs %zu bytes of shared memory per matrix; the device offers %zu", n,
+              per_warp, optin);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  const size_t smem = per_warp * warps;
+  auto kern = arith == ARITH_REF ? lup_plain_kernel<ARITH_REF> : lup_plain_kernel<ARITH_FUSED>;
+  int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
+                      "cudaFuncSetAttribute(plain)");
+  if (rc) return rc;
+  int per_sm = 0;
+  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
+                  "occupancy(plain)");
+  if (rc) return rc;
+  if (per_sm < 1) per_sm = 1;
+  long long want = (batch + warps - 1) / warps;
+  long long cap = (long long)device_sm_count() * per_sm;
+  int grid = (int)(want < cap ? want : cap);
+  kern<<<grid, warps * 32, smem, stream>>>(A, Aout, n, lda, batch, logabs, phase, parity, status);
+  return check_cuda(cudaGetLastError(), "lup_plain_kernel launch");
+}
+
+int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,
+                     const double *phase, const int32_t *status, int pair_product,
+                     cudaStream_t stream) {
+  if (batch == 0) return LUFQHE_SUCCESS;
+  int threads = 256;
+  long long blocks = (batch + threads - 1) / threads;
+  write_det_kernel<<<(unsigned)blocks, threads, 0, stream>>>(A, n, lda, batch, logabs, phase,
+                                                             status, pair_product);
+  return check_cuda(cudaGetLastError(), "write_det_kernel launch");
+}
+
+}  // namespace lufqhe

@@ -1,0 +1,82 @@
+"""CPU checks of the C-ABI library: it loads, exports every declared symbol,
+rejects bad arguments before touching a device, and its host generators are
+deterministic. No compute call runs here."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def test_exports_match_header(lufqhe_mod):
+    from lufqhe import _native
+    lib = lufqhe_mod.lib()
+    declared = _native.header_functions()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/lufqhe.h but not exported"
+        assert name in _native.SIGNATURES, f"{name} has no ctypes signature"
+    for name in _native.SIGNATURES:
+        assert name in declared, f"{name} bound but not declared"
+
+
+def test_header_constants_match_python(lufqhe_mod):
+    from lufqhe import _native
+    c = _native.header_constants()
+    assert c["LUFQHE_MODE_PLAIN_FP64"] == lufqhe_mod.MODE_PLAIN_FP64
+    assert c["LUFQHE_MODE_PLAIN_FP64_FUSED"] == lufqhe_mod.MODE_PLAIN_FP64_FUSED
+    assert c["LUFQHE_MODE_MIXED"] == lufqhe_mod.MODE_MIXED
+    assert c["LUFQHE_ST_SINGULAR"] == lufqhe_mod.ST_SINGULAR
+    assert c["LUFQHE_ST_FALLBACK"] == lufqhe_mod.ST_FALLBACK
+    assert c["LUFQHE_MAX_N"] == lufqhe_mod.MAX_N
+
+
+def test_version_and_error_string(lufqhe_mod):
+    lib = lufqhe_mod.lib()
+    assert lib.lufqhe_version().decode().count(".") == 2
+    assert isinstance(lib.lufqhe_last_error(), bytes)
+
+
+FAKE = ctypes.c_void_p(0x1000)   # never dereferenced: validation fails first
+FAKE_ODD = ctypes.c_void_p(0x1008)
+
+
+@pytest.mark.parametrize("args,code", [
+    ((None, 8, 8, 4, 0, 0, FAKE, None, None, None, None), -1),     # null A
+    ((FAKE, 8, 8, 4, 0, 0, None, None, None, None, None), -1),     # null logabs
+    ((FAKE, 0, 8, 4, 0, 0, FAKE, None, None, None, None), -1),     # n < 1
+    ((FAKE, 8, 7, 4, 0, 0, FAKE, None, None, None, None), -1),     # lda < n
+    ((FAKE, 8, 8, -1, 0, 0, FAKE, None, None, None, None), -1),    # batch < 0
+    ((FAKE, 65, 65, 4, 0, 0, FAKE, None, None, None, None), -2),   # n too large
+    ((FAKE_ODD, 8, 8, 4, 0, 0, FAKE, None, None, None, None), -1),  # misaligned
+    ((FAKE, 8, 8, 4, 1, 0, FAKE, None, None, None, None), -4),     # complex64 not offered
+    ((FAKE, 8, 8, 4, 0, 9, FAKE, None, None, None, None), -4),     # unknown mode
+])
+def test_argument_validation(lufqhe_mod, args, code):
+    lib = lufqhe_mod.lib()
+    assert lib.lufqhe_batch_lup_det(*args) == code
+    assert len(lib.lufqhe_last_error()) > 0
+
+
+def test_inplace_rejects_mixed(lufqhe_mod):
+    lib = lufqhe_mod.lib()
+    rc = lib.lufqhe_batch_lup_factor_inplace(FAKE, 8, 8, 4, 2, FAKE, None, None, None, None)
+    assert rc == -4
+
+
+def test_host_generators_deterministic(lufqhe_mod):
+    a = lufqhe_mod.gen_gaussian_host(64, 8, seed=0)
+    b = lufqhe_mod.gen_gaussian_host(64, 8, seed=0)
+    c = lufqhe_mod.gen_gaussian_host(64, 8, seed=1)
+    assert (a == b).all() and not (a == c).all()
+    # Re, Im ~ N(0, 1/2)
+    assert abs(a.real.var() - 0.5) < 0.05 and abs(a.imag.var() - 0.5) < 0.05
+    assert abs(a.mean()) < 0.05
+
+
+def test_host_lll_structure(lufqhe_mod):
+    n = 12
+    A, z = lufqhe_mod.gen_lll_host(16, n, seed=3)
+    w = np.exp(-np.abs(z) ** 2 / 4)
+    want = z[:, :, None] ** np.arange(n)[None, None, :] * w[:, :, None]
+    assert np.abs(A - want).max() / np.abs(want).max() < 1e-12
+    assert abs((np.abs(z) ** 2).mean() - n) < 0.25 * n

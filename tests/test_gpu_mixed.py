@@ -1,0 +1,123 @@
+"""GPU accuracy of the mixed-precision mode (FP32 LUP + FP64-accurate
+correction + FP64 fallback) against the double-double truth oracle.
+
+Tolerance: relative log|det| error <= 1e-10 (relative to max(1, |log|det||))
+and phase error <= 1e-10 rad for every matrix the mixed path accepts; fallback
+matrices carry the FP64 fused result bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_MIXED = 1e-10
+
+
+def rel(a, b):
+    return np.abs(a - b) / np.maximum(1.0, np.abs(b))
+
+
+def dphase(a, b):
+    return np.abs(np.angle(np.exp(1j * (a - b))))
+
+
+def host(out):
+    return {k: getattr(out, k).cpu().numpy() for k in ("logabs", "phase", "parity", "status")}
+
+
+@pytest.fixture
+def threshold(lufqhe_mod):
+    lib = lufqhe_mod.lib()
+    old = lib.lufqhe_get_option(1)
+    yield lambda v: lib.lufqhe_set_option(1, v)
+    lib.lufqhe_set_option(1, old)
+
+
+def check_mixed(lufqhe_mod, oracle, A, max_fallback_frac):
+    out = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    A_np = A.cpu().numpy()
+    la, ph, st = oracle.logdet_dd(A_np)
+    ok = out["status"] == 0
+    fb = (out["status"] & lufqhe_mod.ST_FALLBACK) != 0
+    assert (ok | fb).all(), f"unexpected status {np.unique(out['status'])}"
+    assert fb.mean() <= max_fallback_frac, f"fallback fraction {fb.mean()}"
+    assert rel(out["logabs"][ok], la[ok]).max(initial=0) < TOL_MIXED
+    assert dphase(out["phase"][ok], ph[ok]).max(initial=0) < TOL_MIXED
+    if fb.any():
+        fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
+        assert (out["logabs"][fb] == fused["logabs"][fb]).all()
+        assert (out["phase"][fb] == fused["phase"][fb]).all()
+    return out
+
+
+def test_config2_gaussian_n16(cuda, lufqhe_mod, oracle):
+    """Complex Gaussian n=16, seed 1 (a 8192-matrix slice of the 65536 batch)."""
+    A = lufqhe_mod.gen_gaussian(8192, 16, seed=1)
+    out = check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.001)
+    assert (out["status"] == 0).mean() > 0.999
+
+
+def test_config3_lll_n24(cuda, lufqhe_mod, oracle):
+    """Lowest-Landau-level orbital matrices n=24, z ~ CN(0, 24)."""
+    A, _ = lufqhe_mod.gen_lll(4096, 24, seed=2)
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.10)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 6, 8, 12, 17, 31, 32, 33, 48, 64])
+def test_sizes_gaussian(cuda, lufqhe_mod, oracle, n):
+    A = lufqhe_mod.gen_gaussian(300, n, seed=50 + n)
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.02)
+
+
+@pytest.mark.parametrize("n", [6, 8, 12, 16, 32, 48])
+def test_sizes_lll(cuda, lufqhe_mod, oracle, n):
+    A, _ = lufqhe_mod.gen_lll(512, n, seed=70 + n)
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.6)
+
+
+def test_wide_dynamic_range_equilibration(cuda, lufqhe_mod, oracle):
+    """Rows and columns scaled by 2^+-300: FP32 alone would overflow/underflow."""
+    rng = np.random.default_rng(9)
+    n, b = 20, 200
+    G = (rng.standard_normal((b, n, n)) + 1j * rng.standard_normal((b, n, n))) / math.sqrt(2)
+    r = 2.0 ** rng.integers(-300, 300, (b, n, 1))
+    c = 2.0 ** rng.integers(-300, 300, (b, 1, n))
+    A_np = G * r * c
+    A = cuda.from_numpy(A_np).cuda()
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.02)
+
+
+def test_zero_threshold_sends_all_to_fp64(cuda, lufqhe_mod, threshold):
+    A, _ = lufqhe_mod.gen_lll(1000, 16, seed=5)
+    threshold(0.0)
+    out = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
+    assert (out["status"] == lufqhe_mod.ST_FALLBACK).all()
+    assert (out["logabs"] == fused["logabs"]).all() and (out["phase"] == fused["phase"]).all()
+    assert (out["parity"] == fused["parity"]).all()
+
+
+def test_singular_and_nonfinite(cuda, lufqhe_mod):
+    n = 6
+    A_np = np.tile(np.eye(n, dtype=np.complex128), (3, 1, 1))
+    A_np[0, 2] = A_np[0, 1]          # duplicate rows: singular in FP32 and FP64
+    A_np[1, 3, 3] = np.nan
+    A = cuda.from_numpy(A_np).cuda()
+    out = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    assert out["status"][0] == (lufqhe_mod.ST_SINGULAR | lufqhe_mod.ST_FALLBACK)
+    assert out["logabs"][0] == -np.inf
+    assert out["status"][1] == lufqhe_mod.ST_NONFINITE
+    assert out["status"][2] == 0 and abs(out["logabs"][2]) < 1e-14
+
+
+def test_mixed_deterministic_across_batch_positions(cuda, lufqhe_mod):
+    """The same matrix gives the same result wherever it sits in the batch."""
+    A, _ = lufqhe_mod.gen_lll(97, 24, seed=6)
+    full = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    for idx in (0, 31, 32, 96):
+        one = host(lufqhe_mod.batch_lup_det(A[idx:idx + 1].contiguous(),
+                                            mode=lufqhe_mod.MODE_MIXED))
+        assert one["logabs"][0] == full["logabs"][idx]
+        assert one["phase"][0] == full["phase"][idx]
