@@ -62,7 +62,7 @@ namespace {
 
 int check_common(const void *A, int n, int lda, long long batch, const double *logabs,
                  const char *fn) {
-  if (!A || !logabs || n < 1 || lda < n || batch < 0) {
+  if ((batch > 0 && (!A || !logabs)) || n < 1 || lda < n || batch < 0) {
     set_error("%s: invalid argument (A=%p logabs=%p n=%d lda=%d batch=%lld)", fn, A,
               (const void *)logabs, n, lda, batch);
     return LUFQHE_ERR_INVALID_ARG;
@@ -71,7 +71,7 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
     set_error("%s: n=%d exceeds the supported maximum %d", fn, n, LUFQHE_MAX_N);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
-  if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) {
+  if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) {  // complex128 alignment
     set_error("%s: A must be 16-byte aligned", fn);
     return LUFQHE_ERR_INVALID_ARG;
   }

@@ -54,18 +54,50 @@ __device__ __forceinline__ bool load_matrix_fp64(const double2 *__restrict__ src
   return bad;
 }
 
-// Factor M in place. Returns 0, LUFQHE_ST_SCALE_TINY or LUFQHE_ST_SINGULAR
+// RN(a / b) for b > 0 given y = RN(1/b): Markstein's correction (P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990): q0 = RN(a*y) is refined once to a faithful
+// q1, then q2 = RN(q1 + RN(a - b*q1)*y) is the correctly rounded quotient when
+// nothing over- or underflows. Outside the guarded ranges, and for a = 0, the
+// quotient is taken from the hardware-independent IEEE division instead, so
+// every result equals the correctly rounded a / b.
+__device__ __forceinline__ double div_rn_markstein(double a, double b, double y, bool b_safe) {
+  const long long lo = 0x0370000000000000ll;  // 2^-968
+  const long long hi = 0x7c70000000000000ll;  // 2^+968
+  const long long ab = abs_bits(a);
+  if (ab == 0) return __dmul_rn(a, y);         // signed zero, exact
+  if (!b_safe || ab < lo || ab > hi) return __ddiv_rn(a, b);
+  const double q0 = __dmul_rn(a, y);
+  const long long qb = abs_bits(q0);
+  if (qb < lo || qb > hi) return __ddiv_rn(a, b);
+  const double r0 = __fma_rn(-b, q0, a);
+  const double q1 = __fma_rn(r0, y, q0);
+  const double r1 = __fma_rn(-b, q1, a);
+  return __fma_rn(r1, y, q1);
+}
+
+// Factor M in place. hold has 2n doubles: the row scales holder_i and their
+// reciprocals. Returns 0, LUFQHE_ST_SCALE_TINY or LUFQHE_ST_SINGULAR
 // (warp-uniform); *parity receives the swap count mod 2.
+//
+// Pivot search: the reference compares q_i = RN(|Re a_ij| / holder_i). The
+// kernel first ranks a_i = RN(|Re a_ij| * RN(1/holder_i)), whose relative
+// distance from q_i is below 3u (u = 2^-53). When the largest a_m beats every
+// other a_k by more than 16 ulps, RN(q_m) > RN(q_k) for all k, so m is the
+// reference's choice; otherwise (near-ties, zero or extreme quotients) the
+// exact quotients are computed and compared with the reference's rule.
 template <int ARITH>
 __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane, int *parity) {
   int par = 0;
+  double *rhold = hold + n;
   {
     bool tiny = false;
     const long long tiny_bits = __double_as_longlong(1e-24);
     for (int i = lane; i < n; i += 32) {
       long long big = 0;
       for (int k = 0; k < n; ++k) big = max(big, abs_bits(M[i * lds + k].x));
-      hold[i] = __longlong_as_double(big);
+      const double h = __longlong_as_double(big);
+      hold[i] = h;
+      rhold[i] = __drcp_rn(h);
       tiny |= big < tiny_bits;
     }
     if (__any_sync(kFull, tiny)) {
@@ -74,14 +106,15 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
     }
     __syncwarp();
   }
+  const long long safe_lo = 0x0170000000000000ll;  // 2^-1000
+  const long long safe_hi = 0x7e70000000000000ll;  // 2^+1000
   for (int j = 0; j < n; ++j) {
-    // pivot: max of |Re a_ij| / holder_i over i >= j, ties to the larger i;
-    // a NaN quotient is never chosen (key -2 < initial -1).
+    // screened pivot search: approximate quotients, ties to the larger i
     long long bk = -1;
     int bi = j;
     for (int i = j + lane; i < n; i += 32) {
-      double q = __ddiv_rn(fabs(M[i * lds + j].x), hold[i]);
-      long long key = (q == q) ? __double_as_longlong(q) : -2ll;
+      double a = __dmul_rn(fabs(M[i * lds + j].x), rhold[i]);
+      long long key = (a == a) ? __double_as_longlong(a) : -2ll;
       if (key >= bk) {
         bk = key;
         bi = i;
@@ -96,6 +129,36 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
         bi = oi;
       }
     }
+    unsigned near = 0;
+    for (int i = j + lane; i < n; i += 32) {
+      double a = __dmul_rn(fabs(M[i * lds + j].x), rhold[i]);
+      long long key = (a == a) ? __double_as_longlong(a) : -2ll;
+      near += key >= bk - 16;
+    }
+    near = __reduce_add_sync(kFull, near);
+    if (near != 1 || bk < safe_lo || bk > safe_hi) {
+      // exact path: the reference's comparison on correctly rounded quotients;
+      // a NaN quotient is never chosen (key -2 < initial -1)
+      bk = -1;
+      bi = j;
+      for (int i = j + lane; i < n; i += 32) {
+        double q = __ddiv_rn(fabs(M[i * lds + j].x), hold[i]);
+        long long key = (q == q) ? __double_as_longlong(q) : -2ll;
+        if (key >= bk) {
+          bk = key;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        long long ok = __shfl_xor_sync(kFull, bk, off);
+        int oi = __shfl_xor_sync(kFull, bi, off);
+        if (ok > bk || (ok == bk && oi > bi)) {
+          bk = ok;
+          bi = oi;
+        }
+      }
+    }
     const int p = bi;
     if (p != j) {
       for (int k = lane; k < n; k += 32) {
@@ -103,7 +166,10 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
         M[p * lds + k] = M[j * lds + k];
         M[j * lds + k] = t;
       }
-      if (lane == 0) hold[p] = hold[j];
+      if (lane == 0) {
+        hold[p] = hold[j];
+        rhold[p] = rhold[j];
+      }
       par ^= 1;
     }
     __syncwarp();
@@ -113,9 +179,23 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
       return LUFQHE_ST_SINGULAR;
     }
     if (j == n - 1) break;
-    const double d = pivot_den<ARITH>(piv);
-    for (int i = j + 1 + lane; i < n; i += 32)
-      M[i * lds + j] = cdiv_pivot<ARITH>(M[i * lds + j], piv, d);
+    if (ARITH == ARITH_REF) {
+      const double den = pivot_den<ARITH_REF>(piv);
+      const double y = __drcp_rn(den);
+      const long long db = abs_bits(den);
+      const bool den_safe = db >= 0x03f0000000000000ll && db <= 0x7bf0000000000000ll;  // [2^-960, 2^960]
+      for (int i = j + 1 + lane; i < n; i += 32) {
+        const double2 a = M[i * lds + j];
+        const double nx = __dadd_rn(__dmul_rn(a.x, piv.x), __dmul_rn(a.y, piv.y));
+        const double ny = __dsub_rn(__dmul_rn(a.y, piv.x), __dmul_rn(a.x, piv.y));
+        M[i * lds + j] = make_double2(div_rn_markstein(nx, den, y, den_safe),
+                                      div_rn_markstein(ny, den, y, den_safe));
+      }
+    } else {
+      const double d = pivot_den<ARITH>(piv);
+      for (int i = j + 1 + lane; i < n; i += 32)
+        M[i * lds + j] = cdiv_pivot<ARITH>(M[i * lds + j], piv, d);
+    }
     __syncwarp();
     // trailing update a_ik -= l_ij * u_jk on the m x m block
     const int m = n - 1 - j;

@@ -3,8 +3,8 @@
 // Per matrix (one warp, shared memory), with FP64 used only where accuracy
 // needs it and almost all arithmetic on the FP32 and integer pipes, which on
 // GB300 run far faster than FP64:
-//  1. power-of-two row/column equilibration A^ = D_r^-1 A D_c^-1, chosen from
-//     the exponent fields (exact; log|det D| is added back in FP64);
+//  1. power-of-two column-then-row equilibration A^ = D_r^-1 A D_c^-1, chosen
+//     from the exponent fields (exact; log|det D| is added back in FP64);
 //  2. split of every scaled FP64 entry into float hi + lo by integer
 //     operations (48 significant bits kept);
 //  3. FP32 complex LUP of hi with partial pivoting on |Re|+|Im|; alongside,
@@ -32,6 +32,12 @@ namespace lufqhe {
 namespace {
 
 constexpr int kMaxWarpsMixed = 8;
+// ||E||_F / max(1, |log|det||) above which the correction may miss 1e-10
+// relative accuracy. E comes from FP32 triangular solves, whose rounding
+// leaves an absolute error of about 1e-6 * ||E||_F in log det(I + E)
+// (measured on lowest-Landau-level matrices against a double-double oracle);
+// 8e-5 keeps that below ~1e-10 relative with margin.
+constexpr float kCorrRelCap = 8e-5f;
 
 // ---- float-float building blocks (never contracted: explicit _rn ops) ------
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -174,7 +180,7 @@ __device__ __forceinline__ CFF shfl_cff(const CFF &a, int src_or_mask, bool xor_
 struct MixedSmem {
   float2 *Af;   // FP32 working matrix -> L\U          [n][lds]
   float4 *SC;   // residual sum (xy) + compensation (zw); also double2 A [n][lds]
-  double *hold; // FP64 fallback row scales [n]
+  double *hold; // FP64 fallback row scales and their reciprocals [2n]
   int *er;      // row exponents [n]
   int *ec;      // column exponents [n]
 };
@@ -187,25 +193,26 @@ __device__ bool mixed_factor(const MixedSmem &S, int n, int lane, float theta2, 
   const int nn = n * n;
   double2 *A = reinterpret_cast<double2 *>(S.SC);
 
-  // 1. exponents
+  // 1. exponents: columns first (for orbital matrices the columns carry the
+  //    |z|^m scales), then rows of the column-scaled matrix
   int rsum = 0, csum = 0;
-  for (int i = lane; i < n; i += 32) {
-    int m = -2000;
-    for (int k = 0; k < n; ++k) m = max(m, cexp_field(A[i * lds + k]));
-    if (m == -2000) m = 0;
-    S.er[i] = m;
-    rsum += m;
-  }
-  __syncwarp();
   for (int k = lane; k < n; k += 32) {
     int m = -2000;
-    for (int i = 0; i < n; ++i) {
-      int e = cexp_field(A[i * lds + k]);
-      if (e != -2000) m = max(m, e - S.er[i]);
-    }
+    for (int i = 0; i < n; ++i) m = max(m, cexp_field(A[i * lds + k]));
     if (m == -2000) m = 0;
     S.ec[k] = m;
     csum += m;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) {
+    int m = -2000;
+    for (int k = 0; k < n; ++k) {
+      int e = cexp_field(A[i * lds + k]);
+      if (e != -2000) m = max(m, e - S.ec[k]);
+    }
+    if (m == -2000) m = 0;
+    S.er[i] = m;
+    rsum += m;
   }
   __syncwarp();
   // 2. split into hi (Af) and hi + lo (SC as s + c); same lane reads and writes
@@ -336,7 +343,24 @@ __device__ bool mixed_factor(const MixedSmem &S, int n, int lane, float theta2, 
     __syncwarp();
   }
 
-  // threshold on ||E||_F (decision taken from lane 0's sum: warp-uniform)
+  // 6 (first half). complex float-float product of the diagonal of U; its
+  // exponent gives log2|det| to within 2 before the correction is accepted
+  {
+    CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+    for (int t = lane; t < n; t += 32) {
+      float2 u = S.Af[t * lds + t];
+      CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
+      ff_renorm(v);
+      acc = ff_cmul(acc, v);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
+    prod = shfl_cff(acc, 0, false);
+  }
+
+  // acceptance: ||E||_F <= theta, and the FP32 evaluation of log det(I+E)
+  // (error ~ eps32 * ||E||_F) small against 1e-11 * max(1, |log|det||).
+  // Decided on lane 0's sum so it is warp-uniform.
   {
     float f = 0.0f;
     BlockWalk w(lane, n);
@@ -348,18 +372,16 @@ __device__ bool mixed_factor(const MixedSmem &S, int n, int lane, float theta2, 
 #pragma unroll
     for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
     f = __shfl_sync(kFull, f, 0);
-    if (!(f <= theta2)) return false;
+    const float la_est = fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
+    const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
+    if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
   }
 
-  // 5. log det(I + E): unpivoted LU with the identity implicit
-  float cre = 0.0f, cim = 0.0f;
-  for (int t = 0; t < n; ++t) {
+  // 5. log det(I + E): unpivoted LU with the identity implicit; the pivots
+  //    1 + d_t stay on the diagonal and their logs are taken lane-parallel.
+  for (int t = 0; t + 1 < n; ++t) {
     const float2 d = R[2 * (t * lds + t)];
-    const float2 piv = make_float2(1.0f + d.x, d.y);
-    cre += 0.5f * log1pf(__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, 2.0f * d.x)));
-    cim += atan2f(d.y, 1.0f + d.x);
-    if (t == n - 1) break;
-    const float2 r = crcpf(piv);
+    const float2 r = crcpf(make_float2(1.0f + d.x, d.y));
     for (int i = t + 1 + lane; i < n; i += 32)
       R[2 * (i * lds + t)] = cmulf(R[2 * (i * lds + t)], r);
     __syncwarp();
@@ -373,19 +395,21 @@ __device__ bool mixed_factor(const MixedSmem &S, int n, int lane, float theta2, 
     }
     __syncwarp();
   }
-  corr = make_float2(cre, cim);
-
-  // 6. complex float-float product of the diagonal of U
-  CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+  float cre = 0.0f, cim = 0.0f;
   for (int t = lane; t < n; t += 32) {
-    float2 u = S.Af[t * lds + t];
-    CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
-    ff_renorm(v);
-    acc = ff_cmul(acc, v);
+    const float2 d = R[2 * (t * lds + t)];
+    cre += 0.5f * log1pf(__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, 2.0f * d.x)));
+    cim += atan2f(d.y, 1.0f + d.x);
   }
 #pragma unroll
-  for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
-  prod = shfl_cff(acc, 0, false);
+  for (int off = 16; off; off >>= 1) {
+    cre += __shfl_xor_sync(kFull, cre, off);
+    cim += __shfl_xor_sync(kFull, cim, off);
+  }
+  cre = __shfl_sync(kFull, cre, 0);
+  cim = __shfl_sync(kFull, cim, 0);
+  corr = make_float2(cre, cim);
+
   return true;
 }
 
@@ -405,8 +429,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
   base += warps * nl * sizeof(float4);
   S.Af = reinterpret_cast<float2 *>(base) + warp * nl;
   base += warps * nl * sizeof(float2);
-  S.hold = reinterpret_cast<double *>(base) + warp * n;
-  base += warps * (size_t)n * sizeof(double);
+  S.hold = reinterpret_cast<double *>(base) + warp * 2 * n;
+  base += warps * 2 * (size_t)n * sizeof(double);
   S.er = reinterpret_cast<int *>(base) + warp * 2 * n;
   S.ec = S.er + n;
 
@@ -489,7 +513,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
 
 size_t mixed_smem_per_warp(int n) {
   const int lds = n + 1;
-  return (size_t)n * lds * (sizeof(float2) + sizeof(float4)) + (size_t)n * sizeof(double) +
+  return (size_t)n * lds * (sizeof(float2) + sizeof(float4)) + 2 * (size_t)n * sizeof(double) +
          2 * (size_t)n * sizeof(int);
 }
 

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
   double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
   double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
                                             (size_t)warps * n * lds) +
-                 warp * n;
+                 warp * 2 * n;
   const int nn = n * n;
 
   for (long long b = (long long)blockIdx.x * warps + warp; b < batch;
@@ -102,7 +102,7 @@ __global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
 }  // namespace
 
 size_t plain_smem_per_warp(int n) {
-  return (size_t)n * (n + 1) * sizeof(double2) + (size_t)n * sizeof(double);
+  return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
 }
 
 int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,

@@ -281,7 +281,13 @@ static inline cdd cdd_mul(cdd a, cdd b) {
   cdd r = {dd_sub(dd_mul(a.x, b.x), dd_mul(a.y, b.y)), dd_add(dd_mul(a.x, b.y), dd_mul(a.y, b.x))};
   return r;
 }
+static inline dd dd_ldexp(dd a, int e) { dd r = {ldexp(a.hi, e), ldexp(a.lo, e)}; return r; }
 static inline cdd cdd_div(cdd a, cdd b) {
+  /* scale both by 2^-e (exact) so |b|^2 cannot overflow or underflow */
+  int e;
+  frexp(fmax(fabs(b.x.hi), fabs(b.y.hi)), &e);
+  a.x = dd_ldexp(a.x, -e); a.y = dd_ldexp(a.y, -e);
+  b.x = dd_ldexp(b.x, -e); b.y = dd_ldexp(b.y, -e);
   dd den = dd_add(dd_mul(b.x, b.x), dd_mul(b.y, b.y));
   dd nx = dd_add(dd_mul(a.x, b.x), dd_mul(a.y, b.y));
   dd ny = dd_sub(dd_mul(a.y, b.x), dd_mul(a.x, b.y));
