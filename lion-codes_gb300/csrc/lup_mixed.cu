@@ -36,8 +36,8 @@ constexpr int kMaxWarpsMixed = 8;
 // relative accuracy. E comes from FP32 triangular solves, whose rounding
 // leaves an absolute error of about 1e-6 * ||E||_F in log det(I + E)
 // (measured on lowest-Landau-level matrices against a double-double oracle);
-// 8e-5 keeps that below ~1e-10 relative with margin.
-constexpr float kCorrRelCap = 8e-5f;
+// 5e-5 keeps that near 5e-11 relative, half the 1e-10 target.
+constexpr float kCorrRelCap = 5e-5f;
 
 // ---- float-float building blocks (never contracted: explicit _rn ops) ------
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
