@@ -105,6 +105,24 @@ int lufqhe_batch_lup_factor_inplace(void *d_A, int n, int lda, long long batch, 
 int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, int load_size,
                           int pair_product, void *stream);
 
+/*
+ * Same call as lufqhe_lucoregpu_call, for callers that cannot allocate device
+ * memory once they run (a fixed device-memory budget sized at start-up, an HBM
+ * admission figure, buffers owned by the caller's pool). No counterpart in the
+ * reference: the reference allocates nothing inside LUCoreGPU::CALL because it
+ * writes each determinant into its matrix, while this library keeps per-matrix
+ * log|det|, phase and status as temporaries. Here they live in a fixed
+ * 5 MiB file-scope device array held by every device that loads the library
+ * until exit; nMat above LUFQHE_NOALLOC_MAX_MATRICES is rejected with
+ * LUFQHE_ERR_INVALID_ARG. All calls share that array: calls whose kernels
+ * overlap on the GPU race, so order them (one stream). The array's address is
+ * looked up on the first call on each device; make that call before any
+ * stream capture.
+ */
+#define LUFQHE_NOALLOC_MAX_MATRICES 262144
+int lufqhe_lucoregpu_call_noalloc(void *d_matrices, int n_mat, int mat_side, int load_size,
+                                  int pair_product, void *stream);
+
 /* ---- on-device synthetic inputs (seeded; identical on every device) ---- */
 /* i.i.d. complex Gaussian entries, Re and Im ~ N(0, sigma^2/2). */
 int lufqhe_gen_gaussian(double *d_A, int n, int lda, long long batch, unsigned long long seed,

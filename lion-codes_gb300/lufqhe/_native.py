@@ -24,6 +24,7 @@ SIGNATURES = {
     "lufqhe_batch_lup_det": (I32, [P, I32, I32, I64, I32, I32, P, P, P, P, P]),
     "lufqhe_batch_lup_factor_inplace": (I32, [P, I32, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_lucoregpu_call": (I32, [P, I32, I32, I32, I32, P]),
+    "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_gen_gaussian": (I32, [P, I32, I32, I64, U64, F64, P]),
     "lufqhe_gen_lll": (I32, [P, P, I32, I32, I64, U64, F64, P]),
     "lufqhe_gen_gaussian_host": (I32, [P, I32, I32, I64, U64, F64]),
