@@ -37,7 +37,10 @@ WORKLOADS = {
     "lll24": ("lll", 24, 32768, 2),
     "gauss16": ("gauss", 16, 65536, 1),
     "gauss8": ("gauss", 8, 4096, 0),
+    # 200000 LLL matrices, n uniform over MIXED_SIZES, one persistent launch
+    "mixedn": ("mixed", 0, 200000, 4),
 }
+MIXED_SIZES = (6, 8, 12, 16, 24, 32, 48)
 
 
 def flops_per_matrix(n: int) -> float:
@@ -227,6 +230,143 @@ def time_device(torch, lufqhe, A, mode, out, steps, warmup, stream):
     return e0.elapsed_time(e1) / steps
 
 
+def run_mixedn(args, world, rank, local):
+    """Mixed-size batch: groups of LLL matrices, one persistent launch replayed
+    from a CUDA graph, tile sizes and warps per CTA from the autotuner."""
+    import numpy as np
+    import torch
+
+    import lufqhe
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    _, _, total, seed = WORKLOADS["mixedn"]
+    counts = np.random.default_rng(seed).multinomial(total, [1.0 / len(MIXED_SIZES)] * len(MIXED_SIZES))
+    groups, off = [], 0
+    with torch.cuda.stream(stream):
+        for n, c in zip(MIXED_SIZES, counts):
+            A, _ = lufqhe.gen_lll(int(c), n, seed=seed * 100 + n, sigma=math.sqrt(n))
+            groups.append((A, off))
+            off += int(c)
+    torch.cuda.synchronize()
+
+    def alloc():
+        return lufqhe.DetResult(torch.empty(total, dtype=torch.float64, device=dev),
+                                torch.empty(total, dtype=torch.float64, device=dev),
+                                torch.empty(total, dtype=torch.int8, device=dev),
+                                torch.empty(total, dtype=torch.int32, device=dev))
+
+    out = alloc()
+    plan = lufqhe.Plan(groups, out, mode=lufqhe.MODE_MIXED, autotune=True, stream=stream)
+    tune = plan.describe()
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    ms = timed(lambda: plan.execute(stream=stream), args.steps)
+    time.sleep(0.2)
+    clocks = sampler.stop()
+    ms_max = max_over_ranks(world, ms)
+    mixed_st = out.status.cpu().numpy()
+    mixed_la = out.logabs.cpu().numpy()
+
+    # the same batch as one plain FP64 (fused) persistent launch
+    out_p = alloc()
+    plan_p = lufqhe.Plan(groups, out_p, mode=lufqhe.MODE_PLAIN_FP64_FUSED, autotune=True,
+                         stream=stream)
+    ms_plain = timed(lambda: plan_p.execute(stream=stream), max(2, args.steps // 2))
+    plain_la = out_p.logabs.cpu().numpy()
+    # per-size throughput: each group as its own batched call
+    per_n = {}
+    for (A, o), n in zip(groups, MIXED_SIZES):
+        r = lufqhe.DetResult(out.logabs[o:o + A.shape[0]], out.phase[o:o + A.shape[0]],
+                             out.parity[o:o + A.shape[0]], out.status[o:o + A.shape[0]])
+        t = timed(lambda: lufqhe.batch_lup_det(A, mode=lufqhe.MODE_MIXED, stream=stream, out=r),
+                  max(2, args.steps // 4))
+        per_n[str(n)] = {"count": int(A.shape[0]), "dets_per_s": A.shape[0] / (t * 1e-3),
+                         "fallbacks": int(((mixed_st[o:o + A.shape[0]] & 8) != 0).sum())}
+    launches = args.steps + max(2, args.steps // 2) + len(groups) * max(2, args.steps // 4)
+
+    # e2e: host buffers in, graph replay, results out
+    hosts = [torch.empty(A.shape, dtype=A.dtype, pin_memory=True) for A, _ in groups]
+    for h, (A, _) in zip(hosts, groups):
+        h.copy_(A)
+    out_host = {k: torch.empty(total, dtype=getattr(out, k).dtype, pin_memory=True)
+                for k in ("logabs", "phase", "parity", "status")}
+
+    def e2e():
+        with torch.cuda.stream(stream):
+            for h, (A, _) in zip(hosts, groups):
+                A.copy_(h, non_blocking=True)
+            plan.execute(stream=stream)
+            for k, t in out_host.items():
+                t.copy_(getattr(out, k), non_blocking=True)
+
+    ms_e2e = max_over_ranks(world, timed(e2e, args.steps))
+    launches += args.steps
+    h2d = sum(h.numel() * h.element_size() for h in hosts)
+    d2h = sum(t.numel() * t.element_size() for t in out_host.values())
+    F = sum(flops_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
+    B = sum(bytes_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
+    pipes = measure_pipe_peaks(torch, lufqhe)
+    hbm_peak = load_peaks().get("hbm_gbs") or 6800.0
+    ok = (plain_la == plain_la) & (mixed_st == 0)
+    rel = np.abs(mixed_la[ok] - plain_la[ok]) / np.maximum(1.0, np.abs(plain_la[ok]))
+    if rank == 0:
+        line = {
+            "metric": "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)",
+            "value": world * total / (ms_max * 1e-3), "unit": "dets/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 in / fp32+float-float compute / f64 out",
+            "data": "synthetic (seeded, generated on device)",
+            "config": {"workload": f"mixedn: {total} LLL matrices, n uniform over "
+                                   f"{list(MIXED_SIZES)}, one persistent launch in a CUDA graph",
+                       "counts": {str(n): int(c) for n, c in zip(MIXED_SIZES, counts)},
+                       "l2": "inputs larger than L2 (no flush)"},
+            "plain_fp64_fused_persistent_dets_per_s": total / (ms_plain * 1e-3),
+            "mixed_over_plain_fused": ms_plain / ms,
+            "per_n": per_n,
+            "autotune": tune,
+            "accuracy_vs_plain_fp64": {"max_rel_logabs_err_accepted": float(rel.max(initial=0)),
+                                       "count_above_1e-10": int((rel > 1e-10).sum())},
+            "fallbacks": {"count": int(((mixed_st & 8) != 0).sum()), "of": total},
+            "e2e": {"value": world * total / (ms_e2e * 1e-3), "unit": "dets/s",
+                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"kernel": "grouped_kernel<MIXED>", "bound": "fp32",
+                         "achieved": F / (ms * 1e-3) * 1e-12, "peak": pipes.get("fp32_tflops"),
+                         "unit": "TFLOP/s",
+                         "frac": (F / (ms * 1e-3) * 1e-12 / pipes["fp32_tflops"])
+                         if pipes.get("fp32_tflops") else None,
+                         "traffic": ncu_traffic("grouped_kernel", "mixedn"),
+                         "hbm": {"achieved": B / (ms * 1e-3) * 1e-9, "peak": hbm_peak,
+                                 "unit": "GB/s", "frac": B / (ms * 1e-3) * 1e-9 / hbm_peak}},
+            "clocks": clocks,
+        }
+        import bench_cpu
+        A0 = groups[MIXED_SIZES.index(24)][0][:4096].cpu().numpy()
+        line["cpu_baseline"] = bench_cpu.cpu_baseline(np, A0, 24, seconds=args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    plan.close()
+    plan_p.close()
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -234,6 +374,8 @@ def run_ours(args):
     import lufqhe
 
     world, rank, local = dist_setup(args)
+    if args.workload == "mixedn":
+        return run_mixedn(args, world, rank, local)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
@@ -406,6 +548,8 @@ def run_reference(args):
         return lufqhe.gen_gaussian_host(count, n, seed=seed)
 
     kind, n, batch, seed = WORKLOADS[args.workload]
+    if kind == "mixed":  # the reference factorises one size at a time; time n=24
+        kind, n = "lll", 24
     line = bench_cpu.reference_arm(np, args, kind, n, batch, seed, make_inputs)
     line["n_gpus"] = world
     print(json.dumps(line), flush=True)

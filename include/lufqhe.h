@@ -123,6 +123,95 @@ int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, int load_si
 int lufqhe_lucoregpu_call_noalloc(void *d_matrices, int n_mat, int mat_side, int load_size,
                                   int pair_product, void *stream);
 
+/*
+ * Wavefunction sum over determinant pairs, S = sum_i det(A_2i) det(A_2i+1)
+ * for i < batch/2 (an odd last matrix is dropped, LU-fqhe/src/LUCoreCPU.cu:83),
+ * from log-polar determinants. Replaces the pair product in the LU kernel
+ * (LU-fqhe/src/LUCoreGPU.cu:403-425) plus LUCoreGPU::globalReduction
+ * (LU-fqhe/src/LUCoreGPU.cu:113-156). d_out receives log|S| and arg S (two
+ * doubles, device memory). One launch; reproducible order.
+ */
+int lufqhe_pair_sum(const double *d_logabs, const double *d_phase, long long batch, double *d_out,
+                    void *stream);
+
+/* ---- mixed-size batches: one persistent launch, autotuned, graph-captured ---- */
+/* One group of same-size matrices of a mixed-size batch. Its results go to
+ * indices out_offset .. out_offset + count - 1 of the output arrays. */
+typedef struct {
+  const void *A;        /* device pointer, complex128, layout as above */
+  int n;
+  int lda;
+  long long count;
+  long long out_offset;
+} lufqhe_group_t;
+
+typedef struct lufqhe_plan_s lufqhe_plan_t;
+
+/* Tune tile sizes per n and warps per CTA by timing candidate launches. */
+#define LUFQHE_PLAN_AUTOTUNE 1
+
+/*
+ * Build a plan for fixed groups and output buffers (device pointers, length =
+ * max out_offset + count). The work list (tiles of same-n matrices, largest n
+ * first) and a CUDA graph of the persistent launch are made once; the input
+ * matrices may change between executions, their addresses may not. The
+ * reference factorises one size per CALL (LU-fqhe/src/LUCoreGPU.cu:38-106);
+ * this has no counterpart there. Synchronises `stream` while building.
+ */
+int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *groups, int ngroups, int mode,
+                       double *d_logabs, double *d_phase, int8_t *d_parity, int32_t *d_status,
+                       int flags, void *stream);
+/* Replay the captured graph on `stream` (asynchronous). */
+int lufqhe_plan_execute(lufqhe_plan_t *plan, void *stream);
+/* The same work as lufqhe_plan_execute, launched directly instead of via the graph. */
+int lufqhe_plan_launch_direct(lufqhe_plan_t *plan, void *stream);
+/* JSON text of the chosen tiles and launch shape (and tuning timings). */
+int lufqhe_plan_describe(const lufqhe_plan_t *plan, char *buf, size_t len);
+int lufqhe_plan_destroy(lufqhe_plan_t *plan);
+
+/* ---- serving: device-resident walkers and a persistent request loop ---- */
+/*
+ * A walker is k matrices of one size n, resident in HBM for its lifetime; each
+ * move resamples particle `particle` (new z per matrix), the GPU rebuilds that
+ * row of every matrix (M_ik = z^k exp(-|z|^2/4)) and recomputes the k
+ * determinants. One persistent kernel per size class polls a tile ring in
+ * mapped host memory (bounded waits; it exits after ~0.5 s idle and is
+ * relaunched on demand), so requests from many walkers share the GPU and
+ * overlap without a batch boundary. Walkers are admitted against the HBM
+ * budget. No counterpart in the reference, whose Monte Carlo loop re-sends
+ * and refactorises every matrix each step (LU-fqhe/src/MonteCarloLoop.cu:216-335).
+ */
+typedef struct lufqhe_server_s lufqhe_server_t;
+/* class_n: sizes served (8, 16, 32, 64); class_sms: SMs given to each (NULL =
+ * equal shares); max_k: most matrices per walker; tile: matrices per work tile.
+ * mode: LUFQHE_MODE_MIXED or LUFQHE_MODE_PLAIN_FP64_FUSED. */
+int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
+                         const int *class_n, const int *class_sms, int nclasses, int max_k,
+                         int tile);
+/* z_host: k*n complex128 particle coordinates. LUFQHE_ERR_BUSY when the HBM
+ * budget is exhausted. Synchronous (uploads and builds the matrices). */
+int lufqhe_server_walker_create(lufqhe_server_t *server, int n, int k, const double *z_host,
+                                int *walker_id);
+int lufqhe_server_walker_destroy(lufqhe_server_t *server, int walker_id);
+/* One move: znew_host holds the k new coordinates of `particle` (particle < 0
+ * recomputes the determinants without a move). LUFQHE_ERR_BUSY when the walker
+ * already has a move in flight or the request ring is full. */
+int lufqhe_server_submit(lufqhe_server_t *server, int walker_id, int particle,
+                         const double *znew_host, long long *ticket);
+/* 0 = done (k results copied to the host arrays if given), LUFQHE_ERR_BUSY =
+ * not yet (wait_us = 0), LUFQHE_ERR_TIMEOUT = not within wait_us. */
+int lufqhe_server_poll(lufqhe_server_t *server, long long ticket, int wait_us, double *logabs,
+                       double *phase, int32_t *status);
+int lufqhe_server_destroy(lufqhe_server_t *server);
+/* Simulated walker stream: Poisson move arrivals at rate_hz, k log-uniform in
+ * [k_min, k_max], n uniform over the classes, `moves` moves per walker.
+ * Writes per-request latency (us, arrival to completion) and n; returns the
+ * number of records, *elapsed_s the wall time, *matrices the determinants. */
+long long lufqhe_server_run_stream(lufqhe_server_t *server, double rate_hz, long long nrequests,
+                                   int moves, int k_min, int k_max, unsigned long long seed,
+                                   double *lat_us, int *rec_n, long long max_records,
+                                   double *elapsed_s, long long *matrices);
+
 /* ---- on-device synthetic inputs (seeded; identical on every device) ---- */
 /* i.i.d. complex Gaussian entries, Re and Im ~ N(0, sigma^2/2). */
 int lufqhe_gen_gaussian(double *d_A, int n, int lda, long long batch, unsigned long long seed,
@@ -144,6 +233,9 @@ int lufqhe_gen_lll_host(double *A, double *z, int n, int lda, long long batch,
  * 0.1; 0 sends every matrix to the FP64 path, +inf disables the fallback
  * except for zero or non-finite FP32 pivots). */
 #define LUFQHE_OPT_MIXED_THRESHOLD 1
+/* Warps per CTA of the register-tiled mixed kernels (n in {6,8,12,16,24,32});
+ * 0 = library default. */
+#define LUFQHE_OPT_TILE_WARPS 2
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

@@ -152,6 +152,7 @@ extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, 
 
 namespace lufqhe {
 extern float g_mixed_theta;
+extern int g_tile_warps;
 }
 
 extern "C" int lufqhe_set_option(int option, double value) {
@@ -163,12 +164,21 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_mixed_theta = (float)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_TILE_WARPS) {
+    if (!(value >= 0.0 && value <= 8.0)) {
+      set_error("lufqhe_set_option: tile warps must be 0..8");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_tile_warps = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   set_error("lufqhe_set_option: unknown option %d", option);
   return LUFQHE_ERR_INVALID_ARG;
 }
 
 extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_MIXED_THRESHOLD) return (double)g_mixed_theta;
+  if (option == LUFQHE_OPT_TILE_WARPS) return (double)g_tile_warps;
   return NAN;
 }
 

@@ -1,0 +1,492 @@
+// Mixed-size batches in one persistent launch.
+//
+// A batch made of groups of same-size matrices (n differs between groups) is
+// cut into work items: tiles of T(n) consecutive matrices of one group. The
+// items are ordered largest n first (longest-processing-time first, so the
+// short small-n items fill the tail), stored in device memory, and consumed
+// by a persistent kernel: each warp takes the next item with one atomicAdd on
+// a device counter and runs the per-n device routine (the register-tiled
+// mixed routine for n in {6, 8, 12, 16, 24, 32}, the generic one otherwise,
+// or the FP64 routines in the plain modes). Shared memory per warp is sized
+// for the largest n of the batch.
+//
+// A plan (lufqhe_plan_create) fixes the groups and output buffers, chooses the
+// tile sizes and the warps per CTA with an autotuner that times candidate
+// launches on the plan's own data, and captures "reset counter + persistent
+// kernel" in a CUDA graph that lufqhe_plan_execute replays.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mixed_core.cuh"
+
+namespace lufqhe {
+
+namespace {
+
+using namespace mixed;
+
+struct WorkItem {
+  const double2 *A;  // group base
+  long long first;   // first matrix of the tile within the group
+  long long out;     // output index of that matrix
+  int count;         // matrices in the tile
+  int n;
+  int lda;
+  int pad;
+};
+
+size_t warp_smem_bytes(int nmax) {
+  const size_t lds = (size_t)nmax + 1;
+  return (size_t)nmax * lds * (sizeof(float4) + sizeof(float2)) + 2 * (size_t)nmax * sizeof(double) +
+         2 * (size_t)nmax * sizeof(int);
+}
+
+template <int MODE>
+__device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
+                               float2 *F, double *hold, int *er, int *ec, int lane, float theta2,
+                               DeferredOut &out, double *logabs, double *phase, int8_t *parity,
+                               int32_t *status) {
+  const int lds = n + 1;
+  double2 *M = reinterpret_cast<double2 *>(HL);
+  if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
+    emit_nonfinite(lane, ob, logabs, phase, parity, status);
+    return;
+  }
+  if (MODE == LUFQHE_MODE_MIXED) {
+    CFF prod;
+    int exp_sum = 0, par = 0;
+    float2 corr;
+    bool ok;
+    switch (n) {
+      case 6: ok = mixed_factor_tile<6>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 8: ok = mixed_factor_tile<8>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 12: ok = mixed_factor_tile<12>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 16: ok = mixed_factor_tile<16>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 24: ok = mixed_factor_tile<24>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 32: ok = mixed_factor_tile<32>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      default: {
+        MixedSmem S;
+        S.SC = HL;
+        S.Af = F;
+        S.hold = hold;
+        S.er = er;
+        S.ec = ec;
+        ok = mixed_factor(S, n, lane, theta2, prod, exp_sum, corr, par);
+      }
+    }
+    if (ok)
+      out.push(lane, ob, prod, exp_sum, corr, par, logabs, phase, parity, status);
+    else
+      fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status);
+  } else {
+    int par = 0;
+    int st = MODE == LUFQHE_MODE_PLAIN_FP64 ? lup_fp64_warp<ARITH_REF>(M, lds, hold, n, lane, &par)
+                                            : lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par);
+    double la, ph;
+    if (st == 0) {
+      logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+    } else if (st == LUFQHE_ST_SINGULAR) {
+      la = -INFINITY;
+      ph = 0.0;
+    } else {
+      la = NAN;
+      ph = NAN;
+      par = 0;
+    }
+    if (lane == 0) {
+      logabs[ob] = la;
+      if (phase) phase[ob] = ph;
+      if (parity) parity[ob] = (int8_t)par;
+      if (status) status[ob] = st;
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
+    grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nmax,
+                   float theta2, double *__restrict__ logabs, double *__restrict__ phase,
+                   int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const size_t nl = (size_t)nmax * (nmax + 1);
+  unsigned char *base = smem_raw;
+  float4 *HL = reinterpret_cast<float4 *>(base) + warp * nl;
+  base += warps * nl * sizeof(float4);
+  float2 *F = reinterpret_cast<float2 *>(base) + warp * nl;
+  base += warps * nl * sizeof(float2);
+  double *hold = reinterpret_cast<double *>(base) + warp * 2 * nmax;
+  base += warps * 2 * (size_t)nmax * sizeof(double);
+  int *er = reinterpret_cast<int *>(base) + warp * 2 * nmax;
+  int *ec = er + nmax;
+
+  DeferredOut out;
+  for (;;) {
+    unsigned int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(kFull, it, 0);
+    if (it >= (unsigned int)nitems) break;
+    const WorkItem w = items[it];
+    for (int j = 0; j < w.count; ++j) {
+      __syncwarp();
+      const long long b = w.first + j;
+      process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
+                           ec, lane, theta2, out, logabs, phase, parity, status);
+    }
+  }
+  out.flush(lane, logabs, phase, parity, status);
+}
+
+using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, float, double *,
+                               double *, int8_t *, int32_t *);
+
+GroupedKernel kernel_for(int mode) {
+  switch (mode) {
+    case LUFQHE_MODE_PLAIN_FP64: return grouped_kernel<LUFQHE_MODE_PLAIN_FP64>;
+    case LUFQHE_MODE_PLAIN_FP64_FUSED: return grouped_kernel<LUFQHE_MODE_PLAIN_FP64_FUSED>;
+    default: return grouped_kernel<LUFQHE_MODE_MIXED>;
+  }
+}
+
+// Default tile: about 64 n=8-equivalents of work per item (flops scale ~n^3).
+int default_tile(int n) {
+  double t = 64.0 * std::pow(8.0 / (double)n, 3.0);
+  int v = (int)std::lround(t);
+  return std::max(1, std::min(256, v));
+}
+
+struct Launch {
+  int warps = 4;
+  int ctas = 0;  // grid size
+  size_t smem = 0;
+};
+
+}  // namespace
+
+}  // namespace lufqhe
+
+using namespace lufqhe;
+
+struct lufqhe_plan_s {
+  std::vector<lufqhe_group_t> groups;
+  int mode = LUFQHE_MODE_MIXED;
+  int nmax = 1;
+  long long total = 0;
+  double *logabs = nullptr, *phase = nullptr;
+  int8_t *parity = nullptr;
+  int32_t *status = nullptr;
+  float theta2 = 0.01f;
+  // per-group tile size chosen by the tuner
+  std::vector<int> tile;
+  Launch launch;
+  // device state
+  WorkItem *d_items = nullptr;
+  unsigned int *d_counter = nullptr;
+  int nitems = 0;
+  size_t items_cap = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  std::string report;
+};
+
+namespace {
+
+int build_items(lufqhe_plan_s *p, cudaStream_t s) {
+  std::vector<int> order(p->groups.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return p->groups[a].n > p->groups[b].n; });
+  std::vector<WorkItem> items;
+  for (int g : order) {
+    const lufqhe_group_t &G = p->groups[g];
+    const int T = p->tile[g];
+    for (long long f = 0; f < G.count; f += T) {
+      WorkItem w;
+      w.A = reinterpret_cast<const double2 *>(G.A);
+      w.first = f;
+      w.out = G.out_offset + f;
+      w.count = (int)std::min<long long>(T, G.count - f);
+      w.n = G.n;
+      w.lda = G.lda;
+      w.pad = 0;
+      items.push_back(w);
+    }
+  }
+  p->nitems = (int)items.size();
+  if (items.size() > p->items_cap) {
+    if (p->d_items) cudaFree(p->d_items);
+    p->d_items = nullptr;
+    int rc = check_cuda(cudaMalloc(&p->d_items, sizeof(WorkItem) * std::max<size_t>(1, items.size())),
+                        "cudaMalloc(work items)");
+    if (rc) return rc;
+    p->items_cap = items.size();
+  }
+  if (!items.empty()) {
+    int rc = check_cuda(cudaMemcpyAsync(p->d_items, items.data(), sizeof(WorkItem) * items.size(),
+                                        cudaMemcpyHostToDevice, s),
+                        "cudaMemcpyAsync(work items)");
+    if (rc) return rc;
+  }
+  return check_cuda(cudaStreamSynchronize(s), "sync(work items)");
+}
+
+int configure_launch(lufqhe_plan_s *p, int warps) {
+  GroupedKernel k = kernel_for(p->mode);
+  const size_t per_warp = warp_smem_bytes(p->nmax);
+  const size_t optin = device_smem_optin();
+  int w = std::min<int>(warps, (int)(optin / per_warp));
+  if (w < 1) {
+    set_error("plan: n=%d needs %zu bytes of shared memory per warp; the device offers %zu",
+              p->nmax, per_warp, optin);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  const size_t smem = per_warp * w;
+  int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
+                      "cudaFuncSetAttribute(grouped)");
+  if (rc) return rc;
+  int per_sm = 0;
+  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, w * 32, smem),
+                  "occupancy(grouped)");
+  if (rc) return rc;
+  if (per_sm < 1) per_sm = 1;
+  p->launch.warps = w;
+  p->launch.smem = smem;
+  p->launch.ctas = device_sm_count() * per_sm;
+  return LUFQHE_SUCCESS;
+}
+
+int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
+  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned int), s), "memset(counter)");
+  if (rc) return rc;
+  if (p->nitems == 0) return LUFQHE_SUCCESS;
+  GroupedKernel k = kernel_for(p->mode);
+  const int grid = std::min<long long>(p->launch.ctas, (p->nitems + p->launch.warps - 1) /
+                                                            p->launch.warps + 0LL);
+  k<<<std::max(1, grid), p->launch.warps * 32, p->launch.smem, s>>>(
+      p->d_items, p->nitems, p->d_counter, p->nmax, p->theta2, p->logabs, p->phase, p->parity,
+      p->status);
+  return check_cuda(cudaGetLastError(), "grouped_kernel launch");
+}
+
+// Time one launch (ms) after one warm-up launch.
+int time_launch(lufqhe_plan_s *p, cudaStream_t s, float *ms) {
+  int rc = launch_once(p, s);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  rc = launch_once(p, s);
+  cudaEventRecord(e1, s);
+  if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "tune sync");
+  if (!rc) cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+// Autotuner: per group (alone), the tile size T from {1/4, 1/2, 1, 2, 4} x the
+// default; then, for the whole batch, the warps per CTA from {2, 4, 8}.
+int autotune(lufqhe_plan_s *p, cudaStream_t s) {
+  char line[256];
+  p->report = "{\"tiles\": {";
+  const std::vector<lufqhe_group_t> all = p->groups;
+  std::vector<int> base_tile = p->tile;
+  const int all_nmax = p->nmax;
+  int rc = configure_launch(p, 4);
+  if (rc) return rc;
+  for (size_t g = 0; g < all.size(); ++g) {
+    if (all[g].count == 0) continue;
+    p->groups.assign(1, all[g]);
+    p->nmax = all[g].n;
+    rc = configure_launch(p, 4);
+    if (rc) return rc;
+    float best = 1e30f;
+    int best_t = base_tile[g];
+    for (double f : {0.25, 0.5, 1.0, 2.0, 4.0}) {
+      int T = std::max(1, std::min(1024, (int)std::lround(base_tile[g] * f)));
+      p->tile.assign(1, T);
+      rc = build_items(p, s);
+      if (rc) return rc;
+      float ms = 0.0f;
+      rc = time_launch(p, s, &ms);
+      if (rc) return rc;
+      if (ms < best) {
+        best = ms;
+        best_t = T;
+      }
+    }
+    p->tile = base_tile;
+    base_tile[g] = best_t;
+    snprintf(line, sizeof(line), "%s\"%d\": {\"tile\": %d, \"ms_alone\": %.4f, \"count\": %lld}",
+             g ? ", " : "", all[g].n, best_t, best, all[g].count);
+    p->report += line;
+  }
+  p->groups = all;
+  p->tile = base_tile;
+  p->nmax = all_nmax;
+  rc = build_items(p, s);
+  if (rc) return rc;
+  float best = 1e30f;
+  int best_w = 4;
+  p->report += "}, \"warps\": {";
+  bool first = true;
+  for (int w : {2, 4, 8}) {
+    rc = configure_launch(p, w);
+    if (rc) return rc;
+    if (p->launch.warps != w) continue;  // does not fit
+    float ms = 0.0f;
+    rc = time_launch(p, s, &ms);
+    if (rc) return rc;
+    snprintf(line, sizeof(line), "%s\"%d\": %.4f", first ? "" : ", ", w, ms);
+    first = false;
+    p->report += line;
+    if (ms < best) {
+      best = ms;
+      best_w = w;
+    }
+  }
+  rc = configure_launch(p, best_w);
+  if (rc) return rc;
+  snprintf(line, sizeof(line), "}, \"chosen_warps\": %d, \"ctas\": %d}", p->launch.warps,
+           p->launch.ctas);
+  p->report += line;
+  return LUFQHE_SUCCESS;
+}
+
+int capture_graph(lufqhe_plan_s *p) {
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  if (p->graph) {
+    cudaGraphDestroy(p->graph);
+    p->graph = nullptr;
+  }
+  int rc = check_cuda(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal),
+                      "cudaStreamBeginCapture");
+  if (rc) return rc;
+  int lrc = launch_once(p, p->cap_stream);
+  rc = check_cuda(cudaStreamEndCapture(p->cap_stream, &p->graph), "cudaStreamEndCapture");
+  if (lrc) return lrc;
+  if (rc) return rc;
+  return check_cuda(cudaGraphInstantiate(&p->exec, p->graph, 0), "cudaGraphInstantiate");
+}
+
+void destroy_plan(lufqhe_plan_s *p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->d_items) cudaFree(p->d_items);
+  if (p->d_counter) cudaFree(p->d_counter);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  delete p;
+}
+
+}  // namespace
+
+namespace lufqhe {
+extern float g_mixed_theta;
+}
+
+extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *groups, int ngroups,
+                                  int mode, double *d_logabs, double *d_phase, int8_t *d_parity,
+                                  int32_t *d_status, int flags, void *stream) {
+  if (!plan || (ngroups > 0 && !groups) || ngroups < 0 || !d_logabs) {
+    set_error("lufqhe_plan_create: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (mode != LUFQHE_MODE_PLAIN_FP64 && mode != LUFQHE_MODE_PLAIN_FP64_FUSED &&
+      mode != LUFQHE_MODE_MIXED) {
+    set_error("lufqhe_plan_create: unknown mode %d", mode);
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  *plan = nullptr;
+  lufqhe_plan_s *p = new lufqhe_plan_s();
+  p->mode = mode;
+  p->logabs = d_logabs;
+  p->phase = d_phase;
+  p->parity = d_parity;
+  p->status = d_status;
+  p->theta2 = g_mixed_theta * g_mixed_theta;
+  for (int g = 0; g < ngroups; ++g) {
+    const lufqhe_group_t &G = groups[g];
+    if (G.count < 0 || G.n < 1 || G.lda < G.n || G.out_offset < 0 || (G.count > 0 && !G.A) ||
+        (reinterpret_cast<uintptr_t>(G.A) & 15) != 0) {
+      set_error("lufqhe_plan_create: group %d is invalid", g);
+      delete p;
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    if (G.n > LUFQHE_MAX_N) {
+      set_error("lufqhe_plan_create: group %d has n=%d > %d", g, G.n, LUFQHE_MAX_N);
+      delete p;
+      return LUFQHE_ERR_UNSUPPORTED_N;
+    }
+    p->groups.push_back(G);
+    p->tile.push_back(default_tile(G.n));
+    p->nmax = std::max(p->nmax, G.n);
+    p->total += G.count;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking),
+                      "cudaStreamCreate(plan)");
+  if (!rc) rc = check_cuda(cudaMalloc(&p->d_counter, sizeof(unsigned int)), "cudaMalloc(counter)");
+  if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sync(plan inputs)");
+  if (!rc && (flags & LUFQHE_PLAN_AUTOTUNE) && p->total > 0) rc = autotune(p, p->cap_stream);
+  if (!rc) rc = build_items(p, p->cap_stream);
+  if (!rc && !(flags & LUFQHE_PLAN_AUTOTUNE)) {
+    rc = configure_launch(p, 4);
+    char line[160];
+    snprintf(line, sizeof(line), "{\"tiles\": \"default\", \"chosen_warps\": %d, \"ctas\": %d}",
+             p->launch.warps, p->launch.ctas);
+    p->report = line;
+  }
+  if (!rc) rc = capture_graph(p);
+  if (rc) {
+    destroy_plan(p);
+    return rc;
+  }
+  *plan = p;
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_plan_execute(lufqhe_plan_t *plan, void *stream) {
+  if (!plan || !plan->exec) {
+    set_error("lufqhe_plan_execute: invalid plan");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  return check_cuda(cudaGraphLaunch(plan->exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+extern "C" int lufqhe_plan_launch_direct(lufqhe_plan_t *plan, void *stream) {
+  if (!plan) {
+    set_error("lufqhe_plan_launch_direct: invalid plan");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  return launch_once(plan, (cudaStream_t)stream);
+}
+
+extern "C" int lufqhe_plan_describe(const lufqhe_plan_t *plan, char *buf, size_t len) {
+  if (!plan || !buf || len == 0) {
+    set_error("lufqhe_plan_describe: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  snprintf(buf, len, "%s", plan->report.c_str());
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_plan_destroy(lufqhe_plan_t *plan) {
+  destroy_plan(plan);
+  return LUFQHE_SUCCESS;
+}

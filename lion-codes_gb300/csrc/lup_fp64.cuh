@@ -38,13 +38,17 @@ struct BlockWalk {
 
 // Coalesced load of an n x n complex128 matrix (row stride lda) into shared
 // memory (row stride lds). Returns true (warp-uniform) if any entry is NaN/Inf.
+// COHERENT loads through L2 only (no read-only / L1 path), for matrices that
+// a long-running kernel itself rewrites between reads.
+template <bool COHERENT = false>
 __device__ __forceinline__ bool load_matrix_fp64(const double2 *__restrict__ src, int n, int lda,
                                                  double2 *M, int lds, int lane) {
   bool bad = false;
   const int nn = n * n;
   BlockWalk w(lane, n);
   for (int e = lane; e < nn; e += 32) {
-    double2 v = __ldg(src + (size_t)w.i * lda + w.k);
+    const double2 *p = src + (size_t)w.i * lda + w.k;
+    double2 v = COHERENT ? __ldcg(p) : __ldg(p);
     bad |= !finite_c(v);
     M[w.i * lds + w.k] = v;
     w.next(n);

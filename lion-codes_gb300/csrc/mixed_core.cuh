@@ -1,0 +1,669 @@
+// Device building blocks of the mixed-precision determinant, shared by the
+// batched kernels (lup_mixed.cu) and the persistent mixed-size kernel
+// (grouped.cu). The method is described in lup_mixed.cu.
+#pragma once
+
+#include <cmath>
+
+#include "lup_fp64.cuh"
+
+namespace lufqhe {
+namespace mixed {
+// internal linkage: every translation unit that includes this gets its own copy
+namespace {
+
+
+constexpr int kMaxWarpsMixed = 8;
+// ||E||_F / max(1, |log|det||) above which the correction may miss 1e-10
+// relative accuracy. E comes from FP32 triangular solves, whose rounding
+// leaves an absolute error of about 1e-6 * ||E||_F in log det(I + E)
+// (measured on lowest-Landau-level matrices against a double-double oracle);
+// 5e-5 keeps that near 5e-11 relative, half the 1e-10 target.
+constexpr float kCorrRelCap = 5e-5f;
+
+// ---- float-float building blocks (never contracted: explicit _rn ops) ------
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// s + c -= l*u exactly up to the compensation's own rounding (Dot2 step).
+__device__ __forceinline__ void dot2_csub(float4 &sc, float2 l, float2 u) {
+  float p1, e1, p2, e2, p3, e3, p4, e4, s, t1, t2;
+  two_prod(l.x, u.x, p1, e1);
+  two_prod(l.y, u.y, p2, e2);
+  two_prod(l.x, u.y, p3, e3);
+  two_prod(l.y, u.x, p4, e4);
+  // real: s - p1 + p2
+  two_sum(sc.x, -p1, s, t1);
+  two_sum(s, p2, sc.x, t2);
+  sc.z = __fadd_rn(sc.z, __fadd_rn(__fsub_rn(t1, e1), __fadd_rn(t2, e2)));
+  // imag: s - p3 - p4
+  two_sum(sc.y, -p3, s, t1);
+  two_sum(s, -p4, sc.y, t2);
+  sc.w = __fadd_rn(sc.w, __fsub_rn(__fadd_rn(t1, t2), __fadd_rn(e3, e4)));
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -a.y * b.y), __fmaf_rn(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cfms(float2 s, float2 l, float2 u) {  // s - l*u
+  float x = __fmaf_rn(-l.x, u.x, s.x);
+  x = __fmaf_rn(l.y, u.y, x);
+  float y = __fmaf_rn(-l.x, u.y, s.y);
+  y = __fmaf_rn(-l.y, u.x, y);
+  return make_float2(x, y);
+}
+__device__ __forceinline__ float2 crcpf(float2 u) {
+  float rd = __frcp_rn(__fmaf_rn(u.x, u.x, u.y * u.y));
+  return make_float2(u.x * rd, -u.y * rd);
+}
+
+// Unbiased exponent field of the larger of |re|, |im| (-2000 for zero/subnormal).
+__device__ __forceinline__ int cexp_field(double2 v) {
+  int ex = (__double2hiint(v.x) >> 20) & 0x7ff;
+  int ey = (__double2hiint(v.y) >> 20) & 0x7ff;
+  int e = max(ex, ey);
+  return e == 0 ? -2000 : e - 1023;
+}
+
+// x * 2^-s split into float hi + lo by integer operations (hi keeps the top 24
+// significant bits, lo the next 24; the last <= 5 bits are dropped). The
+// caller guarantees |x| * 2^-s < 2. Subnormal results flush to zero.
+__device__ __forceinline__ void split_scaled(double x, int s, float &hi, float &lo) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  int e = (int)((u >> 52) & 0x7ff);
+  int E = e - 1023 - s;
+  if (e == 0 || E < -126) {
+    hi = __int_as_float((int)sign);
+    lo = 0.0f;
+    return;
+  }
+  unsigned long long mant = u & 0xFFFFFFFFFFFFFull;
+  hi = __int_as_float((int)(sign | ((unsigned)(E + 127) << 23) | (unsigned)(mant >> 29)));
+  unsigned rem = (unsigned)(mant & 0x1FFFFFFFull);
+  if (rem == 0) {
+    lo = 0.0f;
+    return;
+  }
+  int p = 31 - __clz(rem);
+  int El = E - 52 + p;
+  if (El < -126) {
+    lo = 0.0f;
+    return;
+  }
+  unsigned lm = (p >= 23) ? (rem >> (p - 23)) : (rem << (23 - p));
+  lo = __int_as_float((int)(sign | ((unsigned)(El + 127) << 23) | (lm & 0x7FFFFFu)));
+}
+
+// ---- complex float-float with a separate power-of-two exponent ------------
+struct CFF {
+  float xh, xl, yh, yl;
+  int e;
+};
+
+__device__ __forceinline__ void ff_renorm(CFF &a) {
+  float m = fmaxf(fabsf(a.xh), fabsf(a.yh));
+  if (m == 0.0f) return;
+  int k = ((__float_as_int(m) >> 23) & 0xff) - 127;
+  // scale by 2^-k (exact): multiply by a power of two built from bits
+  float sc = __int_as_float((127 - k) << 23);
+  a.xh *= sc;
+  a.xl *= sc;
+  a.yh *= sc;
+  a.yl *= sc;
+  a.e += k;
+}
+
+__device__ __forceinline__ CFF ff_cmul(const CFF &a, const CFF &b) {
+  float p1, e1, p2, e2, p3, e3, p4, e4, s, t;
+  two_prod(a.xh, b.xh, p1, e1);
+  two_prod(a.yh, b.yh, p2, e2);
+  two_prod(a.xh, b.yh, p3, e3);
+  two_prod(a.yh, b.xh, p4, e4);
+  CFF r;
+  // every operation explicit (_rn): no context-dependent FMA contraction, so
+  // each kernel that uses this gets the same bits
+  two_sum(p1, -p2, s, t);
+  float cx = __fmaf_rn(a.xh, b.xl, __fmul_rn(a.xl, b.xh));
+  float cy = __fmaf_rn(a.yh, b.yl, __fmul_rn(a.yl, b.yh));
+  float lo = __fsub_rn(__fadd_rn(__fsub_rn(__fadd_rn(t, e1), e2), cx), cy);
+  r.xh = __fadd_rn(s, lo);
+  r.xl = __fsub_rn(lo, __fsub_rn(r.xh, s));
+  two_sum(p3, p4, s, t);
+  cx = __fmaf_rn(a.xh, b.yl, __fmul_rn(a.xl, b.yh));
+  cy = __fmaf_rn(a.yh, b.xl, __fmul_rn(a.yl, b.xh));
+  lo = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t, e3), e4), cx), cy);
+  r.yh = __fadd_rn(s, lo);
+  r.yl = __fsub_rn(lo, __fsub_rn(r.yh, s));
+  r.e = a.e + b.e;
+  ff_renorm(r);
+  return r;
+}
+
+__device__ __forceinline__ CFF shfl_cff(const CFF &a, int src_or_mask, bool xor_mode) {
+  CFF r;
+  if (xor_mode) {
+    r.xh = __shfl_xor_sync(kFull, a.xh, src_or_mask);
+    r.xl = __shfl_xor_sync(kFull, a.xl, src_or_mask);
+    r.yh = __shfl_xor_sync(kFull, a.yh, src_or_mask);
+    r.yl = __shfl_xor_sync(kFull, a.yl, src_or_mask);
+    r.e = __shfl_xor_sync(kFull, a.e, src_or_mask);
+  } else {
+    r.xh = __shfl_sync(kFull, a.xh, src_or_mask);
+    r.xl = __shfl_sync(kFull, a.xl, src_or_mask);
+    r.yh = __shfl_sync(kFull, a.yh, src_or_mask);
+    r.yl = __shfl_sync(kFull, a.yl, src_or_mask);
+    r.e = __shfl_sync(kFull, a.e, src_or_mask);
+  }
+  return r;
+}
+
+struct MixedSmem {
+  float2 *Af;   // FP32 working matrix -> L\U          [n][lds]
+  float4 *SC;   // residual sum (xy) + compensation (zw); also double2 A [n][lds]
+  double *hold; // FP64 fallback row scales and their reciprocals [2n]
+  int *er;      // row exponents [n]
+  int *ec;      // column exponents [n]
+};
+
+// Steps 4-6 on the factored F (L\\U, row stride lds) and the residual R
+// (entry (i, k) at R[RS * (i * lds + k)]): E = U^-1 L^-1 R in place, the
+// float-float product of diag(U), the acceptance test, and log det(I + E).
+// Returns false (warp-uniform) if the matrix must be refactorised in FP64.
+template <int RS>
+__device__ bool mixed_finish(const float2 *F, float2 *R, int n, int lds, int lane, float theta2,
+                             int exp_sum, CFF &prod, float2 &corr) {
+  const int nn = n * n;
+  // 4a. Y = L^-1 R (unit lower, forward)
+  for (int t = 0; t + 1 < n; ++t) {
+    const int rows = n - 1 - t;
+    const int tot = rows * n;
+    BlockWalk w(lane, n);
+    for (int e = lane; e < tot; e += 32) {
+      const int i = t + 1 + w.i, k = w.k;
+      R[RS * (i * lds + k)] = cfms(R[RS * (i * lds + k)], F[i * lds + t], R[RS * (t * lds + k)]);
+      w.next(n);
+    }
+    __syncwarp();
+  }
+  // 4b. E = U^-1 Y (backward)
+  for (int t = n - 1; t >= 0; --t) {
+    const float2 r = crcpf(F[t * lds + t]);
+    for (int k = lane; k < n; k += 32) R[RS * (t * lds + k)] = cmulf(R[RS * (t * lds + k)], r);
+    __syncwarp();
+    const int tot = t * n;
+    BlockWalk w(lane, n);
+    for (int e = lane; e < tot; e += 32) {
+      const int i = w.i, k = w.k;
+      R[RS * (i * lds + k)] = cfms(R[RS * (i * lds + k)], F[i * lds + t], R[RS * (t * lds + k)]);
+      w.next(n);
+    }
+    __syncwarp();
+  }
+
+  // 6 (first half). complex float-float product of the diagonal of U; its
+  // exponent gives log2|det| to within 2 before the correction is accepted
+  {
+    CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+    for (int t = lane; t < n; t += 32) {
+      float2 u = F[t * lds + t];
+      CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
+      ff_renorm(v);
+      acc = ff_cmul(acc, v);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
+    prod = shfl_cff(acc, 0, false);
+  }
+
+  // acceptance: ||E||_F <= theta, and the FP32 evaluation of log det(I+E)
+  // (error ~ eps32 * ||E||_F) small against 1e-11 * max(1, |log|det||).
+  // Decided on lane 0's sum so it is warp-uniform.
+  {
+    float f = 0.0f;
+    BlockWalk w(lane, n);
+    for (int e = lane; e < nn; e += 32) {
+      float2 v = R[RS * (w.i * lds + w.k)];
+      f = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, f));
+      w.next(n);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
+    f = __shfl_sync(kFull, f, 0);
+    const float la_est = fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
+    const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
+    if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
+  }
+
+  // 5. log det(I + E): unpivoted LU with the identity implicit; the pivots
+  //    1 + d_t stay on the diagonal and their logs are taken lane-parallel.
+  for (int t = 0; t + 1 < n; ++t) {
+    const float2 d = R[RS * (t * lds + t)];
+    const float2 r = crcpf(make_float2(1.0f + d.x, d.y));
+    for (int i = t + 1 + lane; i < n; i += 32)
+      R[RS * (i * lds + t)] = cmulf(R[RS * (i * lds + t)], r);
+    __syncwarp();
+    const int m = n - 1 - t;
+    const int mm = m * m;
+    BlockWalk w(lane, m);
+    for (int e = lane; e < mm; e += 32) {
+      const int i = t + 1 + w.i, k = t + 1 + w.k;
+      R[RS * (i * lds + k)] = cfms(R[RS * (i * lds + k)], R[RS * (i * lds + t)], R[RS * (t * lds + k)]);
+      w.next(m);
+    }
+    __syncwarp();
+  }
+  float cre = 0.0f, cim = 0.0f;
+  for (int t = lane; t < n; t += 32) {
+    const float2 d = R[RS * (t * lds + t)];
+    cre = __fmaf_rn(0.5f, log1pf(__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, 2.0f * d.x))), cre);
+    cim += atan2f(d.y, 1.0f + d.x);
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    cre += __shfl_xor_sync(kFull, cre, off);
+    cim += __shfl_xor_sync(kFull, cim, off);
+  }
+  cre = __shfl_sync(kFull, cre, 0);
+  cim = __shfl_sync(kFull, cim, 0);
+  corr = make_float2(cre, cim);
+
+  return true;
+}
+
+// Steps 1-6 for the matrix already loaded (as double2) into S.SC. Returns
+// false (warp-uniform) if the matrix must be refactorised in FP64.
+__device__ bool mixed_factor(const MixedSmem &S, int n, int lane, float theta2, CFF &prod,
+                             int &exp_sum, float2 &corr, int &par) {
+  const int lds = n + 1;
+  const int nn = n * n;
+  double2 *A = reinterpret_cast<double2 *>(S.SC);
+
+  // 1. exponents: columns first (for orbital matrices the columns carry the
+  //    |z|^m scales), then rows of the column-scaled matrix
+  int rsum = 0, csum = 0;
+  for (int k = lane; k < n; k += 32) {
+    int m = -2000;
+    for (int i = 0; i < n; ++i) m = max(m, cexp_field(A[i * lds + k]));
+    if (m == -2000) m = 0;
+    S.ec[k] = m;
+    csum += m;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) {
+    int m = -2000;
+    for (int k = 0; k < n; ++k) {
+      int e = cexp_field(A[i * lds + k]);
+      if (e != -2000) m = max(m, e - S.ec[k]);
+    }
+    if (m == -2000) m = 0;
+    S.er[i] = m;
+    rsum += m;
+  }
+  __syncwarp();
+  // 2. split into hi (Af) and hi + lo (SC as s + c); same lane reads and writes
+  {
+    BlockWalk w(lane, n);
+    for (int e = lane; e < nn; e += 32) {
+      const int idx = w.i * lds + w.k;
+      const double2 v = A[idx];
+      const int s = S.er[w.i] + S.ec[w.k];
+      float xh, xl, yh, yl;
+      split_scaled(v.x, s, xh, xl);
+      split_scaled(v.y, s, yh, yl);
+      S.Af[idx] = make_float2(xh, yh);
+      S.SC[idx] = make_float4(xh, yh, xl, yl);
+      w.next(n);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    rsum += __shfl_xor_sync(kFull, rsum, off);
+    csum += __shfl_xor_sync(kFull, csum, off);
+  }
+  exp_sum = rsum + csum;
+  __syncwarp();
+
+  // 3. FP32 LUP with the float-float residual
+  par = 0;
+  for (int t = 0; t < n; ++t) {
+    float best = -1.0f;
+    int bi = t;
+    for (int i = t + lane; i < n; i += 32) {
+      float2 v = S.Af[i * lds + t];
+      float m = fabsf(v.x) + fabsf(v.y);
+      if (m > best) {
+        best = m;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      float om = __shfl_xor_sync(kFull, best, off);
+      int oi = __shfl_xor_sync(kFull, bi, off);
+      if (om > best || (om == best && oi < bi)) {
+        best = om;
+        bi = oi;
+      }
+    }
+    if (!(best > 0.0f) || !(best < INFINITY)) return false;  // zero/NaN/Inf pivot
+    const int p = bi;
+    if (p != t) {
+      for (int k = lane; k < n; k += 32) {
+        float2 a = S.Af[p * lds + k];
+        S.Af[p * lds + k] = S.Af[t * lds + k];
+        S.Af[t * lds + k] = a;
+        float4 c = S.SC[p * lds + k];
+        S.SC[p * lds + k] = S.SC[t * lds + k];
+        S.SC[t * lds + k] = c;
+      }
+      par ^= 1;
+    }
+    __syncwarp();
+    const float2 r = crcpf(S.Af[t * lds + t]);
+    for (int i = t + 1 + lane; i < n; i += 32) S.Af[i * lds + t] = cmulf(S.Af[i * lds + t], r);
+    __syncwarp();
+    const int m = n - t;
+    const int mm = m * m;
+    BlockWalk w(lane, m);
+    for (int e = lane; e < mm; e += 32) {
+      const int i = t + w.i, k = t + w.k;
+      const float2 U = S.Af[t * lds + k];
+      float4 sc = S.SC[i * lds + k];
+      if (i == t) {
+        float s, c;
+        two_sum(sc.x, -U.x, s, c);
+        sc.x = s;
+        sc.z = __fadd_rn(sc.z, c);
+        two_sum(sc.y, -U.y, s, c);
+        sc.y = s;
+        sc.w = __fadd_rn(sc.w, c);
+      } else {
+        const float2 L = S.Af[i * lds + t];
+        dot2_csub(sc, L, U);
+        if (k > t) S.Af[i * lds + k] = cfms(S.Af[i * lds + k], L, U);
+      }
+      S.SC[i * lds + k] = sc;
+      w.next(m);
+    }
+    __syncwarp();
+  }
+
+  // R = s + c, kept in the xy half of SC
+  float2 *R = reinterpret_cast<float2 *>(S.SC);  // entry idx at R[2*idx]
+  {
+    BlockWalk w(lane, n);
+    for (int e = lane; e < nn; e += 32) {
+      const int idx = w.i * lds + w.k;
+      float4 sc = S.SC[idx];
+      R[2 * idx] = make_float2(__fadd_rn(sc.x, sc.z), __fadd_rn(sc.y, sc.w));
+      w.next(n);
+    }
+  }
+  __syncwarp();
+
+  return mixed_finish<2>(S.Af, R, n, lds, lane, theta2, exp_sum, prod, corr);
+}
+
+// Deferred FP64 finalisation: lane L holds the L-th accepted matrix of the
+// current group of 32; one warp-wide log/atan2 then serves all 32.
+struct DeferredOut {
+  long long slot_b = -1;
+  CFF slot_p = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+  int slot_e = 0, slot_par = 0;
+  float2 slot_c = make_float2(0.0f, 0.0f);
+  int cnt = 0;
+
+  __device__ __forceinline__ void flush(int lane, double *logabs, double *phase, int8_t *parity,
+                                        int32_t *status) {
+    if (lane < cnt && slot_b >= 0) {
+      const double re = __dadd_rn((double)slot_p.xh, (double)slot_p.xl);
+      const double im = __dadd_rn((double)slot_p.yh, (double)slot_p.yl);
+      const double m2 = __fma_rn(re, re, __dmul_rn(im, im));
+      const double la =
+          __dadd_rn(__fma_rn((double)slot_e, kLn2, __dmul_rn(0.5, log(m2))), (double)slot_c.x);
+      const double ph = __dadd_rn(__dadd_rn(atan2(im, re), (double)slot_c.y), slot_par ? kPi : 0.0);
+      logabs[slot_b] = la;
+      if (phase) phase[slot_b] = wrap_phase(ph);
+      if (parity) parity[slot_b] = (int8_t)slot_par;
+      if (status) status[slot_b] = 0;
+    }
+    slot_b = -1;
+    cnt = 0;
+  }
+  __device__ __forceinline__ void push(int lane, long long b, const CFF &prod, int exp_sum,
+                                       float2 corr, int par, double *logabs, double *phase,
+                                       int8_t *parity, int32_t *status) {
+    if (lane == cnt) {
+      slot_b = b;
+      slot_p = prod;
+      slot_e = prod.e + exp_sum;
+      slot_c = corr;
+      slot_par = par;
+    }
+    if (++cnt == 32) flush(lane, logabs, phase, parity, status);
+  }
+};
+
+__device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *logabs,
+                                               double *phase, int8_t *parity, int32_t *status) {
+  if (lane == 0) {
+    logabs[b] = NAN;
+    if (phase) phase[b] = NAN;
+    if (parity) parity[b] = 0;
+    if (status) status[b] = LUFQHE_ST_NONFINITE;
+  }
+}
+
+// FP64 refactorisation of the original matrix (reloaded into M), status |= FALLBACK.
+template <bool COHERENT = false>
+__device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, int lds,
+                              double *hold, int lane, long long b, double *logabs, double *phase,
+                              int8_t *parity, int32_t *status) {
+  __syncwarp();
+  load_matrix_fp64<COHERENT>(src, n, lda, M, lds, lane);
+  int par = 0;
+  int st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par);
+  double la, ph;
+  if (st == 0) {
+    logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+  } else if (st == LUFQHE_ST_SINGULAR) {
+    la = -INFINITY;
+    ph = 0.0;
+  } else {
+    la = NAN;
+    ph = NAN;
+    par = 0;
+  }
+  if (lane == 0) {
+    logabs[b] = la;
+    if (phase) phase[b] = ph;
+    if (parity) parity[b] = (int8_t)par;
+    if (status) status[b] = st | LUFQHE_ST_FALLBACK;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Register-tiled form of the same method for a compile-time n <= 32.
+//  * FP32 LUP as above (shared memory, right-looking, rows of F and of the
+//    hi/lo copy swap together).
+//  * Residual: the 32 lanes form a 4 x 8 grid; lane (r, c) owns the entries
+//    (4a + r, 8b + c) and accumulates their float-float Dot2 sums in registers
+//    over t, reading l_it and u_tk from shared memory (operands that do not
+//    contribute are zero, which leaves a Dot2 step exact and branch-free).
+//  * Solves: lane k owns column k of R in registers; the L and U entries are
+//    shared-memory broadcasts.
+//  * log det(I + E): E transposed to one row per lane; unpivoted elimination
+//    with the pivot row shuffled from its lane.
+template <int N>
+struct TileGeom {
+  static constexpr int LDS = N + 1;
+  static constexpr int SA = (N + 3) / 4;  // row slots per lane
+  static constexpr int SB = (N + 7) / 8;  // column slots per lane
+};
+
+template <int N>
+__device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane, float theta2,
+                                  CFF &prod, int &exp_sum, float2 &corr, int &par) {
+  constexpr int LDS = TileGeom<N>::LDS;
+  constexpr int SA = TileGeom<N>::SA;
+  constexpr int SB = TileGeom<N>::SB;
+  const double2 *A = reinterpret_cast<const double2 *>(HL);
+
+  // 1. exponents, columns first
+  int esum = 0;
+  if (lane < N) {
+    int m = -2000;
+#pragma unroll 4
+    for (int i = 0; i < N; ++i) m = max(m, cexp_field(A[i * LDS + lane]));
+    if (m == -2000) m = 0;
+    ec[lane] = m;
+    esum = m;
+  }
+  __syncwarp();
+  if (lane < N) {
+    int m = -2000;
+#pragma unroll 4
+    for (int k = 0; k < N; ++k) {
+      int e = cexp_field(A[lane * LDS + k]);
+      if (e != -2000) m = max(m, e - ec[k]);
+    }
+    if (m == -2000) m = 0;
+    er[lane] = m;
+    esum += m;
+  }
+  exp_sum = __reduce_add_sync(kFull, esum);
+  __syncwarp();
+  // 2. split (each lane rewrites the entries it read)
+  for (int e = lane; e < N * N; e += 32) {
+    const int i = e / N, k = e - i * N;
+    const int idx = i * LDS + k;
+    const double2 v = A[idx];
+    const int s = er[i] + ec[k];
+    float xh, xl, yh, yl;
+    split_scaled(v.x, s, xh, xl);
+    split_scaled(v.y, s, yh, yl);
+    F[idx] = make_float2(xh, yh);
+    HL[idx] = make_float4(xh, yh, xl, yl);
+  }
+  __syncwarp();
+
+  // 3. FP32 LUP
+  par = 0;
+  for (int t = 0; t < N; ++t) {
+    float best = -1.0f;
+    int bi = t;
+    if (lane >= t && lane < N) {
+      const float2 v = F[lane * LDS + t];
+      best = fabsf(v.x) + fabsf(v.y);
+      bi = lane;
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      float om = __shfl_xor_sync(kFull, best, off);
+      int oi = __shfl_xor_sync(kFull, bi, off);
+      if (om > best || (om == best && oi < bi)) {
+        best = om;
+        bi = oi;
+      }
+    }
+    if (!(best > 0.0f) || !(best < INFINITY)) return false;
+    if (bi != t) {
+      if (lane < N) {
+        const float2 a = F[bi * LDS + lane];
+        F[bi * LDS + lane] = F[t * LDS + lane];
+        F[t * LDS + lane] = a;
+        const float4 c = HL[bi * LDS + lane];
+        HL[bi * LDS + lane] = HL[t * LDS + lane];
+        HL[t * LDS + lane] = c;
+      }
+      par ^= 1;
+    }
+    __syncwarp();
+    const float2 r = crcpf(F[t * LDS + t]);
+    if (lane > t && lane < N) F[lane * LDS + t] = cmulf(F[lane * LDS + t], r);
+    __syncwarp();
+    const int m = N - 1 - t;
+    if (m > 0) {
+      BlockWalk w(lane, m);
+      for (int e = lane; e < m * m; e += 32) {
+        const int i = t + 1 + w.i, k = t + 1 + w.k;
+        F[i * LDS + k] = cfms(F[i * LDS + k], F[i * LDS + t], F[t * LDS + k]);
+        w.next(m);
+      }
+    }
+    __syncwarp();
+  }
+
+  // 4. residual R = P A^ - L U (float-float) in a 4 x 8 lane grid
+  const int tr = lane >> 3, tc = lane & 7;
+  float4 acc[SA][SB];
+#pragma unroll
+  for (int a = 0; a < SA; ++a)
+#pragma unroll
+    for (int b = 0; b < SB; ++b) {
+      const int i = 4 * a + tr, k = 8 * b + tc;
+      acc[a][b] = (i < N && k < N) ? HL[i * LDS + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll 1
+  for (int t = 0; t < N; ++t) {
+    float2 Lv[SA], Uv[SB];
+#pragma unroll
+    for (int a = 0; a < SA; ++a) {
+      const int i = 4 * a + tr;
+      Lv[a] = make_float2(0.f, 0.f);
+      if (i == t) Lv[a] = make_float2(1.f, 0.f);
+      else if (i > t && i < N) Lv[a] = F[i * LDS + t];
+    }
+#pragma unroll
+    for (int b = 0; b < SB; ++b) {
+      const int k = 8 * b + tc;
+      Uv[b] = make_float2(0.f, 0.f);
+      if (k >= t && k < N) Uv[b] = F[t * LDS + k];
+    }
+    // slots whose rows and columns all lie before t have nothing left to add
+#pragma unroll
+    for (int a = 0; a < SA; ++a) {
+      if (4 * a + 3 < t) continue;
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        if (8 * b + 7 < t) continue;
+        dot2_csub(acc[a][b], Lv[a], Uv[b]);
+      }
+    }
+  }
+  float2 *Rm = reinterpret_cast<float2 *>(HL);  // R, then E, row stride LDS
+  __syncwarp();
+#pragma unroll
+  for (int a = 0; a < SA; ++a)
+#pragma unroll
+    for (int b = 0; b < SB; ++b) {
+      const int i = 4 * a + tr, k = 8 * b + tc;
+      if (i < N && k < N)
+        Rm[i * LDS + k] = make_float2(__fadd_rn(acc[a][b].x, acc[a][b].z),
+                                      __fadd_rn(acc[a][b].y, acc[a][b].w));
+    }
+  __syncwarp();
+
+    // 5-6. solves, acceptance, log det(I + E) and the diagonal product: the
+  //      shared-memory forms of the generic path with n fixed at compile time
+  return mixed_finish<1>(F, Rm, N, LDS, lane, theta2, exp_sum, prod, corr);
+}
+
+template <int N>
+constexpr size_t tile_smem_per_warp() {
+  return (size_t)N * (N + 1) * (sizeof(float4) + sizeof(float2)) + 2 * (size_t)N * sizeof(double) +
+         2 * (size_t)N * sizeof(int);
+}
+
+
+}  // namespace
+}  // namespace mixed
+}  // namespace lufqhe

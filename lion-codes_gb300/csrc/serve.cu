@@ -1,0 +1,839 @@
+// Serving: device-resident Monte Carlo walkers and a persistent request loop.
+//
+// A walker is k matrices of one size n (the Slater-type matrices of one
+// Monte Carlo configuration set) that stay in HBM for its whole life. A move
+// resamples particle i of every matrix: the host sends only the k new z_i and
+// the GPU rebuilds row i (M_ik = z^k exp(-|z|^2/4)) in place, then recomputes
+// the k determinants. Walkers are admitted against an HBM byte budget.
+//
+// Each size class (n) has its own persistent kernel on its own stream, sized
+// to a share of the SMs, so all classes are resident at once. A request
+// (one move of one walker) is cut into tiles of matrices; the host appends the
+// tiles to the class's ring in mapped host memory and publishes them with a
+// release store. Warps of the class kernel claim tile indices with an
+// atomicAdd, wait (bounded) until the index is published, process the tile and
+// count it against its request; the warp that finishes a request's last tile
+// writes the request's completion flag to mapped host memory. Tiles of
+// different requests are in flight at the same time on different warps: new
+// requests are admitted as soon as ring slots and HBM free up, without waiting
+// for a batch boundary.
+//
+// Every device wait is bounded: a warp that sees no new tile for
+// kIdleCycles gives up, records the first tile index it had claimed, and the
+// kernel exits; the host relaunches it (restarting the claim counter at the
+// first abandoned index) the next time it publishes work.
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "mixed_core.cuh"
+
+namespace lufqhe {
+
+namespace {
+
+using namespace mixed;
+
+constexpr unsigned kRing = 1u << 16;                  // tiles per class ring
+constexpr long long kIdleCycles = 1000000000ll;       // ~0.5 s at 2 GHz
+constexpr int kServeWarps = 4;
+
+struct ServeTile {
+  double2 *mats;             // first matrix of the tile (device)
+  double2 *z;                // its particle coordinates (device, n per matrix)
+  const double2 *znew;       // new coordinate of `particle` per matrix (mapped host), or null
+  double *logabs;            // outputs for the tile's first matrix (mapped host)
+  double *phase;
+  int32_t *status;
+  unsigned int *req_done;    // tiles finished, per request slot (device)
+  unsigned int *completion;  // request completion flag (mapped host)
+  unsigned int seq;          // value stored into *completion
+  unsigned int req_tiles;
+  int count;
+  int particle;
+};
+
+struct ClassCtl {              // device memory, one per class
+  unsigned int claimed;        // next tile index to claim
+  unsigned int abandoned_min;  // first claimed-but-unpublished index at exit
+  unsigned int exited;         // warps that left the loop
+  unsigned int pad;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Row `particle` of each matrix of the tile: lane j rebuilds matrix j's row.
+__device__ void rebuild_rows(const ServeTile &t, int n, int lane) {
+  for (int j0 = 0; j0 < t.count; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < t.count) {
+      const double2 z = __ldcv(t.znew + j);
+      t.z[(size_t)j * n + t.particle] = z;
+      double2 *row = t.mats + (size_t)j * n * n + (size_t)t.particle * n;
+      const double w = exp(-(z.x * z.x + z.y * z.y) * 0.25);
+      double px = 1.0, py = 0.0;
+      for (int k = 0; k < n; ++k) {
+        row[k] = make_double2(px * w, py * w);
+        const double nx = px * z.x - py * z.y;
+        const double ny = px * z.y + py * z.x;
+        px = nx;
+        py = ny;
+      }
+    }
+  }
+  __syncwarp();
+  __threadfence_block();
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kServeWarps * 32, 1)
+    serve_kernel(const ServeTile *ring, const unsigned int *published, const unsigned int *stop,
+                 ClassCtl *ctl, int mode, float theta2) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LDS = NC + 1;
+  constexpr size_t NL = (size_t)NC * LDS;
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  unsigned char *base = smem_raw;
+  float4 *HL = reinterpret_cast<float4 *>(base) + warp * NL;
+  base += warps * NL * sizeof(float4);
+  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
+  base += warps * NL * sizeof(float2);
+  double *hold = reinterpret_cast<double *>(base) + warp * 2 * NC;
+  base += warps * 2 * (size_t)NC * sizeof(double);
+  int *er = reinterpret_cast<int *>(base) + warp * 2 * NC;
+  int *ec = er + NC;
+
+  for (;;) {
+    unsigned int idx = 0;
+    if (lane == 0) idx = atomicAdd(&ctl->claimed, 1u);
+    idx = __shfl_sync(kFull, idx, 0);
+    // bounded wait for the tile to be published
+    int give_up = 0;
+    if (lane == 0) {
+      const long long t0 = clock64();
+      while (ld_acquire_sys(published) <= idx) {
+        if (ld_acquire_sys(stop) || clock64() - t0 > kIdleCycles) {
+          give_up = 1;
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    give_up = __shfl_sync(kFull, give_up, 0);
+    if (give_up) {
+      if (lane == 0) {
+        atomicMin(&ctl->abandoned_min, idx);
+        atomicAdd(&ctl->exited, 1u);
+      }
+      return;
+    }
+    __syncwarp();  // order every lane's reads after lane 0's acquire
+    ServeTile t;
+    {
+      // the ring lives in mapped host memory: read it uncached, word by word
+      const unsigned long long *srcw =
+          reinterpret_cast<const unsigned long long *>(ring + (idx % kRing));
+      unsigned long long *dstw = reinterpret_cast<unsigned long long *>(&t);
+#pragma unroll
+      for (int q = 0; q < (int)(sizeof(ServeTile) / 8); ++q) dstw[q] = __ldcv(srcw + q);
+    }
+    if (t.particle >= 0 && t.znew) rebuild_rows(t, NC, lane);
+    DeferredOut out;
+    for (int j = 0; j < t.count; ++j) {
+      __syncwarp();
+      const double2 *src = t.mats + (size_t)j * NC * NC;
+      double2 *M = reinterpret_cast<double2 *>(HL);
+      if (load_matrix_fp64<true>(src, NC, NC, M, LDS, lane)) {
+        emit_nonfinite(lane, j, t.logabs, t.phase, nullptr, t.status);
+        continue;
+      }
+      if (mode == LUFQHE_MODE_MIXED) {
+        CFF prod;
+        int exp_sum = 0, par = 0;
+        float2 corr;
+        bool ok;
+        if constexpr (NC <= 32) {
+          ok = mixed_factor_tile<NC>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
+        } else {
+          MixedSmem S;
+          S.SC = HL;
+          S.Af = F;
+          S.hold = hold;
+          S.er = er;
+          S.ec = ec;
+          ok = mixed_factor(S, NC, lane, theta2, prod, exp_sum, corr, par);
+        }
+        if (ok)
+          out.push(lane, j, prod, exp_sum, corr, par, t.logabs, t.phase, nullptr, t.status);
+        else
+          fallback_fp64<true>(src, NC, NC, M, LDS, hold, lane, j, t.logabs, t.phase, nullptr,
+                              t.status);
+      } else {
+        int par = 0;
+        int st = lup_fp64_warp<ARITH_FUSED>(M, LDS, hold, NC, lane, &par);
+        double la, ph;
+        if (st == 0) {
+          logdet_from_diag(M, LDS, NC, lane, par, &la, &ph);
+        } else if (st == LUFQHE_ST_SINGULAR) {
+          la = -INFINITY;
+          ph = 0.0;
+        } else {
+          la = NAN;
+          ph = NAN;
+        }
+        if (lane == 0) {
+          t.logabs[j] = la;
+          t.phase[j] = ph;
+          t.status[j] = st;
+        }
+      }
+    }
+    out.flush(lane, t.logabs, t.phase, nullptr, t.status);
+    __threadfence_system();  // each lane's result stores before the count
+    __syncwarp();
+    if (lane == 0) {
+      const unsigned int done = atomicAdd(t.req_done, 1u) + 1u;
+      if (done == t.req_tiles) {
+        // last tile of the request: re-arm the counter for the slot's next
+        // request, then publish completion
+        atomicExch(t.req_done, 0u);
+        __threadfence_system();
+        st_release_sys(t.completion, t.seq);
+      }
+    }
+  }
+}
+
+__global__ void build_walker_kernel(double2 *mats, const double2 *z, int n, int k) {
+  long long total = (long long)k * n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long j = e / n;
+    const int i = (int)(e - j * n);
+    const double2 zz = z[e];
+    double2 *row = mats + (size_t)j * n * n + (size_t)i * n;
+    const double w = exp(-(zz.x * zz.x + zz.y * zz.y) * 0.25);
+    double px = 1.0, py = 0.0;
+    for (int c = 0; c < n; ++c) {
+      row[c] = make_double2(px * w, py * w);
+      const double nx = px * zz.x - py * zz.y;
+      const double ny = px * zz.y + py * zz.x;
+      px = nx;
+      py = ny;
+    }
+  }
+}
+
+
+using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
+                             ClassCtl *, int, float);
+
+ServeKernel serve_kernel_for(int n) {
+  switch (n) {
+    case 8: return serve_kernel<8>;
+    case 16: return serve_kernel<16>;
+    case 32: return serve_kernel<32>;
+    case 64: return serve_kernel<64>;
+    default: return nullptr;
+  }
+}
+
+size_t serve_smem_per_warp(int n) {
+  return (size_t)n * (n + 1) * (sizeof(float4) + sizeof(float2)) + 2 * (size_t)n * sizeof(double) +
+         2 * (size_t)n * sizeof(int);
+}
+
+// ---- host side -------------------------------------------------------------
+
+constexpr int kReqSlots = 1024;   // requests in flight at once (all classes)
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Walker {
+  bool live = false;
+  int n = 0;
+  int k = 0;
+  int cls = -1;
+  size_t offset = 0;     // in the HBM pool
+  size_t bytes = 0;
+  bool busy = false;     // a move is in flight
+};
+
+struct ReqSlot {
+  bool used = false;
+  int walker = -1;
+  int k = 0;
+  unsigned int seq = 0;
+  unsigned int first_tile = 0, last_tile = 0;
+  int cls = -1;
+};
+
+struct SClass {
+  int n = 0;
+  int sms = 0;
+  ServeKernel kern = nullptr;
+  cudaStream_t stream = nullptr;
+  ServeTile *ring_h = nullptr;     // mapped host
+  ServeTile *ring_d = nullptr;     // device view of the same memory
+  unsigned int *pub_h = nullptr;   // published count (mapped host)
+  unsigned int *pub_d = nullptr;
+  ClassCtl *ctl = nullptr;         // device
+  unsigned int published = 0;     // host copy
+  int grid = 0, warps = kServeWarps;
+  size_t smem = 0;
+  bool running = false;
+  unsigned int relaunches = 0;
+};
+
+}  // namespace
+}  // namespace lufqhe
+
+using namespace lufqhe;
+
+struct lufqhe_server_s {
+  int mode = LUFQHE_MODE_MIXED;
+  int max_k = 4096;
+  int tile = 8;
+  float theta2 = 0.01f;
+  std::vector<SClass> classes;
+  // HBM pool with a first-fit free list
+  unsigned char *pool = nullptr;
+  size_t pool_bytes = 0;
+  std::vector<std::pair<size_t, size_t>> free_list;  // (offset, bytes), sorted by offset
+  std::vector<Walker> walkers;
+  // request slots: staging (mapped host) and results (mapped host)
+  double2 *znew_h = nullptr, *znew_d = nullptr;        // kReqSlots * max_k
+  double *la_h = nullptr, *la_d = nullptr;
+  double *ph_h = nullptr, *ph_d = nullptr;
+  int32_t *st_h = nullptr, *st_d = nullptr;
+  unsigned int *comp_h = nullptr, *comp_d = nullptr;   // completion flags (mapped)
+  unsigned int *req_done = nullptr;                    // device counters
+  unsigned int *stop_h = nullptr, *stop_d = nullptr;
+  cudaStream_t setup = nullptr;   // walker uploads (the class streams hold the loops)
+  std::vector<ReqSlot> slots;
+  unsigned int next_seq = 1;
+  long long next_ticket = 1;
+  std::mutex mu;
+};
+
+namespace {
+
+int pool_alloc(lufqhe_server_s *s, size_t bytes, size_t *off) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  for (size_t i = 0; i < s->free_list.size(); ++i) {
+    if (s->free_list[i].second >= bytes) {
+      *off = s->free_list[i].first;
+      s->free_list[i].first += bytes;
+      s->free_list[i].second -= bytes;
+      if (s->free_list[i].second == 0) s->free_list.erase(s->free_list.begin() + i);
+      return LUFQHE_SUCCESS;
+    }
+  }
+  return LUFQHE_ERR_BUSY;
+}
+
+void pool_free(lufqhe_server_s *s, size_t off, size_t bytes) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  auto it = std::lower_bound(s->free_list.begin(), s->free_list.end(),
+                             std::make_pair(off, (size_t)0));
+  it = s->free_list.insert(it, {off, bytes});
+  // coalesce with neighbours
+  size_t i = it - s->free_list.begin();
+  if (i + 1 < s->free_list.size() &&
+      s->free_list[i].first + s->free_list[i].second == s->free_list[i + 1].first) {
+    s->free_list[i].second += s->free_list[i + 1].second;
+    s->free_list.erase(s->free_list.begin() + i + 1);
+  }
+  if (i > 0 && s->free_list[i - 1].first + s->free_list[i - 1].second == s->free_list[i].first) {
+    s->free_list[i - 1].second += s->free_list[i].second;
+    s->free_list.erase(s->free_list.begin() + i);
+  }
+}
+
+int class_index(lufqhe_server_s *s, int n) {
+  for (size_t c = 0; c < s->classes.size(); ++c)
+    if (s->classes[c].n == n) return (int)c;
+  return -1;
+}
+
+// (Re)launch a class kernel if it is not running.
+int ensure_running(lufqhe_server_s *s, SClass &c) {
+  if (c.running) {
+    cudaError_t q = cudaStreamQuery(c.stream);
+    if (q == cudaErrorNotReady) return LUFQHE_SUCCESS;
+    c.running = false;
+    if (q != cudaSuccess) return check_cuda(q, "serve kernel");
+  }
+  // restart claims at the first abandoned index (everything before it is done)
+  ClassCtl h;
+  int rc = check_cuda(cudaMemcpyAsync(&h, c.ctl, sizeof(h), cudaMemcpyDeviceToHost, c.stream),
+                      "read class ctl");
+  if (!rc) rc = check_cuda(cudaStreamSynchronize(c.stream), "sync class ctl");
+  if (rc) return rc;
+  ClassCtl n{};
+  n.claimed = h.abandoned_min == 0xffffffffu ? h.claimed : h.abandoned_min;
+  n.abandoned_min = 0xffffffffu;
+  rc = check_cuda(cudaMemcpyAsync(c.ctl, &n, sizeof(n), cudaMemcpyHostToDevice, c.stream),
+                  "write class ctl");
+  if (rc) return rc;
+  c.kern<<<c.grid, c.warps * 32, c.smem, c.stream>>>(c.ring_d, c.pub_d, s->stop_d, c.ctl, s->mode,
+                                                     s->theta2);
+  rc = check_cuda(cudaGetLastError(), "serve kernel launch");
+  if (rc) return rc;
+  c.running = true;
+  ++c.relaunches;
+  return LUFQHE_SUCCESS;
+}
+
+void destroy_server(lufqhe_server_s *s) {
+  if (!s) return;
+  if (s->stop_h) __atomic_store_n(s->stop_h, 1u, __ATOMIC_RELEASE);
+  for (auto &c : s->classes) {
+    if (c.stream) {
+      cudaStreamSynchronize(c.stream);
+      cudaStreamDestroy(c.stream);
+    }
+    if (c.ring_h) cudaFreeHost(c.ring_h);
+    if (c.pub_h) cudaFreeHost(c.pub_h);
+    if (c.ctl) cudaFree(c.ctl);
+  }
+  if (s->pool) cudaFree(s->pool);
+  if (s->znew_h) cudaFreeHost(s->znew_h);
+  if (s->la_h) cudaFreeHost(s->la_h);
+  if (s->ph_h) cudaFreeHost(s->ph_h);
+  if (s->st_h) cudaFreeHost(s->st_h);
+  if (s->comp_h) cudaFreeHost(s->comp_h);
+  if (s->stop_h) cudaFreeHost(s->stop_h);
+  if (s->req_done) cudaFree(s->req_done);
+  if (s->setup) cudaStreamDestroy(s->setup);
+  delete s;
+}
+
+template <typename T>
+int host_mapped(T **h, T **d, size_t count, const char *what) {
+  int rc = check_cuda(cudaHostAlloc((void **)h, sizeof(T) * count, cudaHostAllocMapped), what);
+  if (rc) return rc;
+  memset(*h, 0, sizeof(T) * count);
+  return check_cuda(cudaHostGetDevicePointer((void **)d, *h, 0), what);
+}
+
+}  // namespace
+
+namespace lufqhe {
+extern float g_mixed_theta;
+}
+
+extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
+                                    const int *class_n, const int *class_sms, int nclasses,
+                                    int max_k, int tile) {
+  if (!server || nclasses < 1 || !class_n || max_k < 1 || tile < 1 || hbm_budget_bytes == 0) {
+    set_error("lufqhe_server_create: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (mode != LUFQHE_MODE_MIXED && mode != LUFQHE_MODE_PLAIN_FP64_FUSED) {
+    set_error("lufqhe_server_create: mode must be MIXED or PLAIN_FP64_FUSED");
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  *server = nullptr;
+  lufqhe_server_s *s = new lufqhe_server_s();
+  s->mode = mode;
+  s->max_k = max_k;
+  s->tile = tile;
+  s->theta2 = g_mixed_theta * g_mixed_theta;
+  s->slots.resize(kReqSlots);
+  int rc = LUFQHE_SUCCESS;
+  const int sms = device_sm_count();
+  int sms_left = sms;
+  for (int c = 0; c < nclasses && !rc; ++c) {
+    SClass sc;
+    sc.n = class_n[c];
+    sc.kern = serve_kernel_for(sc.n);
+    if (!sc.kern) {
+      set_error("lufqhe_server_create: class n=%d not offered (8, 16, 32, 64)", sc.n);
+      rc = LUFQHE_ERR_UNSUPPORTED_N;
+      break;
+    }
+    int want = class_sms ? class_sms[c] : std::max(1, sms / nclasses);
+    sc.sms = std::max(1, std::min(want, sms_left - (nclasses - 1 - c)));
+    sms_left -= sc.sms;
+    const size_t per_warp = serve_smem_per_warp(sc.n);
+    sc.warps = std::max(1, std::min<int>(kServeWarps, (int)(device_smem_optin() / per_warp)));
+    sc.smem = per_warp * sc.warps;
+    rc = check_cuda(cudaFuncSetAttribute(sc.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sc.smem),
+                    "cudaFuncSetAttribute(serve)");
+    if (rc) break;
+    int per_sm = 0;
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sc.kern, sc.warps * 32,
+                                                                  sc.smem),
+                    "occupancy(serve)");
+    if (rc) break;
+    sc.grid = std::max(1, sc.sms * std::max(1, per_sm));
+    rc = check_cuda(cudaStreamCreateWithFlags(&sc.stream, cudaStreamNonBlocking), "serve stream");
+    if (!rc) rc = host_mapped(&sc.ring_h, &sc.ring_d, kRing, "serve ring");
+    if (!rc) rc = host_mapped(&sc.pub_h, &sc.pub_d, 1, "serve published");
+    if (!rc) rc = check_cuda(cudaMalloc(&sc.ctl, sizeof(ClassCtl)), "serve ctl");
+    if (!rc) {
+      ClassCtl z{};
+      z.abandoned_min = 0xffffffffu;
+      rc = check_cuda(cudaMemcpy(sc.ctl, &z, sizeof(z), cudaMemcpyHostToDevice), "serve ctl init");
+    }
+    s->classes.push_back(sc);
+  }
+  if (!rc) rc = check_cuda(cudaMalloc(&s->pool, hbm_budget_bytes), "cudaMalloc(walker pool)");
+  if (!rc) {
+    s->pool_bytes = hbm_budget_bytes;
+    s->free_list.push_back({0, hbm_budget_bytes});
+  }
+  const size_t slot_elems = (size_t)kReqSlots * max_k;
+  if (!rc) rc = host_mapped(&s->znew_h, &s->znew_d, slot_elems, "serve staging");
+  if (!rc) rc = host_mapped(&s->la_h, &s->la_d, slot_elems, "serve logabs");
+  if (!rc) rc = host_mapped(&s->ph_h, &s->ph_d, slot_elems, "serve phase");
+  if (!rc) rc = host_mapped(&s->st_h, &s->st_d, slot_elems, "serve status");
+  if (!rc) rc = host_mapped(&s->comp_h, &s->comp_d, kReqSlots, "serve completion");
+  if (!rc) rc = host_mapped(&s->stop_h, &s->stop_d, 1, "serve stop");
+  if (!rc) rc = check_cuda(cudaMalloc(&s->req_done, sizeof(unsigned int) * kReqSlots), "req_done");
+  if (!rc) rc = check_cuda(cudaMemset(s->req_done, 0, sizeof(unsigned int) * kReqSlots), "req_done");
+  if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&s->setup, cudaStreamNonBlocking), "setup stream");
+  if (!rc) rc = check_cuda(cudaDeviceSynchronize(), "serve init");
+  if (rc) {
+    destroy_server(s);
+    return rc;
+  }
+  *server = s;
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_server_walker_create(lufqhe_server_t *s, int n, int k, const double *z_host,
+                                           int *walker_id) {
+  if (!s || !z_host || !walker_id || k < 1 || k > s->max_k) {
+    set_error("lufqhe_server_walker_create: invalid argument (k must be 1..%d)", s ? s->max_k : 0);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  const int cls = class_index(s, n);
+  if (cls < 0) {
+    set_error("lufqhe_server_walker_create: no class for n=%d", n);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  const size_t bytes = (size_t)k * n * n * sizeof(double2) + (size_t)k * n * sizeof(double2);
+  size_t off = 0;
+  if (pool_alloc(s, bytes, &off) != LUFQHE_SUCCESS) {
+    set_error("lufqhe_server_walker_create: HBM budget exhausted (%zu bytes needed)", bytes);
+    return LUFQHE_ERR_BUSY;
+  }
+  int id = -1;
+  for (size_t w = 0; w < s->walkers.size(); ++w)
+    if (!s->walkers[w].live) {
+      id = (int)w;
+      break;
+    }
+  if (id < 0) {
+    id = (int)s->walkers.size();
+    s->walkers.emplace_back();
+  }
+  Walker &W = s->walkers[id];
+  W.live = true;
+  W.n = n;
+  W.k = k;
+  W.cls = cls;
+  W.offset = off;
+  W.bytes = bytes;
+  W.busy = false;
+  double2 *mats = reinterpret_cast<double2 *>(s->pool + off);
+  double2 *z = mats + (size_t)k * n * n;
+  cudaStream_t st = s->setup;
+  int rc = check_cuda(cudaMemcpyAsync(z, z_host, (size_t)k * n * sizeof(double2),
+                                      cudaMemcpyHostToDevice, st),
+                      "walker z upload");
+  if (!rc) {
+    build_walker_kernel<<<std::max(1, std::min(1024, (k * n + 255) / 256)), 256, 0, st>>>(mats, z,
+                                                                                       n, k);
+    rc = check_cuda(cudaGetLastError(), "build_walker_kernel");
+  }
+  if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "walker build");
+  if (rc) {
+    pool_free(s, off, bytes);
+    W.live = false;
+    return rc;
+  }
+  *walker_id = id;
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_server_walker_destroy(lufqhe_server_t *s, int walker_id) {
+  if (!s) return LUFQHE_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (walker_id < 0 || walker_id >= (int)s->walkers.size() || !s->walkers[walker_id].live) {
+    set_error("lufqhe_server_walker_destroy: unknown walker %d", walker_id);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  Walker &W = s->walkers[walker_id];
+  if (W.busy) {
+    set_error("lufqhe_server_walker_destroy: walker %d has a move in flight", walker_id);
+    return LUFQHE_ERR_BUSY;
+  }
+  pool_free(s, W.offset, W.bytes);
+  W.live = false;
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int particle,
+                                    const double *znew_host, long long *ticket) {
+  if (!s || !ticket) return LUFQHE_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (walker_id < 0 || walker_id >= (int)s->walkers.size() || !s->walkers[walker_id].live) {
+    set_error("lufqhe_server_submit: unknown walker %d", walker_id);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  Walker &W = s->walkers[walker_id];
+  if (W.busy) {
+    set_error("lufqhe_server_submit: walker %d already has a move in flight", walker_id);
+    return LUFQHE_ERR_BUSY;
+  }
+  if (particle >= W.n || (particle >= 0 && !znew_host)) {
+    set_error("lufqhe_server_submit: bad particle %d", particle);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  // a free request slot
+  int slot = -1;
+  for (int r = 0; r < kReqSlots; ++r)
+    if (!s->slots[r].used) {
+      slot = r;
+      break;
+    }
+  if (slot < 0) {
+    set_error("lufqhe_server_submit: all %d request slots in flight", kReqSlots);
+    return LUFQHE_ERR_BUSY;
+  }
+  SClass &C = s->classes[W.cls];
+  const unsigned int ntiles = (unsigned int)((W.k + s->tile - 1) / s->tile);
+  // ring space: tiles of the oldest in-flight request of this class bound the reuse
+  unsigned int oldest = C.published;
+  for (int r = 0; r < kReqSlots; ++r)
+    if (s->slots[r].used && s->slots[r].cls == W.cls) oldest = std::min(oldest, s->slots[r].first_tile);
+  if (C.published + ntiles - oldest > kRing) {
+    set_error("lufqhe_server_submit: tile ring of class n=%d is full", W.n);
+    return LUFQHE_ERR_BUSY;
+  }
+  const size_t sbase = (size_t)slot * s->max_k;
+  if (particle >= 0) memcpy(s->znew_h + sbase, znew_host, sizeof(double2) * W.k);
+  ReqSlot &R = s->slots[slot];
+  R.used = true;
+  R.walker = walker_id;
+  R.k = W.k;
+  R.cls = W.cls;
+  R.seq = s->next_seq++;
+  if (s->next_seq == 0) s->next_seq = 1;
+  R.first_tile = C.published;
+  R.last_tile = C.published + ntiles;
+  __atomic_store_n(&s->comp_h[slot], 0u, __ATOMIC_RELAXED);
+  double2 *mats = reinterpret_cast<double2 *>(s->pool + W.offset);
+  double2 *z = mats + (size_t)W.k * W.n * W.n;
+  for (unsigned int t = 0; t < ntiles; ++t) {
+    const int first = (int)t * s->tile;
+    ServeTile T;
+    T.mats = mats + (size_t)first * W.n * W.n;
+    T.z = z + (size_t)first * W.n;
+    T.znew = particle >= 0 ? s->znew_d + sbase + first : nullptr;
+    T.logabs = s->la_d + sbase + first;
+    T.phase = s->ph_d + sbase + first;
+    T.status = s->st_d + sbase + first;
+    T.req_done = s->req_done + slot;
+    T.completion = s->comp_d + slot;
+    T.seq = R.seq;
+    T.req_tiles = ntiles;
+    T.count = std::min(s->tile, W.k - first);
+    T.particle = particle;
+    s->classes[W.cls].ring_h[(C.published + t) % kRing] = T;
+  }
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  C.published += ntiles;
+  __atomic_store_n(C.pub_h, C.published, __ATOMIC_RELEASE);
+  int rc = ensure_running(s, C);
+  if (rc) return rc;
+  W.busy = true;
+  *ticket = ((long long)R.seq << 16) | slot;
+  return LUFQHE_SUCCESS;
+}
+
+// 0 = done (results copied if pointers given), LUFQHE_ERR_BUSY = not yet,
+// LUFQHE_ERR_TIMEOUT = not done within wait_us.
+extern "C" int lufqhe_server_poll(lufqhe_server_t *s, long long ticket, int wait_us,
+                                  double *logabs, double *phase, int32_t *status) {
+  if (!s) return LUFQHE_ERR_INVALID_ARG;
+  const int slot = (int)(ticket & 0xffff);
+  const unsigned int seq = (unsigned int)(ticket >> 16);
+  if (slot < 0 || slot >= kReqSlots) return LUFQHE_ERR_INVALID_ARG;
+  const double t0 = now_s();
+  int spins = 0;
+  for (;;) {
+    if (__atomic_load_n(&s->comp_h[slot], __ATOMIC_ACQUIRE) == seq) break;
+    // a class loop that gave up while idle (racing a publish) is relaunched
+    if ((spins++ & 255) == 0) {
+      std::lock_guard<std::mutex> lock(s->mu);
+      ReqSlot &R = s->slots[slot];
+      if (R.used && R.seq == seq) {
+        int rc = ensure_running(s, s->classes[R.cls]);
+        if (rc) return rc;
+      }
+    }
+    if (wait_us == 0) return LUFQHE_ERR_BUSY;
+    if ((now_s() - t0) * 1e6 > wait_us) return LUFQHE_ERR_TIMEOUT;
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  ReqSlot &R = s->slots[slot];
+  if (!R.used || R.seq != seq) {
+    set_error("lufqhe_server_poll: stale ticket");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  const size_t sbase = (size_t)slot * s->max_k;
+  if (logabs) memcpy(logabs, s->la_h + sbase, sizeof(double) * R.k);
+  if (phase) memcpy(phase, s->ph_h + sbase, sizeof(double) * R.k);
+  if (status) memcpy(status, s->st_h + sbase, sizeof(int32_t) * R.k);
+  s->walkers[R.walker].busy = false;
+  R.used = false;
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_server_destroy(lufqhe_server_t *s) {
+  destroy_server(s);
+  return LUFQHE_SUCCESS;
+}
+
+// Simulated Monte Carlo walker stream (Poisson arrivals of move requests).
+// Walkers: k log-uniform in [k_min, k_max], n uniform over the server's
+// classes; each makes `moves` single-particle moves; a request arrives at the
+// Poisson schedule time (rate `rate_hz`) or, if its walker's previous move is
+// still running, when that move completes. Walkers are admitted against the HBM
+// budget (a walker that does not fit waits for one to finish). Per request the
+// latency from its arrival to its completion is written to lat_us (capacity
+// max_records), and the request's n to rec_n. Returns the number recorded;
+// *elapsed_s gets the wall time and *matrices the determinants computed.
+extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz,
+                                              long long nrequests, int moves, int k_min, int k_max,
+                                              unsigned long long seed, double *lat_us, int *rec_n,
+                                              long long max_records, double *elapsed_s,
+                                              long long *matrices) {
+  if (!s || rate_hz <= 0 || nrequests < 1 || moves < 1 || k_min < 1 || k_max < k_min ||
+      k_max > s->max_k) {
+    set_error("lufqhe_server_run_stream: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  std::mt19937_64 rng(seed);
+  std::exponential_distribution<double> gap(rate_hz);
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  std::normal_distribution<double> gauss(0.0, 1.0);
+  struct Active {
+    int id;
+    int n, k;
+    int moves_left;
+    long long ticket;
+    double arrival;
+    bool in_flight;
+  };
+  std::vector<Active> act;
+  std::vector<double> zbuf;
+  const int nclass = (int)s->classes.size();
+  long long issued = 0, recorded = 0, mats = 0;
+  double next_arrival = now_s();
+  const double start = next_arrival;
+  // pending arrivals not yet bound to a walker (arrival times)
+  std::vector<double> pending;
+  while (recorded < nrequests) {
+    const double t = now_s();
+    // arrivals due
+    while (issued < nrequests && next_arrival <= t) {
+      pending.push_back(next_arrival);
+      next_arrival += gap(rng);
+      ++issued;
+    }
+    // bind pending arrivals: to an idle walker with moves left, else a new walker
+    for (size_t p = 0; p < pending.size();) {
+      int use = -1;
+      for (size_t a = 0; a < act.size(); ++a)
+        if (!act[a].in_flight && act[a].moves_left > 0) {
+          use = (int)a;
+          break;
+        }
+      if (use < 0) {
+        const int n = s->classes[(int)(uni(rng) * nclass) % nclass].n;
+        const double lk = std::log((double)k_min) +
+                          uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
+        const int k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
+        const double sig = std::sqrt((double)n / 2.0);
+        zbuf.resize((size_t)2 * k * n);
+        for (auto &v : zbuf) v = gauss(rng) * sig;
+        int id = -1;
+        int rc = lufqhe_server_walker_create(s, n, k, zbuf.data(), &id);
+        if (rc == LUFQHE_ERR_BUSY) break;  // HBM budget: wait for walkers to finish
+        if (rc) return rc;
+        act.push_back({id, n, k, moves, 0, 0.0, false});
+        use = (int)act.size() - 1;
+      }
+      Active &A = act[use];
+      const int particle = (int)(uni(rng) * A.n) % A.n;
+      zbuf.resize((size_t)2 * A.k);
+      const double sig = std::sqrt((double)A.n / 2.0);
+      for (auto &v : zbuf) v = gauss(rng) * sig;
+      long long ticket = 0;
+      int rc = lufqhe_server_submit(s, A.id, particle, zbuf.data(), &ticket);
+      if (rc == LUFQHE_ERR_BUSY) break;  // ring or slots full: retry next pass
+      if (rc) return rc;
+      A.ticket = ticket;
+      A.arrival = pending[p];
+      A.in_flight = true;
+      pending.erase(pending.begin() + p);
+    }
+    // completions
+    for (size_t a = 0; a < act.size();) {
+      Active &A = act[a];
+      if (A.in_flight) {
+        int rc = lufqhe_server_poll(s, A.ticket, 0, nullptr, nullptr, nullptr);
+        if (rc == LUFQHE_SUCCESS) {
+          const double done = now_s();
+          if (recorded < max_records) {
+            lat_us[recorded] = (done - A.arrival) * 1e6;
+            if (rec_n) rec_n[recorded] = A.n;
+          }
+          ++recorded;
+          mats += A.k;
+          A.in_flight = false;
+          if (--A.moves_left == 0) {
+            rc = lufqhe_server_walker_destroy(s, A.id);
+            if (rc) return rc;
+            act.erase(act.begin() + a);
+            continue;
+          }
+        } else if (rc != LUFQHE_ERR_BUSY) {
+          return rc;
+        }
+      }
+      ++a;
+    }
+  }
+  if (elapsed_s) *elapsed_s = now_s() - start;
+  if (matrices) *matrices = mats;
+  // retire the remaining walkers
+  for (auto &A : act) lufqhe_server_walker_destroy(s, A.id);
+  return std::min(recorded, max_records);
+}

@@ -145,3 +145,177 @@ def gen_lll_host(batch: int, n: int, seed: int, sigma: float | None = None):
     rc = lib().lufqhe_gen_lll_host(A.ctypes.data, z.ctypes.data, n, n, batch, seed, sigma)
     _native.check(rc, "lufqhe_gen_lll_host")
     return A, z
+
+
+class Plan:
+    """A mixed-size batch (groups of same-size matrices) in one persistent,
+    graph-captured launch: wraps lufqhe_plan_create/execute/destroy.
+
+    groups: list of (A, out_offset) with A a (count, n, lda) complex128 CUDA
+    tensor; results land in `out` at out_offset .. out_offset + count - 1.
+    The tensors must stay alive (and at the same address) while the plan lives.
+    """
+
+    def __init__(self, groups, out: DetResult, mode: int = MODE_MIXED, autotune: bool = True,
+                 stream=None):
+        import ctypes
+        self._h = None
+        self._keep = [A for A, _ in groups]
+        arr = (_native.Group * max(1, len(groups)))()
+        for i, (A, off) in enumerate(groups):
+            count, n, lda = _shape(A, None)
+            arr[i].A = A.data_ptr()
+            arr[i].n = n
+            arr[i].lda = lda
+            arr[i].count = count
+            arr[i].out_offset = off
+        self.out = out
+        h = ctypes.c_void_p()
+        rc = lib().lufqhe_plan_create(ctypes.byref(h), arr, len(groups), mode,
+                                      out.logabs.data_ptr(), out.phase.data_ptr(),
+                                      out.parity.data_ptr(), out.status.data_ptr(),
+                                      1 if autotune else 0, _stream_ptr(stream))
+        _native.check(rc, "lufqhe_plan_create")
+        self._h = h
+
+    def execute(self, stream=None, graph: bool = True):
+        fn = lib().lufqhe_plan_execute if graph else lib().lufqhe_plan_launch_direct
+        _native.check(fn(self._h, _stream_ptr(stream)), "lufqhe_plan_execute")
+
+    def describe(self) -> dict:
+        import ctypes
+        import json
+        buf = ctypes.create_string_buffer(8192)
+        _native.check(lib().lufqhe_plan_describe(self._h, buf, len(buf)), "lufqhe_plan_describe")
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if self._h:
+            lib().lufqhe_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Device-resident walkers and the persistent request loop (lufqhe_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int, mode: int = MODE_MIXED, classes=(8, 16, 32, 64),
+                 class_sms=None, max_k: int = 4096, tile: int = 8):
+        import ctypes
+        self._h = None
+        cn = (ctypes.c_int * len(classes))(*classes)
+        cs = (ctypes.c_int * len(classes))(*class_sms) if class_sms else None
+        h = ctypes.c_void_p()
+        rc = lib().lufqhe_server_create(ctypes.byref(h), int(hbm_budget_bytes), mode, cn, cs,
+                                        len(classes), max_k, tile)
+        _native.check(rc, "lufqhe_server_create")
+        self._h = h
+        self.max_k = max_k
+
+    def walker(self, z):
+        """z: (k, n) complex128 numpy array of particle coordinates -> walker id."""
+        import ctypes
+
+        import numpy as np
+        z = np.ascontiguousarray(z, dtype=np.complex128)
+        k, n = z.shape
+        wid = ctypes.c_int()
+        rc = lib().lufqhe_server_walker_create(self._h, n, k, z.ctypes.data, ctypes.byref(wid))
+        if rc == -5:
+            return None  # HBM budget exhausted
+        _native.check(rc, "lufqhe_server_walker_create")
+        return wid.value
+
+    def destroy_walker(self, wid: int):
+        _native.check(lib().lufqhe_server_walker_destroy(self._h, wid), "walker_destroy")
+
+    def submit(self, wid: int, particle: int, znew=None):
+        import ctypes
+
+        import numpy as np
+        t = ctypes.c_longlong()
+        ptr = None
+        if znew is not None:
+            znew = np.ascontiguousarray(znew, dtype=np.complex128)
+            ptr = znew.ctypes.data
+        rc = lib().lufqhe_server_submit(self._h, wid, particle, ptr, ctypes.byref(t))
+        _native.check(rc, "lufqhe_server_submit")
+        return t.value
+
+    def result(self, ticket: int, k: int, wait_us: int = 10_000_000):
+        import numpy as np
+        la = np.empty(k)
+        ph = np.empty(k)
+        st = np.empty(k, np.int32)
+        rc = lib().lufqhe_server_poll(self._h, ticket, wait_us, la.ctypes.data, ph.ctypes.data,
+                                      st.ctypes.data)
+        _native.check(rc, "lufqhe_server_poll")
+        return la, ph, st
+
+    def run_stream(self, rate_hz: float, nrequests: int, moves: int = 100, k_min: int = 1,
+                   k_max: int = 4096, seed: int = 5):
+        import ctypes
+
+        import numpy as np
+        lat = np.empty(nrequests)
+        ns = np.empty(nrequests, np.int32)
+        el = ctypes.c_double()
+        mats = ctypes.c_longlong()
+        r = lib().lufqhe_server_run_stream(self._h, rate_hz, nrequests, moves, k_min, k_max, seed,
+                                           lat.ctypes.data, ns.ctypes.data, nrequests,
+                                           ctypes.byref(el), ctypes.byref(mats))
+        if r < 0:
+            _native.check(int(r), "lufqhe_server_run_stream")
+        return lat[:r], ns[:r], el.value, mats.value
+
+    def close(self):
+        if self._h:
+            lib().lufqhe_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pair_sum(out: DetResult, stream=None):
+    """log|S| and arg S of S = sum_i det(A_2i) det(A_2i+1) (device computation)."""
+    import torch
+    res = torch.empty(2, dtype=torch.float64, device=out.logabs.device)
+    rc = lib().lufqhe_pair_sum(out.logabs.data_ptr(), out.phase.data_ptr(), out.logabs.numel(),
+                               res.data_ptr(), _stream_ptr(stream))
+    _native.check(rc, "lufqhe_pair_sum")
+    return res
+
+
+def combine_log_sums(parts):
+    """Complex log-sum-exp of partial sums given as (log|S_r|, arg S_r) pairs:
+    the host-side reduction of per-rank (or per-batch) wavefunction sums."""
+    parts = [(float(a), float(b)) for a, b in parts if a == a and a != float("-inf")]
+    if not parts:
+        return float("-inf"), 0.0
+    m = max(a for a, _ in parts)
+    re = sum(math.exp(a - m) * math.cos(b) for a, b in parts)
+    im = sum(math.exp(a - m) * math.sin(b) for a, b in parts)
+    return m + math.log(math.hypot(re, im)), math.atan2(im, re)
+
+
+def allreduce_log_sum(part, group=None):
+    """Combine one (log|S|, arg S) per rank over torch.distributed (any
+    backend): all-gather the pairs, then the same log-sum-exp on every rank.
+    The replicas' only exchange (LU-fqhe/src/MonteCarloLoop.cu:373-392)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(part[0]), float(part[1])], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        t = t.cuda()
+    outs = [torch.empty_like(t) for _ in range(dist.get_world_size(group))]
+    dist.all_gather(outs, t, group=group)
+    return combine_log_sums([(o[0].item(), o[1].item()) for o in outs])

@@ -25,6 +25,19 @@ SIGNATURES = {
     "lufqhe_batch_lup_factor_inplace": (I32, [P, I32, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_lucoregpu_call": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),
+    "lufqhe_pair_sum": (I32, [P, P, I64, P, P]),
+    "lufqhe_plan_create": (I32, [P, P, I32, I32, P, P, P, P, I32, P]),
+    "lufqhe_plan_execute": (I32, [P, P]),
+    "lufqhe_plan_launch_direct": (I32, [P, P]),
+    "lufqhe_plan_describe": (I32, [P, P, _c.c_size_t]),
+    "lufqhe_plan_destroy": (I32, [P]),
+    "lufqhe_server_create": (I32, [P, _c.c_size_t, I32, P, P, I32, I32, I32]),
+    "lufqhe_server_walker_create": (I32, [P, I32, I32, P, P]),
+    "lufqhe_server_walker_destroy": (I32, [P, I32]),
+    "lufqhe_server_submit": (I32, [P, I32, I32, P, P]),
+    "lufqhe_server_poll": (I32, [P, I64, I32, P, P, P]),
+    "lufqhe_server_destroy": (I32, [P]),
+    "lufqhe_server_run_stream": (I64, [P, F64, I64, I32, I32, I32, U64, P, P, I64, P, P]),
     "lufqhe_gen_gaussian": (I32, [P, I32, I32, I64, U64, F64, P]),
     "lufqhe_gen_lll": (I32, [P, P, I32, I32, I64, U64, F64, P]),
     "lufqhe_gen_gaussian_host": (I32, [P, I32, I32, I64, U64, F64]),
@@ -40,6 +53,11 @@ SIGNATURES = {
 _lib = None
 
 
+class Group(ctypes.Structure):
+    """lufqhe_group_t"""
+    _fields_ = [("A", P), ("n", I32), ("lda", I32), ("count", I64), ("out_offset", I64)]
+
+
 def header_constants() -> dict[str, int]:
     """#define NAME value pairs from include/lufqhe.h (integers only)."""
     out = {}
@@ -52,7 +70,8 @@ def header_constants() -> dict[str, int]:
 
 def header_functions() -> list[str]:
     text = (INCLUDE / "lufqhe.h").read_text()
-    return re.findall(r"^\s*(?:const\s+)?[\w]+\s*\*?\s*(lufqhe_\w+)\s*\(", text, re.M)
+    return re.findall(r"^\s*(?:const\s+)?(?:(?:unsigned|long)\s+)*[\w]+\s*\*?\s*(lufqhe_\w+)\s*\(",
+                      text, re.M)
 
 
 def load(path: Path | None = None) -> ctypes.CDLL:

@@ -63,7 +63,7 @@ def test_config2_gaussian_n16(cuda, lufqhe_mod, oracle):
 def test_config3_lll_n24(cuda, lufqhe_mod, oracle):
     """Lowest-Landau-level orbital matrices n=24, z ~ CN(0, 24)."""
     A, _ = lufqhe_mod.gen_lll(4096, 24, seed=2)
-    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.10)
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.15)
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 6, 8, 12, 17, 31, 32, 33, 48, 64])

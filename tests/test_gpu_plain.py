@@ -195,3 +195,18 @@ def test_concurrent_streams_different_n(cuda, lufqhe_mod, oracle):
         want = oracle.lup_det(A.cpu().numpy(), arith=0)
         got = {k: getattr(o, k).cpu().numpy() for k in ("logabs", "phase", "parity", "status")}
         assert_parity(got, want)
+
+
+@pytest.mark.parametrize("batch", [1, 2, 9, 1000, 4097])
+def test_pair_sum_matches_oracle(cuda, lufqhe_mod, oracle, batch):
+    """Wavefunction pair sum (LUCoreCPU::CALL / globalReduction) on the GPU."""
+    A = lufqhe_mod.gen_gaussian(batch, 8, seed=batch)
+    out = lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64)
+    res = lufqhe_mod.pair_sum(out).cpu().numpy()
+    cuda.cuda.synchronize()
+    if batch < 2:
+        assert res[0] == -np.inf
+        return
+    la, ar = oracle.pair_sum(A.cpu().numpy())
+    assert abs(res[0] - la) < 1e-12 * max(1.0, abs(la))
+    assert dphase(res[1], ar) < 1e-11

@@ -1,0 +1,93 @@
+"""Serving: device-resident walkers, moves, HBM admission, and the same
+result for a walker alone and inside a mix of concurrent requests."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def lll_host(z):
+    """(k, n) particle coordinates -> (k, n, n) orbital matrices."""
+    n = z.shape[1]
+    return z[:, :, None] ** np.arange(n)[None, None, :] * np.exp(-np.abs(z) ** 2 / 4)[:, :, None]
+
+
+def zdraw(rng, k, n):
+    return (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))) * math.sqrt(n / 2)
+
+
+@pytest.fixture
+def server(lufqhe_mod, cuda):
+    srv = lufqhe_mod.Server(1 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(8, 16), max_k=256)
+    yield srv
+    srv.close()
+
+
+def test_move_matches_direct_determinant(server, oracle):
+    rng = np.random.default_rng(1)
+    z = zdraw(rng, 50, 16)
+    w = server.walker(z)
+    # no move: determinants of the initial matrices
+    la, ph, st = server.result(server.submit(w, -1), 50)
+    want, wph, _ = oracle.logdet_dd(lll_host(z))
+    ok = (st & 8) == 0
+    assert ok.mean() > 0.9
+    assert (np.abs(la - want) / np.maximum(1, np.abs(want))).max() < 1e-10
+    # move particle 5
+    znew = zdraw(rng, 50, 1)[:, 0]
+    la2, ph2, st2 = server.result(server.submit(w, 5, znew), 50)
+    z[:, 5] = znew
+    want2, wph2, _ = oracle.logdet_dd(lll_host(z))
+    assert (np.abs(la2 - want2) / np.maximum(1, np.abs(want2))).max() < 1e-10
+    d = np.abs(np.angle(np.exp(1j * (ph2 - wph2)))) / np.maximum(1, np.abs(want2))
+    assert d.max() < 1e-10
+    server.destroy_walker(w)
+
+
+def test_alone_and_in_mix_give_the_same_bits(server):
+    rng = np.random.default_rng(2)
+    z = zdraw(rng, 120, 16)
+    znew = zdraw(rng, 120, 1)[:, 0]
+    a = server.walker(z)
+    alone = server.result(server.submit(a, 3, znew), 120)
+    server.destroy_walker(a)
+    # the same walker and move among many other walkers' moves in flight
+    others = [server.walker(zdraw(rng, int(k), n)) for k, n in
+              zip(rng.integers(1, 256, 12), [8, 16] * 6)]
+    b = server.walker(z)
+    tickets = []
+    for i, w in enumerate(others[:6]):
+        tickets.append((w, server.submit(w, i % 8, zdraw(rng, 256, 1)[:, 0])))
+    tb = server.submit(b, 3, znew)
+    for i, w in enumerate(others[6:]):
+        tickets.append((w, server.submit(w, i % 8, zdraw(rng, 256, 1)[:, 0])))
+    mixed = server.result(tb, 120)
+    for w, t in tickets:
+        server.result(t, 256)
+    for x, y in zip(alone, mixed):
+        assert (np.ascontiguousarray(x).view(np.uint8) == np.ascontiguousarray(y).view(np.uint8)).all()
+    for w in others + [b]:
+        server.destroy_walker(w)
+
+
+def test_hbm_admission(lufqhe_mod, cuda):
+    n, k = 16, 256
+    per_walker = k * n * n * 16 + k * n * 16
+    srv = lufqhe_mod.Server(3 * per_walker + 4096, classes=(16,), max_k=256)
+    rng = np.random.default_rng(3)
+    ws = [srv.walker(zdraw(rng, k, n)) for _ in range(3)]
+    assert all(w is not None for w in ws)
+    assert srv.walker(zdraw(rng, k, n)) is None          # over budget
+    srv.destroy_walker(ws[1])
+    assert srv.walker(zdraw(rng, k, n)) is not None      # admitted once memory frees
+    srv.close()
+
+
+def test_walker_stream(server):
+    lat, ns, elapsed, mats = server.run_stream(rate_hz=5000, nrequests=400, moves=10, k_min=1,
+                                               k_max=256, seed=7)
+    assert len(lat) == 400 and np.isfinite(lat).all() and (lat > 0).all()
+    assert set(np.unique(ns)) <= {8, 16}
+    assert mats > 400 and elapsed > 0
