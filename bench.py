@@ -39,7 +39,11 @@ WORKLOADS = {
     "gauss8": ("gauss", 8, 4096, 0),
     # 200000 LLL matrices, n uniform over MIXED_SIZES, one persistent launch
     "mixedn": ("mixed", 0, 200000, 4),
+    # Monte Carlo walker stream: Poisson moves, k log-uniform 1..4096, n in
+    # SERVE_SIZES, 100 moves per walker, HBM-budgeted device-resident walkers
+    "serving": ("serve", 0, 0, 5),
 }
+SERVE_SIZES = (8, 16, 32, 64)
 MIXED_SIZES = (6, 8, 12, 16, 24, 32, 48)
 
 
@@ -367,6 +371,89 @@ def run_mixedn(args, world, rank, local):
     plan_p.close()
 
 
+def run_serving(args, world, rank, local):
+    """Serving: offline capacity per size class, then the walker stream at 70%
+    of it and at the configured 20k requests/s; p50/p99 latency (arrival to
+    result on the host) and throughput, mixed and FP64."""
+    import numpy as np
+    import torch
+
+    import lufqhe
+
+    torch.cuda.set_device(local)
+    seed = WORKLOADS["serving"][3]
+    rng = np.random.default_rng(seed)
+    ks = np.maximum(1, np.minimum(4096, np.floor(np.exp(rng.uniform(0, np.log(4097), 200000)))))
+    mean_k = float(ks.mean())
+
+    def offline_rate(n, mode):
+        count = max(512, min(32768, int(2e8 // (16 * n * n))))
+        A, _ = lufqhe.gen_lll(count, n, seed=seed * 100 + n)
+        out = lufqhe.batch_lup_det(A, mode=mode)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            lufqhe.batch_lup_det(A, mode=mode, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        return count / (e0.elapsed_time(e1) / 3 * 1e-3)
+
+    result = {}
+    launches = 0
+    for label, mode in (("mixed", lufqhe.MODE_MIXED), ("fp64", lufqhe.MODE_PLAIN_FP64_FUSED)):
+        rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
+        launches += 4 * len(SERVE_SIZES)
+        sec_per_matrix = float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
+        offline_mps = 1.0 / sec_per_matrix                  # matrices/s of the mix
+        cap_req = offline_mps / mean_k                      # requests/s at full load
+        inv = np.array([1.0 / rates[n] for n in SERVE_SIZES])
+        sms = np.maximum(2, np.round(152 * inv / inv.sum())).astype(int)
+        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
+        srv = lufqhe.Server(64 << 30, mode=mode, classes=SERVE_SIZES, class_sms=list(map(int, sms)),
+                            max_k=4096, tile=8)
+        runs = {}
+        for tag, rate, nreq in (("at_70pct_offline", 0.7 * cap_req, args.serve_requests),
+                                ("at_20k_req_s", 20000.0, max(200, args.serve_requests // 4))):
+            lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nreq, moves=100, k_min=1,
+                                               k_max=4096, seed=seed)
+            per = {}
+            for n in SERVE_SIZES:
+                m = ns == n
+                if m.any():
+                    per[str(n)] = {"p50_ms": float(np.percentile(lat[m], 50) / 1e3),
+                                   "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
+                                   "requests": int(m.sum())}
+            runs[tag] = {"rate_req_s": rate, "requests": int(len(lat)),
+                         "p50_ms": float(np.percentile(lat, 50) / 1e3),
+                         "p99_ms": float(np.percentile(lat, 99) / 1e3),
+                         "throughput_dets_s": mats / el,
+                         "fraction_of_offline": (mats / el) / offline_mps,
+                         "per_n": per}
+        srv.close()
+        result[label] = {"offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
+                         "offline_mix_dets_per_s": offline_mps,
+                         "offline_capacity_req_s": cap_req, "class_sms": list(map(int, sms)),
+                         "runs": runs}
+    if rank == 0:
+        r70 = result["mixed"]["runs"]["at_70pct_offline"]
+        line = {
+            "metric": "serving: determinants/s at 70% of offline load, with p50/p99 latency",
+            "value": r70["throughput_dets_s"], "unit": "dets/s", "n_gpus": world,
+            "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 in / fp32+float-float compute / f64 out",
+            "data": "synthetic (seeded Poisson walker stream)",
+            "config": {"workload": "serving: Poisson move requests, k log-uniform 1..4096, "
+                                   "n in (8,16,32,64), 100 moves per walker, walkers resident in "
+                                   "HBM (64 GiB budget)", "mean_k": mean_k},
+            "p50_ms": r70["p50_ms"], "p99_ms": r70["p99_ms"],
+            "serving": result, "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -376,6 +463,8 @@ def run_ours(args):
     world, rank, local = dist_setup(args)
     if args.workload == "mixedn":
         return run_mixedn(args, world, rank, local)
+    if args.workload == "serving":
+        return run_serving(args, world, rank, local)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
@@ -548,8 +637,8 @@ def run_reference(args):
         return lufqhe.gen_gaussian_host(count, n, seed=seed)
 
     kind, n, batch, seed = WORKLOADS[args.workload]
-    if kind == "mixed":  # the reference factorises one size at a time; time n=24
-        kind, n = "lll", 24
+    if kind in ("mixed", "serve"):  # the reference factorises one size at a time; n=24
+        kind, n, batch = "lll", 24, 32768
     line = bench_cpu.reference_arm(np, args, kind, n, batch, seed, make_inputs)
     line["n_gpus"] = world
     print(json.dumps(line), flush=True)
@@ -564,6 +653,7 @@ def main():
     ap.add_argument("--workload", default="lll24", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-sample", type=int, default=8192)
+    ap.add_argument("--serve-requests", type=int, default=4000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sys.path.insert(0, str(ROOT / "oracle"))

@@ -51,6 +51,8 @@ extern "C" {
 #define LUFQHE_ST_SINGULAR 2   /* exact zero pivot: logabs = -inf, phase = 0 */
 #define LUFQHE_ST_NONFINITE 4  /* NaN/Inf in the input: logabs = phase = NaN */
 #define LUFQHE_ST_FALLBACK 8   /* mixed mode: refactorised in FP64 (result is the FP64 one) */
+#define LUFQHE_ST_FP64 16      /* mixed mode: routed straight to the FP64 routine so the FP64
+                                  pipe works beside the FP32 pipes (result is the FP64 one) */
 
 /* ---- element types ---- */
 #define LUFQHE_C128 0
@@ -228,6 +230,15 @@ int lufqhe_gen_gaussian_host(double *A, int n, int lda, long long batch, unsigne
 int lufqhe_gen_lll_host(double *A, double *z, int n, int lda, long long batch,
                         unsigned long long seed, double sigma);
 
+/* ---- reference input files ---- */
+/* Reads matrices [first, first + count) of a raw file of n x n complex64
+ * matrices (interleaved float32, row-major, back to back: the format
+ * PermHandler reads, LU-fqhe/src/PermHandler.cpp:91-170) into host memory as
+ * complex128 with row stride lda. Returns the number of whole matrices read
+ * (fewer at the end of the file) or a negative error. n <= 512. */
+long long lufqhe_read_matrices_f32(const char *path, int n, long long first, long long count,
+                                   int lda, double *out);
+
 /* ---- options (process-wide, read when a call is issued) ---- */
 /* ||E||_F above which the mixed mode refactorises a matrix in FP64 (default
  * 0.1; 0 sends every matrix to the FP64 path, +inf disables the fallback
@@ -236,6 +247,11 @@ int lufqhe_gen_lll_host(double *A, double *z, int n, int lda, long long batch,
 /* Warps per CTA of the register-tiled mixed kernels (n in {6,8,12,16,24,32});
  * 0 = library default. */
 #define LUFQHE_OPT_TILE_WARPS 2
+/* Fraction (0..1) of the matrices the batched mixed mode sends straight to the
+ * FP64 routine, chosen by a hash of each matrix's first entry (so a matrix
+ * takes the same path wherever it sits); the FP64 pipe then works beside the
+ * FP32 pipes. A negative value restores the per-n default. */
+#define LUFQHE_OPT_FP64_SHARE 3
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

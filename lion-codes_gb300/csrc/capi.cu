@@ -153,6 +153,7 @@ extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, 
 namespace lufqhe {
 extern float g_mixed_theta;
 extern int g_tile_warps;
+extern float g_fp64_share;
 }
 
 extern "C" int lufqhe_set_option(int option, double value) {
@@ -172,6 +173,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_tile_warps = (int)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_FP64_SHARE) {
+    if (!(value <= 1.0)) {
+      set_error("lufqhe_set_option: FP64 share must be <= 1 (negative = default)");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_fp64_share = (float)value;
+    return LUFQHE_SUCCESS;
+  }
   set_error("lufqhe_set_option: unknown option %d", option);
   return LUFQHE_ERR_INVALID_ARG;
 }
@@ -179,6 +188,7 @@ extern "C" int lufqhe_set_option(int option, double value) {
 extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_MIXED_THRESHOLD) return (double)g_mixed_theta;
   if (option == LUFQHE_OPT_TILE_WARPS) return (double)g_tile_warps;
+  if (option == LUFQHE_OPT_FP64_SHARE) return (double)g_fp64_share;
   return NAN;
 }
 

@@ -28,6 +28,8 @@
 
 namespace lufqhe {
 
+unsigned int fp64_share_64k(int n);
+
 namespace {
 
 using namespace mixed;
@@ -39,7 +41,7 @@ struct WorkItem {
   int count;         // matrices in the tile
   int n;
   int lda;
-  int pad;
+  unsigned int share64k;  // mixed mode: share routed straight to FP64 (1/65536)
 };
 
 size_t warp_smem_bytes(int nmax) {
@@ -51,10 +53,15 @@ size_t warp_smem_bytes(int nmax) {
 template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int lane, float theta2,
-                               DeferredOut &out, double *logabs, double *phase, int8_t *parity,
-                               int32_t *status) {
+                               unsigned int share64k, DeferredOut &out, double *logabs,
+                               double *phase, int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
+  if (MODE == LUFQHE_MODE_MIXED && route_fp64(src, share64k)) {
+    fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
+                  LUFQHE_ST_FP64);
+    return;
+  }
   if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
     emit_nonfinite(lane, ob, logabs, phase, parity, status);
     return;
@@ -140,7 +147,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, lane, theta2, out, logabs, phase, parity, status);
+                           ec, lane, theta2, w.share64k, out, logabs, phase, parity, status);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -185,8 +192,9 @@ struct lufqhe_plan_s {
   int8_t *parity = nullptr;
   int32_t *status = nullptr;
   float theta2 = 0.01f;
-  // per-group tile size chosen by the tuner
+  // per-group tile size and FP64 share (1/65536) chosen by the tuner
   std::vector<int> tile;
+  std::vector<unsigned int> share;
   Launch launch;
   // device state
   WorkItem *d_items = nullptr;
@@ -218,7 +226,7 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
       w.count = (int)std::min<long long>(T, G.count - f);
       w.n = G.n;
       w.lda = G.lda;
-      w.pad = 0;
+      w.share64k = p->mode == LUFQHE_MODE_MIXED ? p->share[g] : 0u;
       items.push_back(w);
     }
   }
@@ -306,6 +314,7 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   const int all_nmax = p->nmax;
   int rc = configure_launch(p, 4);
   if (rc) return rc;
+  std::vector<unsigned int> base_share = p->share;
   for (size_t g = 0; g < all.size(); ++g) {
     if (all[g].count == 0) continue;
     p->groups.assign(1, all[g]);
@@ -314,25 +323,38 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
     if (rc) return rc;
     float best = 1e30f;
     int best_t = base_tile[g];
-    for (double f : {0.25, 0.5, 1.0, 2.0, 4.0}) {
-      int T = std::max(1, std::min(1024, (int)std::lround(base_tile[g] * f)));
-      p->tile.assign(1, T);
-      rc = build_items(p, s);
-      if (rc) return rc;
-      float ms = 0.0f;
-      rc = time_launch(p, s, &ms);
-      if (rc) return rc;
-      if (ms < best) {
-        best = ms;
-        best_t = T;
+    unsigned int best_s = base_share[g];
+    // precision policy: the default FP64 share, half, or everything in FP64
+    std::vector<unsigned int> shares = {base_share[g]};
+    if (p->mode == LUFQHE_MODE_MIXED) {
+      if (base_share[g] != 32768u) shares.push_back(32768u);
+      shares.push_back(65536u);
+    }
+    for (unsigned int sh : shares) {
+      for (double f : {0.25, 0.5, 1.0, 2.0, 4.0}) {
+        int T = std::max(1, std::min(1024, (int)std::lround(base_tile[g] * f)));
+        p->tile.assign(1, T);
+        p->share.assign(1, sh);
+        rc = build_items(p, s);
+        if (rc) return rc;
+        float ms = 0.0f;
+        rc = time_launch(p, s, &ms);
+        if (rc) return rc;
+        if (ms < best) {
+          best = ms;
+          best_t = T;
+          best_s = sh;
+        }
       }
     }
-    p->tile = base_tile;
     base_tile[g] = best_t;
-    snprintf(line, sizeof(line), "%s\"%d\": {\"tile\": %d, \"ms_alone\": %.4f, \"count\": %lld}",
-             g ? ", " : "", all[g].n, best_t, best, all[g].count);
+    base_share[g] = best_s;
+    snprintf(line, sizeof(line),
+             "%s\"%d\": {\"tile\": %d, \"fp64_share\": %.3f, \"ms_alone\": %.4f, \"count\": %lld}",
+             g ? ", " : "", all[g].n, best_t, best_s / 65536.0, best, all[g].count);
     p->report += line;
   }
+  p->share = base_share;
   p->groups = all;
   p->tile = base_tile;
   p->nmax = all_nmax;
@@ -435,6 +457,10 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
     }
     p->groups.push_back(G);
     p->tile.push_back(default_tile(G.n));
+    // as the batched mixed kernels: the per-n share for the register-tiled
+    // sizes, none for the others
+    const bool tiled = G.n == 6 || G.n == 8 || G.n == 12 || G.n == 16 || G.n == 24 || G.n == 32;
+    p->share.push_back(tiled ? fp64_share_64k(G.n) : 0u);
     p->nmax = std::max(p->nmax, G.n);
     p->total += G.count;
   }

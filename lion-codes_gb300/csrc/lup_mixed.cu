@@ -30,6 +30,27 @@
 namespace lufqhe {
 
 int g_tile_warps = 0;
+float g_fp64_share = -1.0f;  // < 0: per-n default
+
+// Share of matrices routed straight to FP64, per n, in 1/65536 units. The
+// defaults come from sweeps on GB300 (the share at which the FP64 pipe and the
+// FP32 pipes finish together); a caller may override them.
+unsigned int fp64_share_64k(int n) {
+  float s = g_fp64_share;
+  if (s < 0.0f) {
+    switch (n) {
+      case 6:
+      case 8: s = 0.0f; break;
+      case 12:
+      case 16: s = 0.25f; break;
+      case 24: s = 0.40f; break;
+      default: s = 0.50f; break;
+    }
+  }
+  if (s <= 0.0f) return 0u;
+  if (s >= 1.0f) return 65536u;
+  return (unsigned int)(s * 65536.0f);
+}
 
 namespace {
 
@@ -83,8 +104,9 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
 template <int N>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     lup_mixed_tile_kernel(const double2 *__restrict__ A, int lda, long long batch, float theta2,
-                          double *__restrict__ logabs, double *__restrict__ phase,
-                          int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+                          unsigned int share64k, double *__restrict__ logabs,
+                          double *__restrict__ phase, int8_t *__restrict__ parity,
+                          int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = N + 1;
   constexpr size_t NL = (size_t)N * LDS;
@@ -107,6 +129,11 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     __syncwarp();
     const double2 *src = A + (size_t)b * N * lda;
     double2 *M = reinterpret_cast<double2 *>(HL);
+    if (route_fp64(src, share64k)) {
+      fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                    LUFQHE_ST_FP64);
+      continue;
+    }
     if (load_matrix_fp64(src, N, lda, M, LDS, lane)) {
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
@@ -145,7 +172,8 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, logabs, phase, parity, status);
+  kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, fp64_share_64k(N), logabs,
+                                           phase, parity, status);
   return check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
 }
 

@@ -452,6 +452,19 @@ struct DeferredOut {
   }
 };
 
+// Route of a matrix in the batched mixed mode: true = straight to FP64. A hash
+// of its first entry's bits, so the route depends on the content only.
+__device__ __forceinline__ bool route_fp64(const double2 *src, unsigned int share64k) {
+  if (share64k == 0) return false;
+  const double2 v = __ldg(src);
+  unsigned long long h = (unsigned long long)__double_as_longlong(v.x) * 0x9E3779B97F4A7C15ull ^
+                         (unsigned long long)__double_as_longlong(v.y);
+  h ^= h >> 29;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 32;
+  return (unsigned int)(h & 0xffffu) < share64k;
+}
+
 __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *logabs,
                                                double *phase, int8_t *parity, int32_t *status) {
   if (lane == 0) {
@@ -466,7 +479,7 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
 template <bool COHERENT = false>
 __device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, int lds,
                               double *hold, int lane, long long b, double *logabs, double *phase,
-                              int8_t *parity, int32_t *status) {
+                              int8_t *parity, int32_t *status, int flag = LUFQHE_ST_FALLBACK) {
   __syncwarp();
   load_matrix_fp64<COHERENT>(src, n, lda, M, lds, lane);
   int par = 0;
@@ -486,7 +499,7 @@ __device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, in
     logabs[b] = la;
     if (phase) phase[b] = ph;
     if (parity) parity[b] = (int8_t)par;
-    if (status) status[b] = st | LUFQHE_ST_FALLBACK;
+    if (status) status[b] = st | flag;
   }
 }
 
@@ -508,6 +521,68 @@ struct TileGeom {
   static constexpr int SA = (N + 3) / 4;  // row slots per lane
   static constexpr int SB = (N + 7) / 8;  // column slots per lane
 };
+
+// Float-float residual for the row slots [A0, A1) of the 4 x 8 lane grid:
+// lane (r, c) owns entries (4a + r, 8b + c); R is written into the float2
+// view of HL (row stride N + 1).
+template <int N, int A0, int A1>
+__device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int lane) {
+  constexpr int LDS = N + 1;
+  constexpr int SB = TileGeom<N>::SB;
+  constexpr int NA = A1 - A0;
+  if constexpr (NA > 0) {
+    const int tr = lane >> 3, tc = lane & 7;
+    float4 acc[NA][SB];
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * (A0 + a) + tr, k = 8 * b + tc;
+        acc[a][b] = (i < N && k < N) ? HL[i * LDS + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    // rows of this pass end at 4 * A1; steps beyond their last row add nothing
+    constexpr int TEND = (4 * A1 < N) ? 4 * A1 : N;
+#pragma unroll 1
+    for (int t = 0; t < TEND; ++t) {
+      float2 Lv[NA], Uv[SB];
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        const int i = 4 * (A0 + a) + tr;
+        Lv[a] = make_float2(0.f, 0.f);
+        if (i == t) Lv[a] = make_float2(1.f, 0.f);
+        else if (i > t && i < N) Lv[a] = F[i * LDS + t];
+      }
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int k = 8 * b + tc;
+        Uv[b] = make_float2(0.f, 0.f);
+        if (k >= t && k < N) Uv[b] = F[t * LDS + k];
+      }
+      // slots whose rows and columns all lie before t have nothing left to add
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        if (4 * (A0 + a) + 3 < t) continue;
+#pragma unroll
+        for (int b = 0; b < SB; ++b) {
+          if (8 * b + 7 < t) continue;
+          dot2_csub(acc[a][b], Lv[a], Uv[b]);
+        }
+      }
+    }
+    float2 *Rm = reinterpret_cast<float2 *>(HL);
+    __syncwarp();
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * (A0 + a) + tr, k = 8 * b + tc;
+        if (i < N && k < N)
+          Rm[i * LDS + k] = make_float2(__fadd_rn(acc[a][b].x, acc[a][b].z),
+                                        __fadd_rn(acc[a][b].y, acc[a][b].w));
+      }
+    __syncwarp();
+  }
+}
 
 template <int N>
 __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane, float theta2,
@@ -602,57 +677,15 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
     __syncwarp();
   }
 
-  // 4. residual R = P A^ - L U (float-float) in a 4 x 8 lane grid
-  const int tr = lane >> 3, tc = lane & 7;
-  float4 acc[SA][SB];
-#pragma unroll
-  for (int a = 0; a < SA; ++a)
-#pragma unroll
-    for (int b = 0; b < SB; ++b) {
-      const int i = 4 * a + tr, k = 8 * b + tc;
-      acc[a][b] = (i < N && k < N) ? HL[i * LDS + k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll 1
-  for (int t = 0; t < N; ++t) {
-    float2 Lv[SA], Uv[SB];
-#pragma unroll
-    for (int a = 0; a < SA; ++a) {
-      const int i = 4 * a + tr;
-      Lv[a] = make_float2(0.f, 0.f);
-      if (i == t) Lv[a] = make_float2(1.f, 0.f);
-      else if (i > t && i < N) Lv[a] = F[i * LDS + t];
-    }
-#pragma unroll
-    for (int b = 0; b < SB; ++b) {
-      const int k = 8 * b + tc;
-      Uv[b] = make_float2(0.f, 0.f);
-      if (k >= t && k < N) Uv[b] = F[t * LDS + k];
-    }
-    // slots whose rows and columns all lie before t have nothing left to add
-#pragma unroll
-    for (int a = 0; a < SA; ++a) {
-      if (4 * a + 3 < t) continue;
-#pragma unroll
-      for (int b = 0; b < SB; ++b) {
-        if (8 * b + 7 < t) continue;
-        dot2_csub(acc[a][b], Lv[a], Uv[b]);
-      }
-    }
-  }
+  // 4. residual R = P A^ - L U (float-float) in a 4 x 8 lane grid, in two
+  //    passes over halves of the row slots (half the accumulator registers).
+  //    R overwrites the front of HL as a float2 array; pass 1 writes rows
+  //    below the ones pass 2 still reads, so the passes never collide.
+  residual_rows<N, 0, SA / 2>(HL, F, lane);
+  residual_rows<N, SA / 2, SA>(HL, F, lane);
   float2 *Rm = reinterpret_cast<float2 *>(HL);  // R, then E, row stride LDS
-  __syncwarp();
-#pragma unroll
-  for (int a = 0; a < SA; ++a)
-#pragma unroll
-    for (int b = 0; b < SB; ++b) {
-      const int i = 4 * a + tr, k = 8 * b + tc;
-      if (i < N && k < N)
-        Rm[i * LDS + k] = make_float2(__fadd_rn(acc[a][b].x, acc[a][b].z),
-                                      __fadd_rn(acc[a][b].y, acc[a][b].w));
-    }
-  __syncwarp();
 
-    // 5-6. solves, acceptance, log det(I + E) and the diagonal product: the
+  // 5-6. solves, acceptance, log det(I + E) and the diagonal product: the
   //      shared-memory forms of the generic path with n fixed at compile time
   return mixed_finish<1>(F, Rm, N, LDS, lane, theta2, exp_sum, prod, corr);
 }

@@ -25,6 +25,7 @@ ST_SCALE_TINY = 1
 ST_SINGULAR = 2
 ST_NONFINITE = 4
 ST_FALLBACK = 8
+ST_FP64 = 16
 
 MAX_N = 64
 
@@ -319,3 +320,19 @@ def allreduce_log_sum(part, group=None):
     outs = [torch.empty_like(t) for _ in range(dist.get_world_size(group))]
     dist.all_gather(outs, t, group=group)
     return combine_log_sums([(o[0].item(), o[1].item()) for o in outs])
+
+
+def read_matrices_f32(path, n: int, first: int = 0, count: int | None = None, lda: int | None = None):
+    """Matrices of a raw float32 complex file (the reference's input format)
+    as a (count, n, lda) complex128 numpy array."""
+    import os
+
+    import numpy as np
+    lda = n if lda is None else lda
+    if count is None:
+        count = os.path.getsize(path) // (8 * n * n) - first
+    out = np.zeros((max(0, count), n, lda), np.complex128)
+    got = lib().lufqhe_read_matrices_f32(str(path).encode(), n, first, count, lda, out.ctypes.data)
+    if got < 0:
+        _native.check(int(got), "lufqhe_read_matrices_f32")
+    return out[:got]

@@ -82,3 +82,16 @@ def test_host_lll_structure(lufqhe_mod):
     want = z[:, :, None] ** np.arange(n)[None, None, :] * w[:, :, None]
     assert np.abs(A - want).max() / np.abs(want).max() < 1e-12
     assert abs((np.abs(z) ** 2).mean() - n) < 0.25 * n
+
+
+def test_read_reference_file_format(lufqhe_mod, tmp_path):
+    """Raw interleaved complex64, row-major, back to back (PermHandler's format)."""
+    rng = np.random.default_rng(4)
+    M = (rng.random((7, 16, 16)) + 1j * rng.random((7, 16, 16))).astype(np.complex64)
+    p = tmp_path / "mats.bin"
+    M.tofile(p)
+    A = lufqhe_mod.read_matrices_f32(p, 16)
+    assert A.shape == (7, 16, 16) and (A == M.astype(np.complex128)).all()
+    B = lufqhe_mod.read_matrices_f32(p, 16, first=5, count=10, lda=32)   # short tail
+    assert B.shape == (2, 16, 32) and (B[:, :, :16] == M[5:].astype(np.complex128)).all()
+    assert (B[:, :, 16:] == 0).all()
