@@ -191,7 +191,8 @@ int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int 
                          const int *class_n, const int *class_sms, int nclasses, int max_k,
                          int tile);
 /* z_host: k*n complex128 particle coordinates. LUFQHE_ERR_BUSY when the HBM
- * budget is exhausted. Synchronous (uploads and builds the matrices). */
+ * budget is exhausted. Uploads the coordinates (synchronously); the matrices
+ * are built on the device by the walker's first request. */
 int lufqhe_server_walker_create(lufqhe_server_t *server, int n, int k, const double *z_host,
                                 int *walker_id);
 int lufqhe_server_walker_destroy(lufqhe_server_t *server, int walker_id);

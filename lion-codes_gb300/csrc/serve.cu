@@ -58,6 +58,8 @@ struct ServeTile {
   unsigned int req_tiles;
   int count;
   int particle;
+  int build;                 // 1: build every row from z first (a walker's first request)
+  int pad;
 };
 
 struct ClassCtl {              // device memory, one per class
@@ -76,24 +78,38 @@ __device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) 
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Row `particle` of each matrix of the tile: lane j rebuilds matrix j's row.
-__device__ void rebuild_rows(const ServeTile &t, int n, int lane) {
-  for (int j0 = 0; j0 < t.count; j0 += 32) {
-    const int j = j0 + lane;
-    if (j < t.count) {
-      const double2 z = __ldcv(t.znew + j);
-      t.z[(size_t)j * n + t.particle] = z;
-      double2 *row = t.mats + (size_t)j * n * n + (size_t)t.particle * n;
-      const double w = exp(-(z.x * z.x + z.y * z.y) * 0.25);
-      double px = 1.0, py = 0.0;
-      for (int k = 0; k < n; ++k) {
-        row[k] = make_double2(px * w, py * w);
-        const double nx = px * z.x - py * z.y;
-        const double ny = px * z.y + py * z.x;
-        px = nx;
-        py = ny;
+__device__ __forceinline__ void lll_row_dev(double2 z, int n, double2 *row) {
+  const double w = exp(-(z.x * z.x + z.y * z.y) * 0.25);
+  double px = 1.0, py = 0.0;
+  for (int k = 0; k < n; ++k) {
+    row[k] = make_double2(px * w, py * w);
+    const double nx = px * z.x - py * z.y;
+    const double ny = px * z.y + py * z.x;
+    px = nx;
+    py = ny;
+  }
+}
+
+// Apply the move to the tile's matrices: z_particle <- znew, then rebuild that
+// row (lane j handles matrix j); with t.build every row of every matrix is
+// built from z instead (lanes over rows), which is how a walker's matrices are
+// first made, inside the loop so no other kernel needs an SM.
+__device__ void apply_move(const ServeTile &t, int n, int lane) {
+  if (t.particle >= 0 && t.znew) {
+    for (int j0 = 0; j0 < t.count; j0 += 32) {
+      const int j = j0 + lane;
+      if (j < t.count) {
+        const double2 z = __ldcv(t.znew + j);
+        t.z[(size_t)j * n + t.particle] = z;
+        if (!t.build) lll_row_dev(z, n, t.mats + (size_t)j * n * n + (size_t)t.particle * n);
       }
     }
+    __syncwarp();
+  }
+  if (t.build) {
+    for (int j = 0; j < t.count; ++j)
+      for (int i = lane; i < n; i += 32)
+        lll_row_dev(__ldcg(t.z + (size_t)j * n + i), n, t.mats + (size_t)j * n * n + (size_t)i * n);
   }
   __syncwarp();
   __threadfence_block();
@@ -153,7 +169,7 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
 #pragma unroll
       for (int q = 0; q < (int)(sizeof(ServeTile) / 8); ++q) dstw[q] = __ldcv(srcw + q);
     }
-    if (t.particle >= 0 && t.znew) rebuild_rows(t, NC, lane);
+    apply_move(t, NC, lane);
     DeferredOut out;
     for (int j = 0; j < t.count; ++j) {
       __syncwarp();
@@ -220,27 +236,6 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
   }
 }
 
-__global__ void build_walker_kernel(double2 *mats, const double2 *z, int n, int k) {
-  long long total = (long long)k * n;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long j = e / n;
-    const int i = (int)(e - j * n);
-    const double2 zz = z[e];
-    double2 *row = mats + (size_t)j * n * n + (size_t)i * n;
-    const double w = exp(-(zz.x * zz.x + zz.y * zz.y) * 0.25);
-    double px = 1.0, py = 0.0;
-    for (int c = 0; c < n; ++c) {
-      row[c] = make_double2(px * w, py * w);
-      const double nx = px * zz.x - py * zz.y;
-      const double ny = px * zz.y + py * zz.x;
-      px = nx;
-      py = ny;
-    }
-  }
-}
-
-
 using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
                              ClassCtl *, int, float);
 
@@ -276,6 +271,7 @@ struct Walker {
   size_t offset = 0;     // in the HBM pool
   size_t bytes = 0;
   bool busy = false;     // a move is in flight
+  bool built = false;    // matrices made from z by the loop (first request)
 };
 
 struct ReqSlot {
@@ -559,18 +555,16 @@ extern "C" int lufqhe_server_walker_create(lufqhe_server_t *s, int n, int k, con
   W.offset = off;
   W.bytes = bytes;
   W.busy = false;
+  W.built = false;
   double2 *mats = reinterpret_cast<double2 *>(s->pool + off);
   double2 *z = mats + (size_t)k * n * n;
+  // only the coordinates cross now (copy engine); the matrices are built by
+  // the class loop when the walker's first request runs
   cudaStream_t st = s->setup;
   int rc = check_cuda(cudaMemcpyAsync(z, z_host, (size_t)k * n * sizeof(double2),
                                       cudaMemcpyHostToDevice, st),
                       "walker z upload");
-  if (!rc) {
-    build_walker_kernel<<<std::max(1, std::min(1024, (k * n + 255) / 256)), 256, 0, st>>>(mats, z,
-                                                                                       n, k);
-    rc = check_cuda(cudaGetLastError(), "build_walker_kernel");
-  }
-  if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "walker build");
+  if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "walker z upload");
   if (rc) {
     pool_free(s, off, bytes);
     W.live = false;
@@ -664,6 +658,8 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
     T.req_tiles = ntiles;
     T.count = std::min(s->tile, W.k - first);
     T.particle = particle;
+    T.build = W.built ? 0 : 1;
+    T.pad = 0;
     s->classes[W.cls].ring_h[(C.published + t) % kRing] = T;
   }
   std::atomic_thread_fence(std::memory_order_seq_cst);
@@ -672,6 +668,7 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
   int rc = ensure_running(s, C);
   if (rc) return rc;
   W.busy = true;
+  W.built = true;
   *ticket = ((long long)R.seq << 16) | slot;
   return LUFQHE_SUCCESS;
 }
