@@ -572,14 +572,15 @@ def run_ours(args):
             "frac": (achieved_tf / fp32_peak) if fp32_peak else None,
             "peak_source": "measured FP32 FMA peak (library probe kernel, this run)",
             "flops_per_matrix": F,
-            "traffic": ncu_traffic("lup_mixed_kernel", args.workload),
+            "traffic": ncu_traffic("lup_mixed_tile_kernel", args.workload),
             "hbm": {"achieved": B * dets_mixed * 1e-9, "peak": hbm_peak, "unit": "GB/s",
                     "frac": B * dets_mixed * 1e-9 / hbm_peak, "peak_source": hbm_src,
                     "bytes_per_matrix": B},
             "plain_fp64": {"kernel": "lup_plain_kernel<ARITH_FUSED>", "bound": "fp64",
                            "achieved": F * dets_fused * 1e-12, "peak": fp64_peak,
                            "unit": "TFLOP/s",
-                           "frac": (F * dets_fused * 1e-12 / fp64_peak) if fp64_peak else None},
+                           "frac": (F * dets_fused * 1e-12 / fp64_peak) if fp64_peak else None,
+                           "traffic": ncu_traffic("lup_plain_kernel", args.workload)},
         }
         out = {
             "metric": "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)",

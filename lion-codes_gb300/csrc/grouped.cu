@@ -28,7 +28,6 @@
 
 namespace lufqhe {
 
-unsigned int fp64_share_64k(int n);
 
 namespace {
 
@@ -457,10 +456,8 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
     }
     p->groups.push_back(G);
     p->tile.push_back(default_tile(G.n));
-    // as the batched mixed kernels: the per-n share for the register-tiled
-    // sizes, none for the others
-    const bool tiled = G.n == 6 || G.n == 8 || G.n == 12 || G.n == 16 || G.n == 24 || G.n == 32;
-    p->share.push_back(tiled ? fp64_share_64k(G.n) : 0u);
+    // the per-n FP64 share of the batched mixed kernels
+    p->share.push_back(fp64_share_64k(G.n));
     p->nmax = std::max(p->nmax, G.n);
     p->total += G.count;
   }

@@ -104,9 +104,13 @@ __host__ __device__ __forceinline__ unsigned long long seed_key(unsigned long lo
 }
 
 // ---- launches implemented in the .cu files ---------------------------------
+// status_or: bits OR-ed into every status (mixed mode's FP64 route)
 int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,
                  double *logabs, double *phase, int8_t *parity, int32_t *status,
-                 cudaStream_t stream);
+                 cudaStream_t stream, int status_or = 0);
+// Mixed mode's precision policy: the share (in 1/65536) of n x n matrices
+// sent straight to the FP64 kernel, chosen by content hash.
+unsigned int fp64_share_64k(int n);
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
                  double *phase, int8_t *parity, int32_t *status, cudaStream_t stream);
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,

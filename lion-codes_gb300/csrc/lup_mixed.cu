@@ -38,14 +38,11 @@ float g_fp64_share = -1.0f;  // < 0: per-n default
 unsigned int fp64_share_64k(int n) {
   float s = g_fp64_share;
   if (s < 0.0f) {
-    switch (n) {
-      case 6:
-      case 8: s = 0.0f; break;
-      case 12:
-      case 16: s = 0.25f; break;
-      case 24: s = 0.40f; break;
-      default: s = 0.50f; break;
-    }
+    // n <= 16: the FP32 path alone is fastest; n = 24: the two pipes balance
+    // near 0.6; n >= 32: the FP64 kernel beats the FP32 path outright
+    if (n <= 16) s = 0.0f;
+    else if (n <= 24) s = 0.60f;
+    else s = 1.0f;
   }
   if (s <= 0.0f) return 0u;
   if (s >= 1.0f) return 65536u;
@@ -60,7 +57,8 @@ constexpr int kDefaultTileWarps = 4;
 
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     lup_mixed_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
-                     float theta2, double *__restrict__ logabs, double *__restrict__ phase,
+                     float theta2, unsigned int share64k, double *__restrict__ logabs,
+                     double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
@@ -85,6 +83,11 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     __syncwarp();
     const double2 *src = A + (size_t)b * n * lda;
     double2 *M = reinterpret_cast<double2 *>(S.SC);
+    if (route_fp64(src, share64k)) {
+      fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status,
+                    LUFQHE_ST_FP64);
+      continue;
+    }
     if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
@@ -190,6 +193,11 @@ float g_mixed_theta = 0.1f;
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
                  double *phase, int8_t *parity, int32_t *status, cudaStream_t stream) {
   if (batch == 0) return LUFQHE_SUCCESS;
+  // every matrix on the FP64 route: the plain fused kernel, whose shared
+  // memory layout holds more warps per SM than the mixed kernels'
+  if (fp64_share_64k(n) >= 65536u)
+    return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity, status,
+                        stream, LUFQHE_ST_FP64);
   const float th2 = g_mixed_theta * g_mixed_theta;
   switch (n) {
     case 6: return launch_mixed_tile<6>(A, lda, batch, th2, logabs, phase, parity, status, stream);
@@ -224,8 +232,9 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
   const float theta2 = g_mixed_theta * g_mixed_theta;
-  lup_mixed_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, theta2, logabs, phase,
-                                                       parity, status);
+  lup_mixed_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, theta2,
+                                                       fp64_share_64k(n), logabs, phase, parity,
+                                                       status);
   return check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
 }
 

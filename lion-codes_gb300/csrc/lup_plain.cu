@@ -24,7 +24,8 @@ template <int ARITH>
 __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
     lup_plain_kernel(const double2 *__restrict__ A, double2 *__restrict__ Aout, int n, int lda,
                      long long batch, double *__restrict__ logabs, double *__restrict__ phase,
-                     int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+                     int8_t *__restrict__ parity, int32_t *__restrict__ status,
+                     int status_or) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
       logabs[b] = la;
       if (phase) phase[b] = ph;
       if (parity) parity[b] = (int8_t)par;
-      if (status) status[b] = st;
+      if (status) status[b] = st | status_or;
     }
   }
 }
@@ -107,7 +108,7 @@ size_t plain_smem_per_warp(int n) {
 
 int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,
                  double *logabs, double *phase, int8_t *parity, int32_t *status,
-                 cudaStream_t stream) {
+                 cudaStream_t stream, int status_or) {
   if (batch == 0) return LUFQHE_SUCCESS;
   const size_t per_warp = plain_smem_per_warp(n);
   const size_t optin = device_smem_optin();
@@ -132,7 +133,8 @@ int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batc
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  kern<<<grid, warps * 32, smem, stream>>>(A, Aout, n, lda, batch, logabs, phase, parity, status);
+  kern<<<grid, warps * 32, smem, stream>>>(A, Aout, n, lda, batch, logabs, phase, parity, status,
+                                           status_or);
   return check_cuda(cudaGetLastError(), "lup_plain_kernel launch");
 }
 

@@ -454,9 +454,11 @@ struct DeferredOut {
 
 // Route of a matrix in the batched mixed mode: true = straight to FP64. A hash
 // of its first entry's bits, so the route depends on the content only.
+template <bool COHERENT = false>
 __device__ __forceinline__ bool route_fp64(const double2 *src, unsigned int share64k) {
   if (share64k == 0) return false;
-  const double2 v = __ldg(src);
+  if (share64k >= 65536u) return true;
+  const double2 v = COHERENT ? __ldcg(src) : __ldg(src);
   unsigned long long h = (unsigned long long)__double_as_longlong(v.x) * 0x9E3779B97F4A7C15ull ^
                          (unsigned long long)__double_as_longlong(v.y);
   h ^= h >> 29;
@@ -584,6 +586,109 @@ __device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int l
   }
 }
 
+// Steps 4-6 in registers for a compile-time n <= 32 (same arithmetic as
+// mixed_finish, which keeps everything in shared memory):
+//  * E = U^-1 L^-1 R with lane k owning column k of R (operands l_it, u_it
+//    are shared-memory broadcasts), fully unrolled so the column stays in
+//    registers;
+//  * log det(I + E) with E transposed to one row per lane; the pivot row is
+//    shuffled from its lane, the multiplier of each row is its own entry.
+// Largest n whose steps 4-6 run fully unrolled in registers; above it the
+// unrolled code outgrows the instruction cache and the shared-memory form wins.
+#ifndef LUFQHE_REG_FINISH_MAX_N
+#define LUFQHE_REG_FINISH_MAX_N 12
+#endif
+constexpr int kRegFinishMaxN = LUFQHE_REG_FINISH_MAX_N;
+
+template <int N>
+__device__ bool mixed_finish_regs(const float2 *F, float2 *Rm, int lane, float theta2,
+                                  int exp_sum, CFF &prod, float2 &corr) {
+  constexpr int LDS = N + 1;
+  const bool col = lane < N;
+  float2 Y[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) Y[i] = col ? Rm[i * LDS + lane] : make_float2(0.f, 0.f);
+  // forward: Y = L^-1 R (unit lower)
+#pragma unroll
+  for (int t = 0; t < N - 1; ++t) {
+    const float2 yt = Y[t];
+#pragma unroll
+    for (int i = t + 1; i < N; ++i) Y[i] = cfms(Y[i], F[i * LDS + t], yt);
+  }
+  // backward: E = U^-1 Y; 1/u_tt comes from lane t
+  const float2 dinv = col ? crcpf(F[lane * LDS + lane]) : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int t = N - 1; t >= 0; --t) {
+    const float2 dt = make_float2(__shfl_sync(kFull, dinv.x, t), __shfl_sync(kFull, dinv.y, t));
+    Y[t] = cmulf(Y[t], dt);
+    const float2 et = Y[t];
+#pragma unroll
+    for (int i = 0; i < t; ++i) Y[i] = cfms(Y[i], F[i * LDS + t], et);
+  }
+  // diagonal product of U (complex float-float)
+  {
+    CFF p = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+    if (col) {
+      const float2 u = F[lane * LDS + lane];
+      p.xh = u.x;
+      p.yh = u.y;
+      ff_renorm(p);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) p = ff_cmul(p, shfl_cff(p, off, true));
+    prod = shfl_cff(p, 0, false);
+  }
+  // acceptance on lane 0's ||E||_F^2 (warp-uniform)
+  {
+    float f = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) f = __fmaf_rn(Y[i].x, Y[i].x, __fmaf_rn(Y[i].y, Y[i].y, f));
+#pragma unroll
+    for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
+    f = __shfl_sync(kFull, f, 0);
+    const float la_est = fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
+    const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
+    if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
+  }
+  // transpose: lane i takes row i of E
+  __syncwarp();
+  if (col) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rm[i * LDS + lane] = Y[i];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < N; ++k) Y[k] = col ? Rm[lane * LDS + k] : make_float2(0.f, 0.f);
+  // log det(I + E): unpivoted elimination, identity implicit
+  float2 mydiag = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int t = 0; t < N - 1; ++t) {
+    const float2 dt = make_float2(__shfl_sync(kFull, Y[t].x, t), __shfl_sync(kFull, Y[t].y, t));
+    if (lane == t) mydiag = dt;
+    const float2 l = cmulf(Y[t], crcpf(make_float2(1.0f + dt.x, dt.y)));
+    const bool below = lane > t;
+#pragma unroll
+    for (int k = t + 1; k < N; ++k) {
+      const float2 ztk = make_float2(__shfl_sync(kFull, Y[k].x, t), __shfl_sync(kFull, Y[k].y, t));
+      const float2 z = cfms(Y[k], l, ztk);
+      if (below) Y[k] = z;
+    }
+  }
+  if (lane == N - 1) mydiag = Y[N - 1];
+  float cre = 0.0f, cim = 0.0f;
+  if (col) {
+    cre = 0.5f * log1pf(__fmaf_rn(mydiag.x, mydiag.x, __fmaf_rn(mydiag.y, mydiag.y, 2.0f * mydiag.x)));
+    cim = atan2f(mydiag.y, 1.0f + mydiag.x);
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    cre += __shfl_xor_sync(kFull, cre, off);
+    cim += __shfl_xor_sync(kFull, cim, off);
+  }
+  corr = make_float2(__shfl_sync(kFull, cre, 0), __shfl_sync(kFull, cim, 0));
+  return true;
+}
+
 template <int N>
 __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane, float theta2,
                                   CFF &prod, int &exp_sum, float2 &corr, int &par) {
@@ -685,9 +790,11 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
   residual_rows<N, SA / 2, SA>(HL, F, lane);
   float2 *Rm = reinterpret_cast<float2 *>(HL);  // R, then E, row stride LDS
 
-  // 5-6. solves, acceptance, log det(I + E) and the diagonal product: the
-  //      shared-memory forms of the generic path with n fixed at compile time
-  return mixed_finish<1>(F, Rm, N, LDS, lane, theta2, exp_sum, prod, corr);
+  // 5-6. solves, acceptance, log det(I + E) and the diagonal product
+  if constexpr (N <= kRegFinishMaxN)
+    return mixed_finish_regs<N>(F, Rm, lane, theta2, exp_sum, prod, corr);
+  else
+    return mixed_finish<1>(F, Rm, N, LDS, lane, theta2, exp_sum, prod, corr);
 }
 
 template <int N>

@@ -10,18 +10,20 @@
 // to a share of the SMs, so all classes are resident at once. A request
 // (one move of one walker) is cut into tiles of matrices; the host appends the
 // tiles to the class's ring in mapped host memory and publishes them with a
-// release store. Warps of the class kernel claim tile indices with an
-// atomicAdd, wait (bounded) until the index is published, process the tile and
-// count it against its request; the warp that finishes a request's last tile
+// release store. Warps of the class kernel claim published tile indices one
+// at a time, process the tile and count it against its request; the warp that finishes a request's last tile
 // writes the request's completion flag to mapped host memory. Tiles of
 // different requests are in flight at the same time on different warps: new
 // requests are admitted as soon as ring slots and HBM free up, without waiting
 // for a batch boundary.
 //
-// Every device wait is bounded: a warp that sees no new tile for
-// kIdleCycles gives up, records the first tile index it had claimed, and the
-// kernel exits; the host relaunches it (restarting the claim counter at the
-// first abandoned index) the next time it publishes work.
+// A warp claims only a published index (compare-and-swap on the class's claim
+// counter while it is below the published count), so a warp that leaves the
+// loop never strands a tile. Every device wait is bounded: when no warp of the
+// class has claimed a tile for kIdleNs (a class-wide timestamp), the warps
+// leave together and the kernel exits; the host relaunches it, continuing
+// from the claim counter, the next time it publishes work or polls a request
+// of that class.
 
 #include <algorithm>
 #include <atomic>
@@ -42,8 +44,12 @@ namespace {
 using namespace mixed;
 
 constexpr unsigned kRing = 1u << 16;                  // tiles per class ring
-constexpr long long kIdleCycles = 1000000000ll;       // ~0.5 s at 2 GHz
-constexpr int kServeWarps = 4;
+constexpr unsigned long long kIdleNs = 200000000ull;  // 0.2 s without a claim
+// Warps per class CTA (its register budget follows from it). Every class CTA
+// asks for more than half of an SM's shared memory, so exactly one CTA of any
+// class fits on an SM: with the class shares summing to the SM count, all
+// class loops are resident together however the scheduler places them.
+constexpr int serve_max_warps(int n) { return n <= 8 ? 16 : n <= 16 ? 12 : n <= 32 ? 8 : 4; }
 
 struct ServeTile {
   double2 *mats;             // first matrix of the tile (device)
@@ -62,12 +68,17 @@ struct ServeTile {
   int pad;
 };
 
-struct ClassCtl {              // device memory, one per class
-  unsigned int claimed;        // next tile index to claim
-  unsigned int abandoned_min;  // first claimed-but-unpublished index at exit
-  unsigned int exited;         // warps that left the loop
-  unsigned int pad;
+struct ClassCtl {                // device memory, one per class
+  unsigned int claimed;          // tiles claimed so far (never above published)
+  unsigned int exited;           // warps that left the loop
+  unsigned long long last_ns;    // %globaltimer of the class's latest claim
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
   unsigned int v;
@@ -115,10 +126,20 @@ __device__ void apply_move(const ServeTile &t, int n, int lane) {
   __threadfence_block();
 }
 
+// Shared memory per warp: the FP64 matrix (as double2, aliased by the FP32
+// path's hi/lo copy) and the row scales come first; the FP32 factor and the
+// exponents follow and are left out when every matrix takes the FP64 kernel.
+size_t serve_smem_per_warp(int n, bool fp64_only) {
+  const size_t nl = (size_t)n * (n + 1);
+  size_t b = nl * sizeof(float4) + 2 * (size_t)n * sizeof(double);
+  if (!fp64_only) b += nl * sizeof(float2) + 2 * (size_t)n * sizeof(int);
+  return b;
+}
+
 template <int NC>
-__global__ void __launch_bounds__(kServeWarps * 32, 1)
+__global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
     serve_kernel(const ServeTile *ring, const unsigned int *published, const unsigned int *stop,
-                 ClassCtl *ctl, int mode, float theta2) {
+                 ClassCtl *ctl, int mode, float theta2, unsigned int share64k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = NC + 1;
   constexpr size_t NL = (size_t)NC * LDS;
@@ -128,35 +149,49 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
   unsigned char *base = smem_raw;
   float4 *HL = reinterpret_cast<float4 *>(base) + warp * NL;
   base += warps * NL * sizeof(float4);
-  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
-  base += warps * NL * sizeof(float2);
   double *hold = reinterpret_cast<double *>(base) + warp * 2 * NC;
   base += warps * 2 * (size_t)NC * sizeof(double);
+  // FP32-path arrays: only addressed when some matrix takes the FP32 path
+  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
+  base += warps * NL * sizeof(float2);
   int *er = reinterpret_cast<int *>(base) + warp * 2 * NC;
   int *ec = er + NC;
 
   for (;;) {
+    // claim the next published tile; give up when the class has been idle
     unsigned int idx = 0;
-    if (lane == 0) idx = atomicAdd(&ctl->claimed, 1u);
-    idx = __shfl_sync(kFull, idx, 0);
-    // bounded wait for the tile to be published
     int give_up = 0;
     if (lane == 0) {
-      const long long t0 = clock64();
-      while (ld_acquire_sys(published) <= idx) {
-        if (ld_acquire_sys(stop) || clock64() - t0 > kIdleCycles) {
+      const unsigned long long t0 = global_ns();
+      volatile unsigned int *claimed = &ctl->claimed;
+      for (;;) {
+        const unsigned int c = *claimed;
+        const unsigned int p = ld_acquire_sys(published);
+        if ((int)(p - c) > 0) {
+          if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
+            idx = c;
+            break;
+          }
+          continue;
+        }
+        if (ld_acquire_sys(stop)) {
+          give_up = 1;
+          break;
+        }
+        const unsigned long long now = global_ns();
+        const unsigned long long last = *(volatile unsigned long long *)&ctl->last_ns;
+        if (now - (last > t0 ? last : t0) > kIdleNs) {
           give_up = 1;
           break;
         }
         __nanosleep(256);
       }
+      if (!give_up) atomicMax(&ctl->last_ns, global_ns());
     }
+    idx = __shfl_sync(kFull, idx, 0);
     give_up = __shfl_sync(kFull, give_up, 0);
     if (give_up) {
-      if (lane == 0) {
-        atomicMin(&ctl->abandoned_min, idx);
-        atomicAdd(&ctl->exited, 1u);
-      }
+      if (lane == 0) atomicAdd(&ctl->exited, 1u);
       return;
     }
     __syncwarp();  // order every lane's reads after lane 0's acquire
@@ -179,7 +214,9 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
         emit_nonfinite(lane, j, t.logabs, t.phase, nullptr, t.status);
         continue;
       }
-      if (mode == LUFQHE_MODE_MIXED) {
+      // mixed mode: the per-n precision policy may send the matrix to FP64
+      const bool mixed = mode == LUFQHE_MODE_MIXED && !route_fp64<true>(src, share64k);
+      if (mixed) {
         CFF prod;
         int exp_sum = 0, par = 0;
         float2 corr;
@@ -216,7 +253,7 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
         if (lane == 0) {
           t.logabs[j] = la;
           t.phase[j] = ph;
-          t.status[j] = st;
+          t.status[j] = st | (mode == LUFQHE_MODE_MIXED ? LUFQHE_ST_FP64 : 0);
         }
       }
     }
@@ -237,7 +274,7 @@ __global__ void __launch_bounds__(kServeWarps * 32, 1)
 }
 
 using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
-                             ClassCtl *, int, float);
+                             ClassCtl *, int, float, unsigned int);
 
 ServeKernel serve_kernel_for(int n) {
   switch (n) {
@@ -249,10 +286,6 @@ ServeKernel serve_kernel_for(int n) {
   }
 }
 
-size_t serve_smem_per_warp(int n) {
-  return (size_t)n * (n + 1) * (sizeof(float4) + sizeof(float2)) + 2 * (size_t)n * sizeof(double) +
-         2 * (size_t)n * sizeof(int);
-}
 
 // ---- host side -------------------------------------------------------------
 
@@ -294,10 +327,11 @@ struct SClass {
   unsigned int *pub_d = nullptr;
   ClassCtl *ctl = nullptr;         // device
   unsigned int published = 0;     // host copy
-  int grid = 0, warps = kServeWarps;
+  int grid = 0, warps = 1;
   size_t smem = 0;
   bool running = false;
   unsigned int relaunches = 0;
+  unsigned int share64k = 0;       // FP64 routing share, fixed at creation
 };
 
 }  // namespace
@@ -379,21 +413,13 @@ int ensure_running(lufqhe_server_s *s, SClass &c) {
     c.running = false;
     if (q != cudaSuccess) return check_cuda(q, "serve kernel");
   }
-  // restart claims at the first abandoned index (everything before it is done)
-  ClassCtl h;
-  int rc = check_cuda(cudaMemcpyAsync(&h, c.ctl, sizeof(h), cudaMemcpyDeviceToHost, c.stream),
-                      "read class ctl");
-  if (!rc) rc = check_cuda(cudaStreamSynchronize(c.stream), "sync class ctl");
-  if (rc) return rc;
-  ClassCtl n{};
-  n.claimed = h.abandoned_min == 0xffffffffu ? h.claimed : h.abandoned_min;
-  n.abandoned_min = 0xffffffffu;
-  rc = check_cuda(cudaMemcpyAsync(c.ctl, &n, sizeof(n), cudaMemcpyHostToDevice, c.stream),
-                  "write class ctl");
-  if (rc) return rc;
+  // every claimed tile was processed before its warp left, so the new loop
+  // continues from the claim counter as it stands
+  // (the shared memory of an FP64-only class holds no FP32 arrays, so the
+  // share is the one fixed when the class was created)
   c.kern<<<c.grid, c.warps * 32, c.smem, c.stream>>>(c.ring_d, c.pub_d, s->stop_d, c.ctl, s->mode,
-                                                     s->theta2);
-  rc = check_cuda(cudaGetLastError(), "serve kernel launch");
+                                                     s->theta2, c.share64k);
+  int rc = check_cuda(cudaGetLastError(), "serve kernel launch");
   if (rc) return rc;
   c.running = true;
   ++c.relaunches;
@@ -471,9 +497,19 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     int want = class_sms ? class_sms[c] : std::max(1, sms / nclasses);
     sc.sms = std::max(1, std::min(want, sms_left - (nclasses - 1 - c)));
     sms_left -= sc.sms;
-    const size_t per_warp = serve_smem_per_warp(sc.n);
-    sc.warps = std::max(1, std::min<int>(kServeWarps, (int)(device_smem_optin() / per_warp)));
-    sc.smem = per_warp * sc.warps;
+    sc.share64k = mode == LUFQHE_MODE_MIXED ? fp64_share_64k(sc.n) : 0u;
+    const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u;
+    const size_t optin = device_smem_optin();
+    const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only);
+    sc.warps = std::max(1, std::min<int>(serve_max_warps(sc.n), (int)(optin / per_warp)));
+    if (per_warp * sc.warps > optin) {
+      set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per warp", sc.n,
+                per_warp);
+      rc = LUFQHE_ERR_UNSUPPORTED_N;
+      break;
+    }
+    // above half the SM's shared memory: one class CTA per SM
+    sc.smem = std::max(per_warp * sc.warps, optin / 2 + 1024);
     rc = check_cuda(cudaFuncSetAttribute(sc.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sc.smem),
                     "cudaFuncSetAttribute(serve)");
@@ -490,7 +526,6 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     if (!rc) rc = check_cuda(cudaMalloc(&sc.ctl, sizeof(ClassCtl)), "serve ctl");
     if (!rc) {
       ClassCtl z{};
-      z.abandoned_min = 0xffffffffu;
       rc = check_cuda(cudaMemcpy(sc.ctl, &z, sizeof(z), cudaMemcpyHostToDevice), "serve ctl init");
     }
     s->classes.push_back(sc);

@@ -91,3 +91,39 @@ def test_walker_stream(server):
     assert len(lat) == 400 and np.isfinite(lat).all() and (lat > 0).all()
     assert set(np.unique(ns)) <= {8, 16}
     assert mats > 400 and elapsed > 0
+
+
+def test_idle_exit_and_relaunch(server, oracle):
+    """The class loops leave after 0.2 s without work; a later request
+    relaunches them and completes with the right result."""
+    import time
+    rng = np.random.default_rng(4)
+    z = zdraw(rng, 64, 8)
+    w = server.walker(z)
+    server.result(server.submit(w, -1), 64)
+    time.sleep(0.6)                      # every class loop has gone idle and exited
+    znew = zdraw(rng, 64, 1)[:, 0]
+    la, ph, st = server.result(server.submit(w, 2, znew), 64)
+    z[:, 2] = znew
+    want, _, _ = oracle.logdet_dd(lll_host(z))
+    ok = (st & 8) == 0
+    assert (np.abs(la[ok] - want[ok]) / np.maximum(1, np.abs(want[ok]))).max() < 1e-10
+    server.destroy_walker(w)
+
+
+def test_large_class_follows_precision_policy(lufqhe_mod, cuda, oracle):
+    """n = 64 in mixed mode takes the FP64 kernel (status bit 16), as batched
+    mixed mode does for n >= 32."""
+    srv = lufqhe_mod.Server(1 << 28, mode=lufqhe_mod.MODE_MIXED, classes=(64,), max_k=64)
+    try:
+        rng = np.random.default_rng(5)
+        z = zdraw(rng, 20, 64)
+        w = srv.walker(z)
+        la, ph, st = srv.result(srv.submit(w, -1), 20)
+        assert (st == lufqhe_mod.ST_FP64).all()
+        want, _, _ = oracle.logdet_dd(lll_host(z))
+        # FP64 LUP on n = 64 orbital matrices: accurate to the FP64 rounding
+        # error the condition number allows, well inside 1e-8 here
+        assert (np.abs(la - want) / np.maximum(1, np.abs(want))).max() < 1e-8
+    finally:
+        srv.close()
