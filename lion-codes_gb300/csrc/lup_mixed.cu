@@ -22,7 +22,13 @@
 // meets a zero or non-finite pivot, is refactorised by the FP64 warp routine
 // (reference pivot rule, fused arithmetic) and flagged LUFQHE_ST_FALLBACK.
 // The permutation parity reported is that of the pivoting actually used.
+//
+// Warps take matrices from a work counter rather than a fixed grid stride: a
+// matrix refactorised in FP64 costs many times an accepted one, and a fixed
+// share of the batch per warp would leave the kernel waiting on the warps
+// that drew the most of them.
 
+#include <atomic>
 #include <cmath>
 
 #include "mixed_core.cuh"
@@ -38,11 +44,9 @@ float g_fp64_share = -1.0f;  // < 0: per-n default
 unsigned int fp64_share_64k(int n) {
   float s = g_fp64_share;
   if (s < 0.0f) {
-    // n <= 16: the FP32 path alone is fastest; n = 24: the two pipes balance
-    // near 0.6; n >= 32: the FP64 kernel beats the FP32 path outright
-    if (n <= 16) s = 0.0f;
-    else if (n <= 24) s = 0.60f;
-    else s = 1.0f;
+    // n <= 24: the FP32 path alone is fastest; n >= 25: the FP64 kernel
+    // beats the FP32 path outright
+    s = n <= 24 ? 0.0f : 1.0f;
   }
   if (s <= 0.0f) return 0u;
   if (s >= 1.0f) return 65536u;
@@ -55,10 +59,37 @@ using namespace mixed;
 
 constexpr int kDefaultTileWarps = 4;
 
+// Work counters of the batched mixed kernels, {next matrix, warps done} per
+// slot. Static device memory starts at zero; each launch takes the next slot
+// in turn and its last warp sets the slot back to zero, so a slot is free
+// again unless 4096 later launches were issued while it still ran.
+constexpr int kWorkSlots = 4096;
+__device__ unsigned long long g_work[kWorkSlots][2];
+std::atomic<unsigned int> g_work_seq{0};
+
+int next_work_slot() { return (int)(g_work_seq.fetch_add(1u) % kWorkSlots); }
+
+__device__ __forceinline__ long long claim_matrix(int slot, int lane) {
+  unsigned long long b = 0;
+  if (lane == 0) b = atomicAdd(&g_work[slot][0], 1ull);
+  return (long long)__shfl_sync(kFull, b, 0);
+}
+
+__device__ __forceinline__ void release_slot(int slot, int lane) {
+  if (lane == 0) {
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    if (atomicAdd(&g_work[slot][1], 1ull) == warps - 1) {
+      // every warp has made its last claim: reset for the slot's next launch
+      atomicExch(&g_work[slot][0], 0ull);
+      atomicExch(&g_work[slot][1], 0ull);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     lup_mixed_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
-                     float theta2, unsigned int share64k, double *__restrict__ logabs,
-                     double *__restrict__ phase,
+                     float theta2, unsigned int share64k, int slot,
+                     double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
@@ -78,8 +109,9 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
   S.ec = S.er + n;
 
   DeferredOut out;
-  for (long long b = (long long)blockIdx.x * warps + warp; b < batch;
-       b += (long long)gridDim.x * warps) {
+  for (;;) {
+    const long long b = claim_matrix(slot, lane);
+    if (b >= batch) break;
     __syncwarp();
     const double2 *src = A + (size_t)b * n * lda;
     double2 *M = reinterpret_cast<double2 *>(S.SC);
@@ -101,13 +133,14 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
       fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
+  release_slot(slot, lane);
 }
 
 
 template <int N>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     lup_mixed_tile_kernel(const double2 *__restrict__ A, int lda, long long batch, float theta2,
-                          unsigned int share64k, double *__restrict__ logabs,
+                          unsigned int share64k, int slot, double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -127,8 +160,9 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
   int *ec = er + N;
 
   DeferredOut out;
-  for (long long b = (long long)blockIdx.x * warps + warp; b < batch;
-       b += (long long)gridDim.x * warps) {
+  for (;;) {
+    const long long b = claim_matrix(slot, lane);
+    if (b >= batch) break;
     __syncwarp();
     const double2 *src = A + (size_t)b * N * lda;
     double2 *M = reinterpret_cast<double2 *>(HL);
@@ -150,6 +184,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
       fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
+  release_slot(slot, lane);
 }
 
 template <int N>
@@ -175,8 +210,8 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, fp64_share_64k(N), logabs,
-                                           phase, parity, status);
+  kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, fp64_share_64k(N),
+                                           next_work_slot(), logabs, phase, parity, status);
   return check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
 }
 
@@ -233,8 +268,8 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
   int grid = (int)(want < cap ? want : cap);
   const float theta2 = g_mixed_theta * g_mixed_theta;
   lup_mixed_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, theta2,
-                                                       fp64_share_64k(n), logabs, phase, parity,
-                                                       status);
+                                                       fp64_share_64k(n), next_work_slot(),
+                                                       logabs, phase, parity, status);
   return check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
 }
 

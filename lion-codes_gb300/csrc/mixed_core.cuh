@@ -513,10 +513,8 @@ __device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, in
 //    (4a + r, 8b + c) and accumulates their float-float Dot2 sums in registers
 //    over t, reading l_it and u_tk from shared memory (operands that do not
 //    contribute are zero, which leaves a Dot2 step exact and branch-free).
-//  * Solves: lane k owns column k of R in registers; the L and U entries are
-//    shared-memory broadcasts.
-//  * log det(I + E): E transposed to one row per lane; unpivoted elimination
-//    with the pivot row shuffled from its lane.
+//  * Solves and log det(I + E): E stays in registers on the same lane grid
+//    (mixed_finish_tile).
 template <int N>
 struct TileGeom {
   static constexpr int LDS = N + 1;
@@ -586,63 +584,121 @@ __device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int l
   }
 }
 
-// Steps 4-6 in registers for a compile-time n <= 32 (same arithmetic as
-// mixed_finish, which keeps everything in shared memory):
-//  * E = U^-1 L^-1 R with lane k owning column k of R (operands l_it, u_it
-//    are shared-memory broadcasts), fully unrolled so the column stays in
-//    registers;
-//  * log det(I + E) with E transposed to one row per lane; the pivot row is
-//    shuffled from its lane, the multiplier of each row is its own entry.
-// Largest n whose steps 4-6 run fully unrolled in registers; above it the
-// unrolled code outgrows the instruction cache and the shared-memory form wins.
-#ifndef LUFQHE_REG_FINISH_MAX_N
-#define LUFQHE_REG_FINISH_MAX_N 12
-#endif
-constexpr int kRegFinishMaxN = LUFQHE_REG_FINISH_MAX_N;
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+  return make_float2(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src));
+}
 
+// Steps 4-6 of the tile path with E in registers on the 4 x 8 lane grid of
+// the residual (lane (r, c) holds entries (4a + r, 8b + c)). Every element
+// update is the same cfms / cmulf as in mixed_finish, so E and log det(I + E)
+// come out bit for bit as there; only the order of the ||E||_F sum differs.
+//  * Step t = 4s + u of a solve or of the elimination: the outer loop over the
+//    row slot s is unrolled, the inner loop over u is not, so register indices
+//    are compile-time while the code stays small. Row t lives in lanes (u, *)
+//    at slot s and reaches the other lanes by shuffle; l_it and u_it are
+//    shared-memory reads that 8 lanes share.
+//  * log det(I + E): unpivoted elimination. Rows and columns up to t are
+//    never read after step t, so the update runs over whole slots without
+//    masks; the pivots 1 + d_t go to `diag` and their logs are taken one per
+//    lane at the end.
 template <int N>
-__device__ bool mixed_finish_regs(const float2 *F, float2 *Rm, int lane, float theta2,
-                                  int exp_sum, CFF &prod, float2 &corr) {
+__device__ bool mixed_finish_tile(const float2 *F, const float2 *Rm, float2 *diag, int lane,
+                                  float theta2, int exp_sum, CFF &prod, float2 &corr) {
   constexpr int LDS = N + 1;
-  const bool col = lane < N;
-  float2 Y[N];
+  constexpr int SA = (N + 3) / 4;
+  constexpr int SB = (N + 7) / 8;
+  const int r = lane >> 3, c = lane & 7;
+  const float2 zero = make_float2(0.f, 0.f);
+  float2 Y[SA][SB];
 #pragma unroll
-  for (int i = 0; i < N; ++i) Y[i] = col ? Rm[i * LDS + lane] : make_float2(0.f, 0.f);
-  // forward: Y = L^-1 R (unit lower)
+  for (int a = 0; a < SA; ++a)
 #pragma unroll
-  for (int t = 0; t < N - 1; ++t) {
-    const float2 yt = Y[t];
+    for (int b = 0; b < SB; ++b) {
+      const int i = 4 * a + r, k = 8 * b + c;
+      Y[a][b] = (i < N && k < N) ? Rm[i * LDS + k] : zero;
+    }
+
+  // 4a. Y = L^-1 R (unit lower)
 #pragma unroll
-    for (int i = t + 1; i < N; ++i) Y[i] = cfms(Y[i], F[i * LDS + t], yt);
+  for (int s = 0; s < SA; ++s) {
+#pragma unroll 1
+    for (int u = 0; u < 4; ++u) {
+      const int t = 4 * s + u;
+      if (t >= N - 1) break;
+      float2 yt[SB];
+#pragma unroll
+      for (int b = 0; b < SB; ++b) yt[b] = shfl2(Y[s][b], u * 8 + c);
+      {
+        const bool below = r > u && 4 * s + r < N;
+        const float2 l = below ? F[(4 * s + r) * LDS + t] : zero;
+#pragma unroll
+        for (int b = 0; b < SB; ++b) {
+          const float2 v = cfms(Y[s][b], l, yt[b]);
+          Y[s][b] = below ? v : Y[s][b];
+        }
+      }
+#pragma unroll
+      for (int a = s + 1; a < SA; ++a) {
+        const int i = 4 * a + r;
+        const float2 l = i < N ? F[i * LDS + t] : zero;
+#pragma unroll
+        for (int b = 0; b < SB; ++b) Y[a][b] = cfms(Y[a][b], l, yt[b]);
+      }
+    }
   }
-  // backward: E = U^-1 Y; 1/u_tt comes from lane t
-  const float2 dinv = col ? crcpf(F[lane * LDS + lane]) : make_float2(0.f, 0.f);
+  // 4b. E = U^-1 Y: row t is scaled by 1/u_tt, then removed from the rows above
 #pragma unroll
-  for (int t = N - 1; t >= 0; --t) {
-    const float2 dt = make_float2(__shfl_sync(kFull, dinv.x, t), __shfl_sync(kFull, dinv.y, t));
-    Y[t] = cmulf(Y[t], dt);
-    const float2 et = Y[t];
+  for (int s = SA - 1; s >= 0; --s) {
+#pragma unroll 1
+    for (int u = 3; u >= 0; --u) {
+      const int t = 4 * s + u;
+      if (t >= N) continue;
+      const float2 dinv = crcpf(F[t * LDS + t]);
+      float2 et[SB];
 #pragma unroll
-    for (int i = 0; i < t; ++i) Y[i] = cfms(Y[i], F[i * LDS + t], et);
+      for (int b = 0; b < SB; ++b) {
+        et[b] = cmulf(shfl2(Y[s][b], u * 8 + c), dinv);
+        Y[s][b] = r == u ? et[b] : Y[s][b];
+      }
+      {
+        const bool above = r < u;
+        const float2 uu = above ? F[(4 * s + r) * LDS + t] : zero;
+#pragma unroll
+        for (int b = 0; b < SB; ++b) {
+          const float2 v = cfms(Y[s][b], uu, et[b]);
+          Y[s][b] = above ? v : Y[s][b];
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < s; ++a) {
+        const float2 uu = F[(4 * a + r) * LDS + t];
+#pragma unroll
+        for (int b = 0; b < SB; ++b) Y[a][b] = cfms(Y[a][b], uu, et[b]);
+      }
+    }
   }
-  // diagonal product of U (complex float-float)
+
+  // 6 (first half). complex float-float product of the diagonal of U
   {
-    CFF p = {1.0f, 0.0f, 0.0f, 0.0f, 0};
-    if (col) {
+    CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+    if (lane < N) {
       const float2 u = F[lane * LDS + lane];
-      p.xh = u.x;
-      p.yh = u.y;
-      ff_renorm(p);
+      CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
+      ff_renorm(v);
+      acc = ff_cmul(acc, v);
     }
 #pragma unroll
-    for (int off = 16; off; off >>= 1) p = ff_cmul(p, shfl_cff(p, off, true));
-    prod = shfl_cff(p, 0, false);
+    for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
+    prod = shfl_cff(acc, 0, false);
   }
-  // acceptance on lane 0's ||E||_F^2 (warp-uniform)
+
+  // acceptance (as in mixed_finish), decided on lane 0's sum
   {
     float f = 0.0f;
 #pragma unroll
-    for (int i = 0; i < N; ++i) f = __fmaf_rn(Y[i].x, Y[i].x, __fmaf_rn(Y[i].y, Y[i].y, f));
+    for (int a = 0; a < SA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) f = __fmaf_rn(Y[a][b].x, Y[a][b].x, __fmaf_rn(Y[a][b].y, Y[a][b].y, f));
 #pragma unroll
     for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
     f = __shfl_sync(kFull, f, 0);
@@ -650,35 +706,37 @@ __device__ bool mixed_finish_regs(const float2 *F, float2 *Rm, int lane, float t
     const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
     if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
   }
-  // transpose: lane i takes row i of E
-  __syncwarp();
-  if (col) {
+
+  // 5. log det(I + E)
 #pragma unroll
-    for (int i = 0; i < N; ++i) Rm[i * LDS + lane] = Y[i];
-  }
-  __syncwarp();
+  for (int s = 0; s < SA; ++s) {
+    const int q = s >> 1;  // column slot of t = 4s + u (compile-time)
+#pragma unroll 1
+    for (int u = 0; u < 4; ++u) {
+      const int t = 4 * s + u;
+      if (t >= N) break;
+      const int ct = 4 * (s & 1) + u;  // lane column of t
+      const float2 d = shfl2(Y[s][q], u * 8 + ct);
+      if (lane == 0) diag[t] = d;
+      if (t == N - 1) break;
+      const float2 rp = crcpf(make_float2(1.0f + d.x, d.y));
+      float2 et[SB];
 #pragma unroll
-  for (int k = 0; k < N; ++k) Y[k] = col ? Rm[lane * LDS + k] : make_float2(0.f, 0.f);
-  // log det(I + E): unpivoted elimination, identity implicit
-  float2 mydiag = make_float2(0.f, 0.f);
+      for (int b = q; b < SB; ++b) et[b] = shfl2(Y[s][b], u * 8 + c);
 #pragma unroll
-  for (int t = 0; t < N - 1; ++t) {
-    const float2 dt = make_float2(__shfl_sync(kFull, Y[t].x, t), __shfl_sync(kFull, Y[t].y, t));
-    if (lane == t) mydiag = dt;
-    const float2 l = cmulf(Y[t], crcpf(make_float2(1.0f + dt.x, dt.y)));
-    const bool below = lane > t;
+      for (int a = s; a < SA; ++a) {
+        const float2 l = cmulf(shfl2(Y[a][q], r * 8 + ct), rp);
 #pragma unroll
-    for (int k = t + 1; k < N; ++k) {
-      const float2 ztk = make_float2(__shfl_sync(kFull, Y[k].x, t), __shfl_sync(kFull, Y[k].y, t));
-      const float2 z = cfms(Y[k], l, ztk);
-      if (below) Y[k] = z;
+        for (int b = q; b < SB; ++b) Y[a][b] = cfms(Y[a][b], l, et[b]);
+      }
     }
   }
-  if (lane == N - 1) mydiag = Y[N - 1];
+  __syncwarp();
   float cre = 0.0f, cim = 0.0f;
-  if (col) {
-    cre = 0.5f * log1pf(__fmaf_rn(mydiag.x, mydiag.x, __fmaf_rn(mydiag.y, mydiag.y, 2.0f * mydiag.x)));
-    cim = atan2f(mydiag.y, 1.0f + mydiag.x);
+  if (lane < N) {
+    const float2 d = diag[lane];
+    cre = __fmaf_rn(0.5f, log1pf(__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, 2.0f * d.x))), cre);
+    cim += atan2f(d.y, 1.0f + d.x);
   }
 #pragma unroll
   for (int off = 16; off; off >>= 1) {
@@ -791,10 +849,9 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
   float2 *Rm = reinterpret_cast<float2 *>(HL);  // R, then E, row stride LDS
 
   // 5-6. solves, acceptance, log det(I + E) and the diagonal product
-  if constexpr (N <= kRegFinishMaxN)
-    return mixed_finish_regs<N>(F, Rm, lane, theta2, exp_sum, prod, corr);
-  else
-    return mixed_finish<1>(F, Rm, N, LDS, lane, theta2, exp_sum, prod, corr);
+  // (the exponent arrays are free again: they hold the pivots of step 5)
+  return mixed_finish_tile<N>(F, Rm, reinterpret_cast<float2 *>(er), lane, theta2, exp_sum, prod,
+                              corr);
 }
 
 template <int N>
