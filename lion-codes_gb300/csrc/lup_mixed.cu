@@ -26,7 +26,14 @@
 // Warps take matrices from a work counter rather than a fixed grid stride: a
 // matrix refactorised in FP64 costs many times an accepted one, and a fixed
 // share of the batch per warp would leave the kernel waiting on the warps
-// that drew the most of them.
+// that drew the most of them. The FP64 refactorisations themselves run after
+// the FP32 pass, in a second kernel on the same stream that has the whole GPU
+// (and the FP64 kernel's smaller shared-memory footprint): the FP32 pass
+// appends the index of a rejected matrix to a pending list in static device
+// memory, and the second kernel's warps claim the list's entries one at a
+// time. A matrix that finds the list full is refactorised where it is. For
+// n < 24 the FP64 refactorisations are cheap and rare enough that the second
+// launch costs more than it saves; there the FP32 pass does them in place.
 
 #include <atomic>
 #include <cmath>
@@ -75,6 +82,30 @@ __device__ __forceinline__ long long claim_matrix(int slot, int lane) {
   return (long long)__shfl_sync(kFull, b, 0);
 }
 
+// Pending lists of the FP64 pass: one per launch in flight, taken in turn
+// (a slot is busy from the FP32 pass to the end of the FP64 pass).
+constexpr int kPendSlots = 32;
+constexpr unsigned int kPendCap = 1u << 17;
+__device__ unsigned int g_pend[kPendSlots][kPendCap];
+__device__ unsigned int g_pend_count[kPendSlots];
+std::atomic<unsigned int> g_pend_seq{0};
+
+int next_pend_slot() { return (int)(g_pend_seq.fetch_add(1u) % kPendSlots); }
+
+constexpr int kDeferMinN = 24;
+
+// Hand matrix b to the FP64 pass; false (warp-uniform) if there is none
+// (pslot < 0) or its list is full.
+__device__ __forceinline__ bool defer_fp64(int pslot, long long b, int lane) {
+  if (pslot < 0) return false;
+  unsigned int pos = 0;
+  if (lane == 0) pos = atomicAdd(&g_pend_count[pslot], 1u);
+  pos = __shfl_sync(kFull, pos, 0);
+  if (pos >= kPendCap || b > 0xffffffffll) return false;
+  if (lane == 0) g_pend[pslot][pos] = (unsigned int)b;
+  return true;
+}
+
 __device__ __forceinline__ void release_slot(int slot, int lane) {
   if (lane == 0) {
     const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
@@ -88,7 +119,7 @@ __device__ __forceinline__ void release_slot(int slot, int lane) {
 
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     lup_mixed_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
-                     float theta2, unsigned int share64k, int slot,
+                     float theta2, unsigned int share64k, int slot, int pslot,
                      double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -129,7 +160,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     float2 corr;
     if (mixed_factor(S, n, lane, theta2, prod, exp_sum, corr, par))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else
+    else if (!defer_fp64(pslot, b, lane))
       fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -140,7 +171,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
 template <int N>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     lup_mixed_tile_kernel(const double2 *__restrict__ A, int lda, long long batch, float theta2,
-                          unsigned int share64k, int slot, double *__restrict__ logabs,
+                          unsigned int share64k, int slot, int pslot,
+                          double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -180,11 +212,82 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     float2 corr;
     if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else
+    else if (!defer_fp64(pslot, b, lane))
       fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
   release_slot(slot, lane);
+}
+
+// The FP64 pass: warps claim the pending list's entries one at a time and
+// refactorise those matrices (reference pivot rule, fused arithmetic, status
+// flag LUFQHE_ST_FALLBACK); the last warp out empties the list for its next
+// user.
+__global__ void __launch_bounds__(4 * 32)
+    lup_mixed_fallback_kernel(const double2 *__restrict__ A, int n, int lda, int slot, int pslot,
+                              double *__restrict__ logabs, double *__restrict__ phase,
+                              int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int lds = n + 1;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
+  double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
+                                            (size_t)warps * n * lds) +
+                 warp * 2 * n;
+  __shared__ unsigned int cta_done;
+  if (threadIdx.x == 0) cta_done = 0u;
+  __syncthreads();
+  const unsigned long long count =
+      min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
+  for (;;) {
+    // look before claiming: in a grid sized for a long list, most warps find
+    // a short one already taken and leave without touching the counter
+    unsigned long long j = count;
+    if (lane == 0 && *(volatile unsigned long long *)&g_work[slot][0] < count)
+      j = atomicAdd(&g_work[slot][0], 1ull);
+    j = __shfl_sync(kFull, j, 0);
+    if (j >= count) break;
+    const long long b = g_pend[pslot][j];
+    fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
+                  status);
+  }
+  // one release per CTA: the last CTA out empties the list and the counter
+  if (lane == 0 && atomicAdd(&cta_done, 1u) == (unsigned int)warps - 1u) {
+    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
+      atomicExch(&g_work[slot][0], 0ull);
+      atomicExch(&g_work[slot][1], 0ull);
+      atomicExch(&g_pend_count[pslot], 0u);
+    }
+  }
+}
+
+int launch_fallback(const double2 *A, int n, int lda, long long batch, int pslot,
+                    double *logabs, double *phase, int8_t *parity, int32_t *status,
+                    cudaStream_t stream) {
+  const size_t per_warp = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
+  int warps = (int)(device_smem_optin() / per_warp);
+  if (warps > 4) warps = 4;
+  if (warps < 1) warps = 1;
+  const size_t smem = per_warp * warps;
+  int rc = check_cuda(cudaFuncSetAttribute(lup_mixed_fallback_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "cudaFuncSetAttribute(mixed fallback)");
+  if (rc) return rc;
+  int per_sm = 0;
+  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lup_mixed_fallback_kernel,
+                                                                warps * 32, smem),
+                  "occupancy(mixed fallback)");
+  if (rc) return rc;
+  if (per_sm < 1) per_sm = 1;
+  // sized for the whole list; warps with nothing to claim leave at once
+  long long want = (batch + warps - 1) / warps;
+  long long cap = (long long)device_sm_count() * per_sm;
+  int grid = (int)(want < cap ? want : cap);
+  lup_mixed_fallback_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, next_work_slot(), pslot,
+                                                                logabs, phase, parity, status);
+  return check_cuda(cudaGetLastError(), "lup_mixed_fallback_kernel launch");
 }
 
 template <int N>
@@ -210,9 +313,12 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
+  const int pslot = N >= kDeferMinN ? next_pend_slot() : -1;
   kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, fp64_share_64k(N),
-                                           next_work_slot(), logabs, phase, parity, status);
-  return check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
+                                           next_work_slot(), pslot, logabs, phase, parity, status);
+  rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
+  if (rc || pslot < 0) return rc;
+  return launch_fallback(A, N, lda, batch, pslot, logabs, phase, parity, status, stream);
 }
 
 }  // namespace
@@ -267,10 +373,13 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
   const float theta2 = g_mixed_theta * g_mixed_theta;
+  const int pslot = n >= kDeferMinN ? next_pend_slot() : -1;
   lup_mixed_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, theta2,
-                                                       fp64_share_64k(n), next_work_slot(),
+                                                       fp64_share_64k(n), next_work_slot(), pslot,
                                                        logabs, phase, parity, status);
-  return check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
+  rc = check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
+  if (rc || pslot < 0) return rc;
+  return launch_fallback(A, n, lda, batch, pslot, logabs, phase, parity, status, stream);
 }
 
 }  // namespace lufqhe

@@ -793,51 +793,70 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
   }
   __syncwarp();
 
-  // 3. FP32 LUP
+  // 3. FP32 LUP. Pivot: the largest |Re| + |Im| in column t at or below row
+  //    t, from one warp max over a key that holds the value's bits with the
+  //    low 5 mantissa bits replaced by 31 - row (values within 2^-18 of each
+  //    other tie; ties go to the smaller row). Trailing update on the 4 x 8
+  //    lane grid: each lane reads l_it for its rows and u_tk for its columns
+  //    once per step, zero outside the trailing block (which leaves those
+  //    entries as they are), and updates its entries in the slots that reach
+  //    the block.
   par = 0;
-  for (int t = 0; t < N; ++t) {
-    float best = -1.0f;
-    int bi = t;
-    if (lane >= t && lane < N) {
-      const float2 v = F[lane * LDS + t];
-      best = fabsf(v.x) + fabsf(v.y);
-      bi = lane;
-    }
+  {
+    const int tr = lane >> 3, tc = lane & 7;
+    const float2 zero = make_float2(0.f, 0.f);
+    for (int t = 0; t < N; ++t) {
+      unsigned int key = 0u;
+      if (lane >= t && lane < N) {
+        const float2 v = F[lane * LDS + t];
+        const float m = fabsf(v.x) + fabsf(v.y);
+        key = (__float_as_uint(m) & ~31u) | (31u - (unsigned int)lane);
+      }
+      key = __reduce_max_sync(kFull, key);
+      const float best = __uint_as_float(key & ~31u);
+      if (!(best > 0.0f) || !(best < INFINITY)) return false;  // zero/NaN/Inf pivot
+      const int bi = 31 - (int)(key & 31u);
+      if (bi != t) {
+        if (lane < N) {
+          const float2 a = F[bi * LDS + lane];
+          F[bi * LDS + lane] = F[t * LDS + lane];
+          F[t * LDS + lane] = a;
+          const float4 c = HL[bi * LDS + lane];
+          HL[bi * LDS + lane] = HL[t * LDS + lane];
+          HL[t * LDS + lane] = c;
+        }
+        par ^= 1;
+      }
+      __syncwarp();
+      const float2 rp = crcpf(F[t * LDS + t]);
+      if (lane > t && lane < N) F[lane * LDS + t] = cmulf(F[lane * LDS + t], rp);
+      __syncwarp();
+      if (t + 1 < N) {
+        float2 lv[SA], uv[SB];
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      float om = __shfl_xor_sync(kFull, best, off);
-      int oi = __shfl_xor_sync(kFull, bi, off);
-      if (om > best || (om == best && oi < bi)) {
-        best = om;
-        bi = oi;
+        for (int a = 0; a < SA; ++a) {
+          const int i = 4 * a + tr;
+          lv[a] = (i > t && i < N) ? F[i * LDS + t] : zero;
+        }
+#pragma unroll
+        for (int b = 0; b < SB; ++b) {
+          const int k = 8 * b + tc;
+          uv[b] = (k > t && k < N) ? F[t * LDS + k] : zero;
+        }
+#pragma unroll
+        for (int a = 0; a < SA; ++a) {
+          if (4 * a + 3 <= t) continue;
+#pragma unroll
+          for (int b = 0; b < SB; ++b) {
+            if (8 * b + 7 <= t) continue;
+            const int i = 4 * a + tr, k = 8 * b + tc;
+            if ((N % 4 == 0 || i < N) && (N % 8 == 0 || k < N))
+              F[i * LDS + k] = cfms(F[i * LDS + k], lv[a], uv[b]);
+          }
+        }
+        __syncwarp();
       }
     }
-    if (!(best > 0.0f) || !(best < INFINITY)) return false;
-    if (bi != t) {
-      if (lane < N) {
-        const float2 a = F[bi * LDS + lane];
-        F[bi * LDS + lane] = F[t * LDS + lane];
-        F[t * LDS + lane] = a;
-        const float4 c = HL[bi * LDS + lane];
-        HL[bi * LDS + lane] = HL[t * LDS + lane];
-        HL[t * LDS + lane] = c;
-      }
-      par ^= 1;
-    }
-    __syncwarp();
-    const float2 r = crcpf(F[t * LDS + t]);
-    if (lane > t && lane < N) F[lane * LDS + t] = cmulf(F[lane * LDS + t], r);
-    __syncwarp();
-    const int m = N - 1 - t;
-    if (m > 0) {
-      BlockWalk w(lane, m);
-      for (int e = lane; e < m * m; e += 32) {
-        const int i = t + 1 + w.i, k = t + 1 + w.k;
-        F[i * LDS + k] = cfms(F[i * LDS + k], F[i * LDS + t], F[t * LDS + k]);
-        w.next(m);
-      }
-    }
-    __syncwarp();
   }
 
   // 4. residual R = P A^ - L U (float-float) in a 4 x 8 lane grid, in two
