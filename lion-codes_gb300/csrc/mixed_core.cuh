@@ -602,7 +602,7 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
 //    masks; the pivots 1 + d_t go to `diag` and their logs are taken one per
 //    lane at the end.
 template <int N>
-__device__ bool mixed_finish_tile(const float2 *F, const float2 *Rm, float2 *diag, int lane,
+__device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int lane,
                                   float theta2, int exp_sum, CFF &prod, float2 &corr) {
   constexpr int LDS = N + 1;
   constexpr int SA = (N + 3) / 4;
@@ -693,6 +693,7 @@ __device__ bool mixed_finish_tile(const float2 *F, const float2 *Rm, float2 *dia
   }
 
   // acceptance (as in mixed_finish), decided on lane 0's sum
+  bool series;
   {
     float f = 0.0f;
 #pragma unroll
@@ -705,6 +706,53 @@ __device__ bool mixed_finish_tile(const float2 *F, const float2 *Rm, float2 *dia
     const float la_est = fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
     const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
     if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
+    // Small E: log det(I + E) = tr E - tr(E^2)/2 + r with |r| <= ||E||_F^3 / (3 (1 - ||E||_F)).
+    // Take the two terms when that bound is below 1e-12 max(1, |log|det||) (la_est is
+    // within 1 of |log|det|| here, so la_est - 1 is a safe lower bound).
+    const float nf = sqrtf(f);
+    series = nf * f <= 3e-12f * fmaxf(1.0f, la_est - 1.0f) * (1.0f - nf);
+  }
+  if (series) {
+    // tr E: entry (t, t) sits in slot (t / 4, t / 8) of lane (t % 4, t % 8), so slot a
+    // holds a diagonal entry in the lanes with c = 4 (a % 2) + r
+    float2 tr = zero, t2 = zero;
+#pragma unroll
+    for (int a = 0; a < SA; ++a)
+      if (c == 4 * (a & 1) + r && 4 * a + r < N) {
+        tr.x += Y[a][a >> 1].x;
+        tr.y += Y[a][a >> 1].y;
+      }
+    // tr(E^2) = sum_ik E_ik E_ki, the transposed entries through shared memory
+    __syncwarp();
+#pragma unroll
+    for (int a = 0; a < SA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * a + r, k = 8 * b + c;
+        if (i < N && k < N) Rm[i * LDS + k] = Y[a][b];
+      }
+    __syncwarp();
+#pragma unroll
+    for (int a = 0; a < SA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * a + r, k = 8 * b + c;
+        if (i < N && k < N) {
+          const float2 e = cmulf(Y[a][b], Rm[k * LDS + i]);
+          t2.x += e.x;
+          t2.y += e.y;
+        }
+      }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      tr.x += __shfl_xor_sync(kFull, tr.x, off);
+      tr.y += __shfl_xor_sync(kFull, tr.y, off);
+      t2.x += __shfl_xor_sync(kFull, t2.x, off);
+      t2.y += __shfl_xor_sync(kFull, t2.y, off);
+    }
+    corr = make_float2(__shfl_sync(kFull, __fmaf_rn(-0.5f, t2.x, tr.x), 0),
+                       __shfl_sync(kFull, __fmaf_rn(-0.5f, t2.y, tr.y), 0));
+    return true;
   }
 
   // 5. log det(I + E)
