@@ -64,7 +64,14 @@ namespace {
 
 using namespace mixed;
 
-constexpr int kDefaultTileWarps = 4;
+// Warps per CTA and CTAs per SM the register-tiled kernels are compiled for:
+// the register budget this leaves (65536 / (32 warps blocks)) is what lets the
+// SM hold that many warps, whichever of registers or shared memory binds.
+// n = 24: 3-warp CTAs, 5 per SM (15 KB of shared memory per warp); n <= 16:
+// 4-warp CTAs, 4 per SM; n = 32: shared memory allows 8 warps whatever the
+// registers.
+constexpr int tile_max_warps(int n) { return n == 24 ? 3 : 4; }
+constexpr int tile_min_ctas(int n) { return n == 24 ? 5 : n == 32 ? 1 : 4; }
 
 // Work counters of the batched mixed kernels, {next matrix, warps done} per
 // slot. Static device memory starts at zero; each launch takes the next slot
@@ -169,7 +176,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
 
 
 template <int N>
-__global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
+__global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     lup_mixed_tile_kernel(const double2 *__restrict__ A, int lda, long long batch, float theta2,
                           unsigned int share64k, int slot, int pslot,
                           double *__restrict__ logabs,
@@ -297,7 +304,8 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   // small CTAs: the register-heavy residual tile limits residency, and
   // smaller CTAs let the scheduler fill an SM with several of them
   int warps = (int)(device_smem_optin() / per_warp);
-  const int wcap = g_tile_warps > 0 ? g_tile_warps : kDefaultTileWarps;
+  int wcap = tile_max_warps(N);
+  if (g_tile_warps > 0 && g_tile_warps < wcap) wcap = g_tile_warps;
   if (warps > wcap) warps = wcap;
   const size_t smem = per_warp * warps;
   auto kern = lup_mixed_tile_kernel<N>;
