@@ -95,6 +95,15 @@ constexpr int kPendSlots = 32;
 constexpr unsigned int kPendCap = 1u << 17;
 __device__ unsigned int g_pend[kPendSlots][kPendCap];
 __device__ unsigned int g_pend_count[kPendSlots];
+__device__ unsigned int g_pend_over[kPendSlots];  // some matrix found the list full
+
+// List entries: the matrix index, with this bit set for the FP64 route (status
+// flag LUFQHE_ST_FP64) rather than a rejection (LUFQHE_ST_FALLBACK).
+constexpr unsigned int kPendRouted = 0x80000000u;
+// logabs bits of a matrix that found the list full: the FP64 pass then scans
+// logabs for them (a quiet NaN payload no log-determinant takes)
+constexpr long long kOverFallbackBits = 0x7ff8c0ffee5eed01ll;
+constexpr long long kOverRoutedBits = 0x7ff8c0ffee5eed02ll;
 std::atomic<unsigned int> g_pend_seq{0};
 
 int next_pend_slot() { return (int)(g_pend_seq.fetch_add(1u) % kPendSlots); }
@@ -103,14 +112,25 @@ constexpr int kDeferMinN = 24;
 
 // Hand matrix b to the FP64 pass; false (warp-uniform) if there is none
 // (pslot < 0) or its list is full.
-__device__ __forceinline__ bool defer_fp64(int pslot, long long b, int lane) {
-  if (pslot < 0) return false;
+__device__ __forceinline__ bool defer_fp64(int pslot, long long b, int lane, bool routed) {
+  if (pslot < 0 || b >= (long long)kPendRouted) return false;
   unsigned int pos = 0;
   if (lane == 0) pos = atomicAdd(&g_pend_count[pslot], 1u);
   pos = __shfl_sync(kFull, pos, 0);
-  if (pos >= kPendCap || b > 0xffffffffll) return false;
-  if (lane == 0) g_pend[pslot][pos] = (unsigned int)b;
+  if (pos >= kPendCap) return false;
+  if (lane == 0) g_pend[pslot][pos] = (unsigned int)b | (routed ? kPendRouted : 0u);
   return true;
+}
+
+// Same, for a kernel that holds no FP64 factorisation of its own: a matrix
+// that finds the list full is marked in logabs for the FP64 pass's scan.
+__device__ __forceinline__ void defer_fp64_always(int pslot, long long b, int lane, bool routed,
+                                                  double *logabs) {
+  if (defer_fp64(pslot, b, lane, routed)) return;
+  if (lane == 0) {
+    logabs[b] = __longlong_as_double(routed ? kOverRoutedBits : kOverFallbackBits);
+    atomicOr(&g_pend_over[pslot], 1u);
+  }
 }
 
 __device__ __forceinline__ void release_slot(int slot, int lane) {
@@ -167,7 +187,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     float2 corr;
     if (mixed_factor(S, n, lane, theta2, prod, exp_sum, corr, par))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else if (!defer_fp64(pslot, b, lane))
+    else if (!defer_fp64(pslot, b, lane, false))
       fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -183,6 +203,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // n >= 24: every FP64 factorisation goes to the FP64 pass, so this kernel
+  // carries no FP64 factorisation code (a smaller instruction footprint)
+  constexpr bool DEFER = N >= kDeferMinN;
   constexpr int LDS = N + 1;
   constexpr size_t NL = (size_t)N * LDS;
   const int warps = blockDim.x >> 5;
@@ -206,8 +229,11 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     const double2 *src = A + (size_t)b * N * lda;
     double2 *M = reinterpret_cast<double2 *>(HL);
     if (route_fp64(src, share64k)) {
-      fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                    LUFQHE_ST_FP64);
+      if constexpr (DEFER)
+        defer_fp64_always(pslot, b, lane, true, logabs);
+      else
+        fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                      LUFQHE_ST_FP64);
       continue;
     }
     if (load_matrix_fp64(src, N, lda, M, LDS, lane)) {
@@ -219,7 +245,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     float2 corr;
     if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else if (!defer_fp64(pslot, b, lane))
+    else if constexpr (DEFER)
+      defer_fp64_always(pslot, b, lane, false, logabs);
+    else
       fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -228,12 +256,14 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
 
 // The FP64 pass: warps claim the pending list's entries one at a time and
 // refactorise those matrices (reference pivot rule, fused arithmetic, status
-// flag LUFQHE_ST_FALLBACK); the last warp out empties the list for its next
-// user.
+// flag LUFQHE_ST_FALLBACK, or LUFQHE_ST_FP64 for the routed share). If the
+// list overflowed, claims past its end are chunks of 32 matrices whose logabs
+// the FP32 pass marked. The last CTA out empties the list for its next user.
 __global__ void __launch_bounds__(4 * 32)
-    lup_mixed_fallback_kernel(const double2 *__restrict__ A, int n, int lda, int slot, int pslot,
-                              double *__restrict__ logabs, double *__restrict__ phase,
-                              int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+    lup_mixed_fallback_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
+                              int slot, int pslot, double *__restrict__ logabs,
+                              double *__restrict__ phase, int8_t *__restrict__ parity,
+                              int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
@@ -246,19 +276,38 @@ __global__ void __launch_bounds__(4 * 32)
   __shared__ unsigned int cta_done;
   if (threadIdx.x == 0) cta_done = 0u;
   __syncthreads();
-  const unsigned long long count =
+  const unsigned long long listed =
       min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
+  const unsigned long long chunks =
+      *(volatile unsigned int *)&g_pend_over[pslot] ? (unsigned long long)(batch + 31) / 32 : 0ull;
+  const unsigned long long claims = listed + chunks;
   for (;;) {
     // look before claiming: in a grid sized for a long list, most warps find
     // a short one already taken and leave without touching the counter
-    unsigned long long j = count;
-    if (lane == 0 && *(volatile unsigned long long *)&g_work[slot][0] < count)
+    unsigned long long j = claims;
+    if (lane == 0 && *(volatile unsigned long long *)&g_work[slot][0] < claims)
       j = atomicAdd(&g_work[slot][0], 1ull);
     j = __shfl_sync(kFull, j, 0);
-    if (j >= count) break;
-    const long long b = g_pend[pslot][j];
-    fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
-                  status);
+    if (j >= claims) break;
+    if (j < listed) {
+      const unsigned int e = g_pend[pslot][j];
+      const long long b = e & ~kPendRouted;
+      fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
+                    status, (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+      continue;
+    }
+    const long long b0 = (long long)(j - listed) * 32;
+    long long bits = 0;
+    if (b0 + lane < batch) bits = __double_as_longlong(logabs[b0 + lane]);
+    const unsigned int routed = __ballot_sync(kFull, bits == kOverRoutedBits);
+    unsigned int mask = __ballot_sync(kFull, bits == kOverFallbackBits) | routed;
+    while (mask) {
+      const int q = __ffs(mask) - 1;
+      mask &= mask - 1u;
+      const long long b = b0 + q;
+      fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
+                    status, (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+    }
   }
   // one release per CTA: the last CTA out empties the list and the counter
   if (lane == 0 && atomicAdd(&cta_done, 1u) == (unsigned int)warps - 1u) {
@@ -266,6 +315,7 @@ __global__ void __launch_bounds__(4 * 32)
       atomicExch(&g_work[slot][0], 0ull);
       atomicExch(&g_work[slot][1], 0ull);
       atomicExch(&g_pend_count[pslot], 0u);
+      atomicExch(&g_pend_over[pslot], 0u);
     }
   }
 }
@@ -292,8 +342,9 @@ int launch_fallback(const double2 *A, int n, int lda, long long batch, int pslot
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  lup_mixed_fallback_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, next_work_slot(), pslot,
-                                                                logabs, phase, parity, status);
+  lup_mixed_fallback_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, next_work_slot(),
+                                                                pslot, logabs, phase, parity,
+                                                                status);
   return check_cuda(cudaGetLastError(), "lup_mixed_fallback_kernel launch");
 }
 

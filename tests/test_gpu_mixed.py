@@ -174,3 +174,25 @@ def test_mixed_deterministic_across_batch_positions(cuda, lufqhe_mod):
                                             mode=lufqhe_mod.MODE_MIXED))
         assert one["logabs"][0] == full["logabs"][idx]
         assert one["phase"][0] == full["phase"][idx]
+
+
+@pytest.mark.parametrize("share", [0.0, 0.5])
+def test_fp64_pass_list_overflow(cuda, lufqhe_mod, threshold, fp64_share, share):
+    """n = 24 hands every FP64 factorisation to the second pass through a list
+    of 131072 entries per call; with every matrix rejected (threshold 0) a batch
+    just past that size overflows it, and the marked rest must be found too."""
+    threshold(0.0)
+    fp64_share(share)
+    batch = 131072 + 1028
+    A, _ = lufqhe_mod.gen_lll(batch, 24, seed=13)
+    out = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
+    flags = lufqhe_mod.ST_FALLBACK | lufqhe_mod.ST_FP64
+    assert np.isin(out["status"] & flags, [lufqhe_mod.ST_FALLBACK, lufqhe_mod.ST_FP64]).all()
+    routed = ((out["status"] & lufqhe_mod.ST_FP64) != 0).mean()
+    assert abs(routed - share) < 0.02
+    assert np.array_equal(out["logabs"], fused["logabs"], equal_nan=True)
+    assert np.array_equal(out["phase"], fused["phase"], equal_nan=True)
+    assert ((out["status"] & ~flags) == fused["status"]).all()
+    del A
+    cuda.cuda.empty_cache()
