@@ -86,6 +86,23 @@ int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int d
                          void *stream);
 
 /*
+ * Same call on HOST buffers: the batch and the four result arrays are in host
+ * memory. Replaces the copy-in / LUCoreGPU::CALL / copy-out sequence of the
+ * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329). The
+ * batch is cut into chunks that two internal streams carry through
+ * host-to-device copy, the batched kernels and device-to-host copy, so copies
+ * of one chunk overlap the factorisation of another. Device staging comes from
+ * the stream-ordered allocator and is released on `stream`. Host buffers
+ * should be page-locked (cudaHostAlloc / cudaHostRegister) for the copies to
+ * overlap; pageable memory works but serialises them. Asynchronous on
+ * `stream`: the results are in host memory once `stream` has completed.
+ * d_parity / d_status may be NULL as in lufqhe_batch_lup_det.
+ */
+int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long long batch, int dtype,
+                              int mode, double *h_logabs, double *h_phase, int8_t *h_parity,
+                              int32_t *h_status, void *stream);
+
+/*
  * In-place variant: overwrites each matrix with its L\U factors (unit-lower L
  * below the diagonal, U on and above it, rows in pivoted order) exactly as the
  * reference kernel leaves global memory (LU-fqhe/src/LUCoreGPU.cu:318-377).

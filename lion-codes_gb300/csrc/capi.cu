@@ -80,6 +80,27 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
 
 }  // namespace
 
+namespace lufqhe {
+
+// The batched kernels for one mode (arguments already checked).
+int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s) {
+  switch (mode) {
+    case LUFQHE_MODE_PLAIN_FP64:
+      return launch_plain(A, nullptr, n, lda, batch, ARITH_REF, logabs, phase, parity, status, s);
+    case LUFQHE_MODE_PLAIN_FP64_FUSED:
+      return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity, status,
+                          s);
+    case LUFQHE_MODE_MIXED:
+      return launch_mixed(A, n, lda, batch, logabs, phase, parity, status, s);
+    default:
+      set_error("lufqhe_batch_lup_det: unknown mode %d", mode);
+      return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+}
+
+}  // namespace lufqhe
+
 extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int dtype,
                                     int mode, double *d_logabs, double *d_phase,
                                     int8_t *d_parity, int32_t *d_status, void *stream) {
@@ -89,21 +110,8 @@ extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long b
     set_error("lufqhe_batch_lup_det: dtype %d not supported (complex128 only)", dtype);
     return LUFQHE_ERR_UNSUPPORTED_MODE;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  const double2 *A = reinterpret_cast<const double2 *>(d_A);
-  switch (mode) {
-    case LUFQHE_MODE_PLAIN_FP64:
-      return launch_plain(A, nullptr, n, lda, batch, ARITH_REF, d_logabs, d_phase, d_parity,
-                          d_status, s);
-    case LUFQHE_MODE_PLAIN_FP64_FUSED:
-      return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, d_logabs, d_phase, d_parity,
-                          d_status, s);
-    case LUFQHE_MODE_MIXED:
-      return launch_mixed(A, n, lda, batch, d_logabs, d_phase, d_parity, d_status, s);
-    default:
-      set_error("lufqhe_batch_lup_det: unknown mode %d", mode);
-      return LUFQHE_ERR_UNSUPPORTED_MODE;
-  }
+  return batch_det_device(reinterpret_cast<const double2 *>(d_A), n, lda, batch, mode, d_logabs,
+                          d_phase, d_parity, d_status, (cudaStream_t)stream);
 }
 
 extern "C" int lufqhe_batch_lup_factor_inplace(void *d_A, int n, int lda, long long batch,

@@ -1,0 +1,151 @@
+// Host-buffer form of the batched determinant: chunked copy / compute / copy
+// pipeline over two internal streams.
+//
+// The reference's Monte Carlo loop copies the batch to the device, runs the
+// LU kernel and copies the result back, one step after the other on one
+// stream (LU-fqhe/src/MonteCarloLoop.cu:316-329). Here chunk c goes to stream
+// c % 2: H2D copy, the batched kernels, D2H copy of its results. Each stream's
+// steps stay in order, and the other stream's chunk fills the gaps, so the
+// copy engines (one per direction) and the SMs work at the same time. The
+// caller's stream is forked into the two streams at entry and joined at exit;
+// staging memory comes from cudaMallocAsync on the caller's stream and is
+// freed there after the join.
+
+#include <mutex>
+
+#include "lufqhe_internal.cuh"
+
+namespace lufqhe {
+namespace {
+
+constexpr int kMaxDevices = 64;
+constexpr size_t kChunkBytes = 32u << 20;  // input bytes per chunk
+
+struct PipeStreams {
+  cudaStream_t s[2] = {nullptr, nullptr};
+};
+
+int pipe_streams(PipeStreams *out) {
+  static std::mutex mu;
+  static PipeStreams per_dev[kMaxDevices];
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("device %d out of range", dev);
+    return LUFQHE_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < 2 && !rc; ++i)
+    if (!per_dev[dev].s[i])
+      rc = check_cuda(cudaStreamCreateWithFlags(&per_dev[dev].s[i], cudaStreamNonBlocking),
+                      "pipeline stream");
+  *out = per_dev[dev];
+  return rc;
+}
+
+}  // namespace
+
+int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s);
+
+}  // namespace lufqhe
+
+using namespace lufqhe;
+
+extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long long batch,
+                                         int dtype, int mode, double *h_logabs, double *h_phase,
+                                         int8_t *h_parity, int32_t *h_status, void *stream) {
+  if ((batch > 0 && (!h_A || !h_logabs)) || n < 1 || lda < n || batch < 0) {
+    set_error("lufqhe_batch_lup_det_host: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (n > LUFQHE_MAX_N) {
+    set_error("lufqhe_batch_lup_det_host: n=%d exceeds the supported maximum %d", n,
+              LUFQHE_MAX_N);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  if (dtype != LUFQHE_C128) {
+    set_error("lufqhe_batch_lup_det_host: dtype %d not supported (complex128 only)", dtype);
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  if (mode != LUFQHE_MODE_PLAIN_FP64 && mode != LUFQHE_MODE_PLAIN_FP64_FUSED &&
+      mode != LUFQHE_MODE_MIXED) {
+    set_error("lufqhe_batch_lup_det_host: unknown mode %d", mode);
+    return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+  if (batch == 0) return LUFQHE_SUCCESS;
+  cudaStream_t user = (cudaStream_t)stream;
+  PipeStreams ps;
+  int rc = pipe_streams(&ps);
+  if (rc) return rc;
+
+  const size_t mat_bytes = (size_t)n * lda * sizeof(double2);
+  long long per_chunk = (long long)(kChunkBytes / mat_bytes);
+  if (per_chunk < 1) per_chunk = 1;
+  const long long chunks = (batch + per_chunk - 1) / per_chunk;
+  const int nbuf = chunks > 1 ? 2 : 1;
+  // per staging buffer: the chunk's matrices and its four result arrays
+  const size_t in_bytes = (size_t)per_chunk * mat_bytes;
+  const size_t out_bytes = (size_t)per_chunk * (2 * sizeof(double) + sizeof(int8_t) + sizeof(int32_t));
+  const size_t buf_bytes = ((in_bytes + 255) & ~(size_t)255) + ((out_bytes + 255) & ~(size_t)255);
+  unsigned char *stage = nullptr;
+  rc = check_cuda(cudaMallocAsync((void **)&stage, buf_bytes * nbuf, user), "cudaMallocAsync(stage)");
+  if (rc) return rc;
+
+  cudaEvent_t fork = nullptr, done[2] = {nullptr, nullptr};
+  rc = check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+  for (int i = 0; i < 2 && !rc; ++i)
+    rc = check_cuda(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming), "event");
+  if (!rc) rc = check_cuda(cudaEventRecord(fork, user), "fork record");
+  for (int i = 0; i < nbuf && !rc; ++i)
+    rc = check_cuda(cudaStreamWaitEvent(ps.s[i], fork, 0), "fork wait");
+
+  const unsigned char *hA = reinterpret_cast<const unsigned char *>(h_A);
+  for (long long c = 0; c < chunks && !rc; ++c) {
+    const int k = (int)(c % nbuf);
+    cudaStream_t s = ps.s[k];
+    const long long lo = c * per_chunk;
+    const long long cnt = (lo + per_chunk <= batch) ? per_chunk : batch - lo;
+    unsigned char *buf = stage + (size_t)k * buf_bytes;
+    double2 *dA = reinterpret_cast<double2 *>(buf);
+    double *dla = reinterpret_cast<double *>(buf + ((in_bytes + 255) & ~(size_t)255));
+    double *dph = dla + per_chunk;
+    int32_t *dst = reinterpret_cast<int32_t *>(dph + per_chunk);
+    int8_t *dpa = reinterpret_cast<int8_t *>(dst + per_chunk);
+    rc = check_cuda(cudaMemcpyAsync(dA, hA + (size_t)lo * mat_bytes, (size_t)cnt * mat_bytes,
+                                    cudaMemcpyHostToDevice, s),
+                    "H2D chunk");
+    if (!rc)
+      rc = batch_det_device(dA, n, lda, cnt, mode, dla, h_phase ? dph : nullptr,
+                            h_parity ? dpa : nullptr, h_status ? dst : nullptr, s);
+    if (!rc)
+      rc = check_cuda(cudaMemcpyAsync(h_logabs + lo, dla, (size_t)cnt * sizeof(double),
+                                      cudaMemcpyDeviceToHost, s),
+                      "D2H logabs");
+    if (!rc && h_phase)
+      rc = check_cuda(cudaMemcpyAsync(h_phase + lo, dph, (size_t)cnt * sizeof(double),
+                                      cudaMemcpyDeviceToHost, s),
+                      "D2H phase");
+    if (!rc && h_status)
+      rc = check_cuda(cudaMemcpyAsync(h_status + lo, dst, (size_t)cnt * sizeof(int32_t),
+                                      cudaMemcpyDeviceToHost, s),
+                      "D2H status");
+    if (!rc && h_parity)
+      rc = check_cuda(cudaMemcpyAsync(h_parity + lo, dpa, (size_t)cnt * sizeof(int8_t),
+                                      cudaMemcpyDeviceToHost, s),
+                      "D2H parity");
+  }
+  // join both streams back into the caller's stream, then release the staging
+  for (int i = 0; i < nbuf; ++i) {
+    int r2 = check_cuda(cudaEventRecord(done[i], ps.s[i]), "join record");
+    if (!r2) r2 = check_cuda(cudaStreamWaitEvent(user, done[i], 0), "join wait");
+    if (!rc) rc = r2;
+  }
+  int r3 = check_cuda(cudaFreeAsync(stage, user), "cudaFreeAsync(stage)");
+  if (!rc) rc = r3;
+  if (fork) cudaEventDestroy(fork);
+  for (int i = 0; i < 2; ++i)
+    if (done[i]) cudaEventDestroy(done[i]);
+  return rc;
+}

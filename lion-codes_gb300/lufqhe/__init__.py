@@ -78,6 +78,30 @@ def batch_lup_det(A, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | 
     return out
 
 
+def batch_lup_det_host(A, mode: int = MODE_PLAIN_FP64, stream=None,
+                       out: DetResult | None = None) -> DetResult:
+    """Determinants of a (batch, n, lda) complex128 tensor in HOST memory, results
+    in host memory: the library pipelines the copies with the factorisation.
+    Page-locked tensors (pin_memory) let the copies overlap. The call is
+    asynchronous on `stream`; synchronise it before reading `out`."""
+    import torch
+    batch, n, lda = _shape(A, None)
+    if A.dtype != torch.complex128 or A.is_cuda or not A.is_contiguous():
+        raise TypeError("A must be a contiguous complex128 host tensor")
+    if out is None:
+        pin = A.is_pinned()
+        out = DetResult(torch.empty(batch, dtype=torch.float64, pin_memory=pin),
+                        torch.empty(batch, dtype=torch.float64, pin_memory=pin),
+                        torch.empty(batch, dtype=torch.int8, pin_memory=pin),
+                        torch.empty(batch, dtype=torch.int32, pin_memory=pin))
+    rc = lib().lufqhe_batch_lup_det_host(A.data_ptr(), n, lda, batch, 0, mode,
+                                         out.logabs.data_ptr(), out.phase.data_ptr(),
+                                         out.parity.data_ptr(), out.status.data_ptr(),
+                                         _stream_ptr(stream))
+    _native.check(rc, "lufqhe_batch_lup_det_host")
+    return out
+
+
 def factor_inplace(A, mode: int = MODE_PLAIN_FP64, stream=None) -> DetResult:
     """Overwrite A with its L\\U factors (pivoted row order); return the determinants."""
     import torch

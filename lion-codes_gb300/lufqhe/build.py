@@ -24,7 +24,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
 
-SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu"]
+SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu"]
 
 
 def _nvcc() -> str:

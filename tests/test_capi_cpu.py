@@ -59,6 +59,24 @@ def test_argument_validation(lufqhe_mod, args, code):
         assert len(lib.lufqhe_last_error()) > 0
 
 
+@pytest.mark.parametrize("args,code", [
+    ((None, 8, 8, 4, 0, 0, FAKE, None, None, None, None), -1),     # null A
+    ((None, 8, 8, 0, 0, 0, None, None, None, None, None), 0),      # empty batch: no-op
+    ((FAKE, 8, 8, 4, 0, 0, None, None, None, None, None), -1),     # null logabs
+    ((FAKE, 8, 7, 4, 0, 0, FAKE, None, None, None, None), -1),     # lda < n
+    ((FAKE, 8, 8, -1, 0, 0, FAKE, None, None, None, None), -1),    # batch < 0
+    ((FAKE, 65, 65, 4, 0, 0, FAKE, None, None, None, None), -2),   # n too large
+    ((FAKE, 8, 8, 4, 1, 0, FAKE, None, None, None, None), -4),     # complex64 not offered
+    ((FAKE, 8, 8, 4, 0, 9, FAKE, None, None, None, None), -4),     # unknown mode
+])
+def test_host_entry_argument_validation(lufqhe_mod, args, code):
+    """The host-buffer entry point checks its arguments before any CUDA call."""
+    lib = lufqhe_mod.lib()
+    assert lib.lufqhe_batch_lup_det_host(*args) == code
+    if code != 0:
+        assert len(lib.lufqhe_last_error()) > 0
+
+
 def test_inplace_rejects_mixed(lufqhe_mod):
     lib = lufqhe_mod.lib()
     rc = lib.lufqhe_batch_lup_factor_inplace(FAKE, 8, 8, 4, 2, FAKE, None, None, None, None)
