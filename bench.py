@@ -73,9 +73,9 @@ def mixed_launches_per_call(n: int) -> int:
     return 2 if n == 24 else 1
 
 
-def host_chunks(n: int, lda: int, batch: int) -> int:
-    """Chunks lufqhe_batch_lup_det_host cuts a batch into (32 MiB of input each)."""
-    per = max(1, (32 << 20) // (n * lda * 16))
+def host_chunks(n: int, lda: int, batch: int, chunk_mb: int = 32) -> int:
+    """Chunks lufqhe_batch_lup_det_host cuts a batch into (chunk_mb MiB of input each)."""
+    per = max(1, (chunk_mb << 20) // (n * lda * 16))
     return (batch + per - 1) // per
 
 

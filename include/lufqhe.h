@@ -89,7 +89,7 @@ int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int d
  * Same call on HOST buffers: the batch and the four result arrays are in host
  * memory. Replaces the copy-in / LUCoreGPU::CALL / copy-out sequence of the
  * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329). The
- * batch is cut into chunks that two internal streams carry through
+ * batch is cut into chunks that three internal streams carry through
  * host-to-device copy, the batched kernels and device-to-host copy, so copies
  * of one chunk overlap the factorisation of another. Device staging comes from
  * the stream-ordered allocator and is released on `stream`. Host buffers
@@ -270,6 +270,9 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
  * takes the same path wherever it sits); the FP64 pipe then works beside the
  * FP32 pipes. A negative value restores the per-n default. */
 #define LUFQHE_OPT_FP64_SHARE 3
+/* Input bytes per chunk of lufqhe_batch_lup_det_host, in MiB (1..1024; default
+ * 32). */
+#define LUFQHE_OPT_HOST_CHUNK_MB 4
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

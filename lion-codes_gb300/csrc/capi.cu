@@ -162,6 +162,7 @@ namespace lufqhe {
 extern float g_mixed_theta;
 extern int g_tile_warps;
 extern float g_fp64_share;
+extern int g_host_chunk_mb;
 }
 
 extern "C" int lufqhe_set_option(int option, double value) {
@@ -189,6 +190,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_fp64_share = (float)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_HOST_CHUNK_MB) {
+    if (!(value >= 1.0 && value <= 1024.0)) {
+      set_error("lufqhe_set_option: host chunk must be 1..1024 MiB");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_host_chunk_mb = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   set_error("lufqhe_set_option: unknown option %d", option);
   return LUFQHE_ERR_INVALID_ARG;
 }
@@ -197,6 +206,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_MIXED_THRESHOLD) return (double)g_mixed_theta;
   if (option == LUFQHE_OPT_TILE_WARPS) return (double)g_tile_warps;
   if (option == LUFQHE_OPT_FP64_SHARE) return (double)g_fp64_share;
+  if (option == LUFQHE_OPT_HOST_CHUNK_MB) return (double)g_host_chunk_mb;
   return NAN;
 }
 

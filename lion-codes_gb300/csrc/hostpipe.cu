@@ -1,12 +1,14 @@
 // Host-buffer form of the batched determinant: chunked copy / compute / copy
-// pipeline over two internal streams.
+// pipeline over three internal streams.
 //
 // The reference's Monte Carlo loop copies the batch to the device, runs the
 // LU kernel and copies the result back, one step after the other on one
 // stream (LU-fqhe/src/MonteCarloLoop.cu:316-329). Here chunk c goes to stream
-// c % 2: H2D copy, the batched kernels, D2H copy of its results. Each stream's
-// steps stay in order, and the other stream's chunk fills the gaps, so the
-// copy engines (one per direction) and the SMs work at the same time. The
+// c % 3 with its own staging buffer: H2D copy, the batched kernels, D2H copy
+// of its results. Each stream's steps stay in order; with three streams the
+// H2D copies of the next two chunks queue behind each other on the copy
+// engine while a chunk is factorised, and one chunk's kernels fill the tail of
+// another's, so the link (about 210 GB/s host-to-device on GB300) stays busy. The
 // caller's stream is forked into the two streams at entry and joined at exit;
 // staging memory comes from cudaMallocAsync on the caller's stream and is
 // freed there after the join.
@@ -19,10 +21,11 @@ namespace lufqhe {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr size_t kChunkBytes = 32u << 20;  // input bytes per chunk
+
+constexpr int kPipe = 3;
 
 struct PipeStreams {
-  cudaStream_t s[2] = {nullptr, nullptr};
+  cudaStream_t s[kPipe] = {};
 };
 
 int pipe_streams(PipeStreams *out) {
@@ -36,7 +39,7 @@ int pipe_streams(PipeStreams *out) {
     return LUFQHE_ERR_CUDA;
   }
   std::lock_guard<std::mutex> lock(mu);
-  for (int i = 0; i < 2 && !rc; ++i)
+  for (int i = 0; i < kPipe && !rc; ++i)
     if (!per_dev[dev].s[i])
       rc = check_cuda(cudaStreamCreateWithFlags(&per_dev[dev].s[i], cudaStreamNonBlocking),
                       "pipeline stream");
@@ -45,6 +48,8 @@ int pipe_streams(PipeStreams *out) {
 }
 
 }  // namespace
+
+int g_host_chunk_mb = 32;  // input bytes per chunk, MiB
 
 int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
                      double *phase, int8_t *parity, int32_t *status, cudaStream_t s);
@@ -81,10 +86,10 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   if (rc) return rc;
 
   const size_t mat_bytes = (size_t)n * lda * sizeof(double2);
-  long long per_chunk = (long long)(kChunkBytes / mat_bytes);
+  long long per_chunk = (long long)(((size_t)g_host_chunk_mb << 20) / mat_bytes);
   if (per_chunk < 1) per_chunk = 1;
   const long long chunks = (batch + per_chunk - 1) / per_chunk;
-  const int nbuf = chunks > 1 ? 2 : 1;
+  const int nbuf = chunks < kPipe ? (int)chunks : kPipe;
   // per staging buffer: the chunk's matrices and its four result arrays
   const size_t in_bytes = (size_t)per_chunk * mat_bytes;
   const size_t out_bytes = (size_t)per_chunk * (2 * sizeof(double) + sizeof(int8_t) + sizeof(int32_t));
@@ -93,9 +98,9 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   rc = check_cuda(cudaMallocAsync((void **)&stage, buf_bytes * nbuf, user), "cudaMallocAsync(stage)");
   if (rc) return rc;
 
-  cudaEvent_t fork = nullptr, done[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, done[kPipe] = {};
   rc = check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
-  for (int i = 0; i < 2 && !rc; ++i)
+  for (int i = 0; i < nbuf && !rc; ++i)
     rc = check_cuda(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming), "event");
   if (!rc) rc = check_cuda(cudaEventRecord(fork, user), "fork record");
   for (int i = 0; i < nbuf && !rc; ++i)
@@ -138,6 +143,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   }
   // join both streams back into the caller's stream, then release the staging
   for (int i = 0; i < nbuf; ++i) {
+    if (!done[i]) continue;
     int r2 = check_cuda(cudaEventRecord(done[i], ps.s[i]), "join record");
     if (!r2) r2 = check_cuda(cudaStreamWaitEvent(user, done[i], 0), "join wait");
     if (!rc) rc = r2;
@@ -145,7 +151,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   int r3 = check_cuda(cudaFreeAsync(stage, user), "cudaFreeAsync(stage)");
   if (!rc) rc = r3;
   if (fork) cudaEventDestroy(fork);
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < kPipe; ++i)
     if (done[i]) cudaEventDestroy(done[i]);
   return rc;
 }
