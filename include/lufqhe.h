@@ -86,6 +86,19 @@ int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int d
                          void *stream);
 
 /*
+ * Determinants of lowest-Landau-level orbital matrices built on the device
+ * from particle coordinates: matrix b is M_ik = z_i^k exp(-|z_i|^2/4) with
+ * z = d_z[b*n .. b*n+n) (complex128). The matrices are built in shared memory
+ * by the factorising kernels themselves, so a call reads 16n bytes per matrix
+ * instead of 16n^2. This is the reference's intended on-device matrix-element
+ * builder (LU-fqhe/src/mkMatrixElements.cu:169-358, compiled out there) fused
+ * into the LUP prologue; the results are bit-identical to lufqhe_gen_lll's
+ * matrices passed to lufqhe_batch_lup_det. Modes and outputs as there.
+ */
+int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode, double *d_logabs,
+                   double *d_phase, int8_t *d_parity, int32_t *d_status, void *stream);
+
+/*
  * Same call on HOST buffers: the batch and the four result arrays are in host
  * memory. Replaces the copy-in / LUCoreGPU::CALL / copy-out sequence of the
  * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329). The

@@ -114,6 +114,28 @@ extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long b
                           d_phase, d_parity, d_status, (cudaStream_t)stream);
 }
 
+extern "C" int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode,
+                              double *d_logabs, double *d_phase, int8_t *d_parity,
+                              int32_t *d_status, void *stream) {
+  int rc = check_common(d_z, n, n, batch, d_logabs, "lufqhe_lll_det");
+  if (rc) return rc;
+  if (batch == 0) return LUFQHE_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  const double2 *Z = reinterpret_cast<const double2 *>(d_z);
+  switch (mode) {
+    case LUFQHE_MODE_PLAIN_FP64:
+      return launch_plain_lll(Z, n, batch, ARITH_REF, d_logabs, d_phase, d_parity, d_status, s);
+    case LUFQHE_MODE_PLAIN_FP64_FUSED:
+      return launch_plain_lll(Z, n, batch, ARITH_FUSED, d_logabs, d_phase, d_parity, d_status,
+                              s);
+    case LUFQHE_MODE_MIXED:
+      return launch_mixed_lll(Z, n, batch, d_logabs, d_phase, d_parity, d_status, s);
+    default:
+      set_error("lufqhe_lll_det: unknown mode %d", mode);
+      return LUFQHE_ERR_UNSUPPORTED_MODE;
+  }
+}
+
 extern "C" int lufqhe_batch_lup_factor_inplace(void *d_A, int n, int lda, long long batch,
                                                int mode, double *d_logabs, double *d_phase,
                                                int8_t *d_parity, int32_t *d_status,

@@ -9,7 +9,7 @@
 
 #include <cmath>
 
-#include "lufqhe_internal.cuh"
+#include "lup_fp64.cuh"
 
 namespace lufqhe {
 
@@ -48,8 +48,10 @@ __host__ __device__ inline double2 lll_z(unsigned long long key, long long b, in
   return make_double2(g0 * scale, g1 * scale);
 }
 
-// Row i of an LLL matrix: M_ik = z^k exp(-|z|^2/4) by repeated multiplication.
-__host__ __device__ inline void lll_row(double2 z, int n, double2 *row, int stride) {
+// Row i of an LLL matrix on the host: M_ik = z^k exp(-|z|^2/4) by repeated
+// multiplication, the same steps as the device's lll_row_rn (the host compiler
+// may fuse some of them, so host and device agree to rounding, not in bits).
+inline void lll_row(double2 z, int n, double2 *row, int stride) {
   double w = exp(-(z.x * z.x + z.y * z.y) * 0.25);
   double px = 1.0, py = 0.0;
   for (int k = 0; k < n; ++k) {
@@ -82,7 +84,8 @@ __global__ void gen_lll_kernel(double2 *A, double2 *Z, int n, int lda, long long
     int i = (int)(e - b * n);
     double2 z = lll_z(key, b, n, i, scale);
     if (Z) Z[e] = z;
-    lll_row(z, n, A + (size_t)b * n * lda + (size_t)i * lda, 1);
+    // the same explicitly rounded row as the kernels that build rows from z
+    lll_row_rn(z, n, A + (size_t)b * n * lda + (size_t)i * lda);
   }
 }
 

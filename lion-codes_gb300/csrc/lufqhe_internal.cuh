@@ -111,6 +111,12 @@ int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batc
 // Mixed mode's precision policy: the share (in 1/65536) of n x n matrices
 // sent straight to the FP64 kernel, chosen by content hash.
 unsigned int fp64_share_64k(int n);
+// Same kernels on LLL orbital matrices built from n coordinates per matrix.
+int launch_plain_lll(const double2 *Z, int n, long long batch, int arith, double *logabs,
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
+                     int status_or = 0);
+int launch_mixed_lll(const double2 *Z, int n, long long batch, double *logabs, double *phase,
+                     int8_t *parity, int32_t *status, cudaStream_t stream);
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
                  double *phase, int8_t *parity, int32_t *status, cudaStream_t stream);
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,

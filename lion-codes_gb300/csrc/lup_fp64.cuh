@@ -58,6 +58,66 @@ __device__ __forceinline__ bool load_matrix_fp64(const double2 *__restrict__ src
   return bad;
 }
 
+// Row of a lowest-Landau-level orbital matrix: M_ik = z^k exp(-|z|^2/4) for
+// k < n, by repeated complex multiplication. Every operation is explicitly
+// rounded (no contraction), so every kernel that builds a row gets the same
+// bits. Returns false if an entry is NaN/Inf.
+__device__ __forceinline__ bool lll_row_rn(double2 z, int n, double2 *row) {
+  const double w = exp(__dmul_rn(-__dadd_rn(__dmul_rn(z.x, z.x), __dmul_rn(z.y, z.y)), 0.25));
+  double px = 1.0, py = 0.0;
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {
+    const double2 v = make_double2(__dmul_rn(px, w), __dmul_rn(py, w));
+    ok &= finite_c(v);
+    row[k] = v;
+    const double nx = __dsub_rn(__dmul_rn(px, z.x), __dmul_rn(py, z.y));
+    const double ny = __dadd_rn(__dmul_rn(px, z.y), __dmul_rn(py, z.x));
+    px = nx;
+    py = ny;
+  }
+  return ok;
+}
+
+// Where the batched kernels take matrix b from.
+//  * DenseSource: n x n complex128 matrices in the reference layout (matrix b
+//    at b*n*lda, row stride lda).
+//  * LllSource: LLL orbital matrices built in shared memory from n particle
+//    coordinates per matrix (z of matrix b at b*n), so a call reads 16n bytes
+//    per matrix instead of 16n^2.
+// load() fills M (row stride lds) and returns true (warp-uniform) if an entry
+// is NaN/Inf; first() is entry (0,0), which the FP64 routing hashes.
+struct DenseSource {
+  const double2 *A;
+  int lda;
+  template <bool COHERENT = false>
+  __device__ __forceinline__ bool load(long long b, int n, double2 *M, int lds, int lane) const {
+    return load_matrix_fp64<COHERENT>(A + (size_t)b * n * lda, n, lda, M, lds, lane);
+  }
+  __device__ __forceinline__ double2 first(long long b, int n) const {
+    return __ldg(A + (size_t)b * n * lda);
+  }
+};
+
+struct LllSource {
+  const double2 *Z;
+  template <bool COHERENT = false>
+  __device__ __forceinline__ bool load(long long b, int n, double2 *M, int lds, int lane) const {
+    bool bad = false;
+    for (int i = lane; i < n; i += 32) {
+      const double2 z = COHERENT ? __ldcg(Z + (size_t)b * n + i) : __ldg(Z + (size_t)b * n + i);
+      bad |= !lll_row_rn(z, n, M + i * lds);
+    }
+    bad = __any_sync(kFull, bad);
+    __syncwarp();
+    return bad;
+  }
+  __device__ __forceinline__ double2 first(long long b, int n) const {
+    const double2 z = __ldg(Z + (size_t)b * n);
+    const double w = exp(__dmul_rn(-__dadd_rn(__dmul_rn(z.x, z.x), __dmul_rn(z.y, z.y)), 0.25));
+    return make_double2(__dmul_rn(1.0, w), __dmul_rn(0.0, w));
+  }
+};
+
 // RN(a / b) for b > 0 given y = RN(1/b): Markstein's correction (P. Markstein,
 // IBM J. Res. Dev. 34(1), 1990): q0 = RN(a*y) is refined once to a faithful
 // q1, then q2 = RN(q1 + RN(a - b*q1)*y) is the correctly rounded quotient when

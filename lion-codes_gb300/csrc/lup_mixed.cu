@@ -144,8 +144,9 @@ __device__ __forceinline__ void release_slot(int slot, int lane) {
   }
 }
 
+template <class Src>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
-    lup_mixed_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
+    lup_mixed_kernel(Src src, int n, long long batch,
                      float theta2, unsigned int share64k, int slot, int pslot,
                      double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status) {
@@ -171,14 +172,13 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     const long long b = claim_matrix(slot, lane);
     if (b >= batch) break;
     __syncwarp();
-    const double2 *src = A + (size_t)b * n * lda;
     double2 *M = reinterpret_cast<double2 *>(S.SC);
-    if (route_fp64(src, share64k)) {
-      fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status,
-                    LUFQHE_ST_FP64);
+    if (share64k && route_fp64_entry(src.first(b, n), share64k)) {
+      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status,
+                        LUFQHE_ST_FP64);
       continue;
     }
-    if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
+    if (src.load(b, n, M, lds, lane)) {
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
     }
@@ -188,16 +188,16 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     if (mixed_factor(S, n, lane, theta2, prod, exp_sum, corr, par))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
     else if (!defer_fp64(pslot, b, lane, false))
-      fallback_fp64(src, n, lda, M, lds, S.hold, lane, b, logabs, phase, parity, status);
+      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
   release_slot(slot, lane);
 }
 
 
-template <int N>
+template <int N, class Src>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
-    lup_mixed_tile_kernel(const double2 *__restrict__ A, int lda, long long batch, float theta2,
+    lup_mixed_tile_kernel(Src src, long long batch, float theta2,
                           unsigned int share64k, int slot, int pslot,
                           double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
@@ -226,17 +226,16 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     const long long b = claim_matrix(slot, lane);
     if (b >= batch) break;
     __syncwarp();
-    const double2 *src = A + (size_t)b * N * lda;
     double2 *M = reinterpret_cast<double2 *>(HL);
-    if (route_fp64(src, share64k)) {
+    if (share64k && route_fp64_entry(src.first(b, N), share64k)) {
       if constexpr (DEFER)
         defer_fp64_always(pslot, b, lane, true, logabs);
       else
-        fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                      LUFQHE_ST_FP64);
+        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                          LUFQHE_ST_FP64);
       continue;
     }
-    if (load_matrix_fp64(src, N, lda, M, LDS, lane)) {
+    if (src.load(b, N, M, LDS, lane)) {
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
     }
@@ -248,7 +247,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     else if constexpr (DEFER)
       defer_fp64_always(pslot, b, lane, false, logabs);
     else
-      fallback_fp64(src, N, lda, M, LDS, hold, lane, b, logabs, phase, parity, status);
+      fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
   }
   out.flush(lane, logabs, phase, parity, status);
   release_slot(slot, lane);
@@ -259,8 +258,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
 // flag LUFQHE_ST_FALLBACK, or LUFQHE_ST_FP64 for the routed share). If the
 // list overflowed, claims past its end are chunks of 32 matrices whose logabs
 // the FP32 pass marked. The last CTA out empties the list for its next user.
+template <class Src>
 __global__ void __launch_bounds__(4 * 32)
-    lup_mixed_fallback_kernel(const double2 *__restrict__ A, int n, int lda, long long batch,
+    lup_mixed_fallback_kernel(Src src, int n, long long batch,
                               int slot, int pslot, double *__restrict__ logabs,
                               double *__restrict__ phase, int8_t *__restrict__ parity,
                               int32_t *__restrict__ status) {
@@ -292,8 +292,8 @@ __global__ void __launch_bounds__(4 * 32)
     if (j < listed) {
       const unsigned int e = g_pend[pslot][j];
       const long long b = e & ~kPendRouted;
-      fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
-                    status, (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+      fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
+                        (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
       continue;
     }
     const long long b0 = (long long)(j - listed) * 32;
@@ -305,8 +305,8 @@ __global__ void __launch_bounds__(4 * 32)
       const int q = __ffs(mask) - 1;
       mask &= mask - 1u;
       const long long b = b0 + q;
-      fallback_fp64(A + (size_t)b * n * lda, n, lda, M, lds, hold, lane, b, logabs, phase, parity,
-                    status, (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+      fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
+                        (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
     }
   }
   // one release per CTA: the last CTA out empties the list and the counter
@@ -320,21 +320,21 @@ __global__ void __launch_bounds__(4 * 32)
   }
 }
 
-int launch_fallback(const double2 *A, int n, int lda, long long batch, int pslot,
-                    double *logabs, double *phase, int8_t *parity, int32_t *status,
-                    cudaStream_t stream) {
+template <class Src>
+int launch_fallback(Src src, int n, long long batch, int pslot, double *logabs, double *phase,
+                    int8_t *parity, int32_t *status, cudaStream_t stream) {
   const size_t per_warp = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
   int warps = (int)(device_smem_optin() / per_warp);
   if (warps > 4) warps = 4;
   if (warps < 1) warps = 1;
   const size_t smem = per_warp * warps;
-  int rc = check_cuda(cudaFuncSetAttribute(lup_mixed_fallback_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  auto kern = lup_mixed_fallback_kernel<Src>;
+  int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
                       "cudaFuncSetAttribute(mixed fallback)");
   if (rc) return rc;
   int per_sm = 0;
-  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lup_mixed_fallback_kernel,
-                                                                warps * 32, smem),
+  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
                   "occupancy(mixed fallback)");
   if (rc) return rc;
   if (per_sm < 1) per_sm = 1;
@@ -342,15 +342,14 @@ int launch_fallback(const double2 *A, int n, int lda, long long batch, int pslot
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  lup_mixed_fallback_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, next_work_slot(),
-                                                                pslot, logabs, phase, parity,
-                                                                status);
+  kern<<<grid, warps * 32, smem, stream>>>(src, n, batch, next_work_slot(), pslot, logabs, phase,
+                                           parity, status);
   return check_cuda(cudaGetLastError(), "lup_mixed_fallback_kernel launch");
 }
 
-template <int N>
-int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, double *logabs,
-                      double *phase, int8_t *parity, int32_t *status, cudaStream_t stream) {
+template <int N, class Src>
+int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, double *phase,
+                      int8_t *parity, int32_t *status, cudaStream_t stream) {
   const size_t per_warp = tile_smem_per_warp<N>();
   // small CTAs: the register-heavy residual tile limits residency, and
   // smaller CTAs let the scheduler fill an SM with several of them
@@ -359,7 +358,7 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   if (g_tile_warps > 0 && g_tile_warps < wcap) wcap = g_tile_warps;
   if (warps > wcap) warps = wcap;
   const size_t smem = per_warp * warps;
-  auto kern = lup_mixed_tile_kernel<N>;
+  auto kern = lup_mixed_tile_kernel<N, Src>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
                       "cudaFuncSetAttribute(mixed tile)");
@@ -373,11 +372,11 @@ int launch_mixed_tile(const double2 *A, int lda, long long batch, float theta2, 
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
   const int pslot = N >= kDeferMinN ? next_pend_slot() : -1;
-  kern<<<grid, warps * 32, smem, stream>>>(A, lda, batch, theta2, fp64_share_64k(N),
-                                           next_work_slot(), pslot, logabs, phase, parity, status);
+  kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), next_work_slot(),
+                                           pslot, logabs, phase, parity, status);
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
   if (rc || pslot < 0) return rc;
-  return launch_fallback(A, N, lda, batch, pslot, logabs, phase, parity, status, stream);
+  return launch_fallback(src, N, batch, pslot, logabs, phase, parity, status, stream);
 }
 
 }  // namespace
@@ -390,22 +389,25 @@ size_t mixed_smem_per_warp(int n) {
 
 float g_mixed_theta = 0.1f;
 
-int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
-                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream) {
+namespace {
+
+// plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
+template <class Src, class PlainFn>
+int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *phase,
+                     int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64) {
   if (batch == 0) return LUFQHE_SUCCESS;
   // every matrix on the FP64 route: the plain fused kernel, whose shared
   // memory layout holds more warps per SM than the mixed kernels'
   if (fp64_share_64k(n) >= 65536u)
-    return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity, status,
-                        stream, LUFQHE_ST_FP64);
+    return plain_fp64();
   const float th2 = g_mixed_theta * g_mixed_theta;
   switch (n) {
-    case 6: return launch_mixed_tile<6>(A, lda, batch, th2, logabs, phase, parity, status, stream);
-    case 8: return launch_mixed_tile<8>(A, lda, batch, th2, logabs, phase, parity, status, stream);
-    case 12: return launch_mixed_tile<12>(A, lda, batch, th2, logabs, phase, parity, status, stream);
-    case 16: return launch_mixed_tile<16>(A, lda, batch, th2, logabs, phase, parity, status, stream);
-    case 24: return launch_mixed_tile<24>(A, lda, batch, th2, logabs, phase, parity, status, stream);
-    case 32: return launch_mixed_tile<32>(A, lda, batch, th2, logabs, phase, parity, status, stream);
+    case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream);
     default: break;
   }
   const size_t per_warp = mixed_smem_per_warp(n);
@@ -418,13 +420,14 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
   const size_t smem = per_warp * warps;
-  int rc = check_cuda(cudaFuncSetAttribute(lup_mixed_kernel,
+  auto kern = lup_mixed_kernel<Src>;
+  int rc = check_cuda(cudaFuncSetAttribute(kern,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "cudaFuncSetAttribute(mixed)");
   if (rc) return rc;
   int per_sm = 0;
   rc = check_cuda(
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lup_mixed_kernel, warps * 32, smem),
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
       "occupancy(mixed)");
   if (rc) return rc;
   if (per_sm < 1) per_sm = 1;
@@ -433,12 +436,30 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
   int grid = (int)(want < cap ? want : cap);
   const float theta2 = g_mixed_theta * g_mixed_theta;
   const int pslot = n >= kDeferMinN ? next_pend_slot() : -1;
-  lup_mixed_kernel<<<grid, warps * 32, smem, stream>>>(A, n, lda, batch, theta2,
-                                                       fp64_share_64k(n), next_work_slot(), pslot,
-                                                       logabs, phase, parity, status);
+  kern<<<grid, warps * 32, smem, stream>>>(src, n, batch, theta2, fp64_share_64k(n),
+                                           next_work_slot(), pslot, logabs, phase, parity, status);
   rc = check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
   if (rc || pslot < 0) return rc;
-  return launch_fallback(A, n, lda, batch, pslot, logabs, phase, parity, status, stream);
+  return launch_fallback(src, n, batch, pslot, logabs, phase, parity, status, stream);
+}
+
+}  // namespace
+
+int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
+                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream) {
+  return launch_mixed_src(DenseSource{A, lda}, n, batch, logabs, phase, parity, status, stream,
+                          [&] {
+                            return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs,
+                                                phase, parity, status, stream, LUFQHE_ST_FP64);
+                          });
+}
+
+int launch_mixed_lll(const double2 *Z, int n, long long batch, double *logabs, double *phase,
+                     int8_t *parity, int32_t *status, cudaStream_t stream) {
+  return launch_mixed_src(LllSource{Z}, n, batch, logabs, phase, parity, status, stream, [&] {
+    return launch_plain_lll(Z, n, batch, ARITH_FUSED, logabs, phase, parity, status, stream,
+                            LUFQHE_ST_FP64);
+  });
 }
 
 }  // namespace lufqhe

@@ -20,9 +20,9 @@ namespace {
 
 constexpr int kMaxWarpsPlain = 8;
 
-template <int ARITH>
+template <int ARITH, class Src>
 __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
-    lup_plain_kernel(const double2 *__restrict__ A, double2 *__restrict__ Aout, int n, int lda,
+    lup_plain_kernel(Src src, double2 *__restrict__ Aout, int n, int lda,
                      long long batch, double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status,
                      int status_or) {
@@ -41,9 +41,7 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
        b += (long long)gridDim.x * warps) {
     __syncwarp();
     int par = 0;
-    int st = load_matrix_fp64(A + (size_t)b * n * lda, n, lda, M, lds, lane)
-                 ? LUFQHE_ST_NONFINITE
-                 : 0;
+    int st = src.load(b, n, M, lds, lane) ? LUFQHE_ST_NONFINITE : 0;
     if (!st) st = lup_fp64_warp<ARITH>(M, lds, hold, n, lane, &par);
 
     double la, ph;
@@ -106,9 +104,10 @@ size_t plain_smem_per_warp(int n) {
   return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
 }
 
-int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,
-                 double *logabs, double *phase, int8_t *parity, int32_t *status,
-                 cudaStream_t stream, int status_or) {
+template <class Src>
+int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, int arith,
+                     double *logabs, double *phase, int8_t *parity, int32_t *status,
+                     cudaStream_t stream, int status_or) {
   if (batch == 0) return LUFQHE_SUCCESS;
   const size_t per_warp = plain_smem_per_warp(n);
   const size_t optin = device_smem_optin();
@@ -120,7 +119,8 @@ int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batc
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
   const size_t smem = per_warp * warps;
-  auto kern = arith == ARITH_REF ? lup_plain_kernel<ARITH_REF> : lup_plain_kernel<ARITH_FUSED>;
+  auto kern =
+      arith == ARITH_REF ? lup_plain_kernel<ARITH_REF, Src> : lup_plain_kernel<ARITH_FUSED, Src>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
                       "cudaFuncSetAttribute(plain)");
@@ -133,9 +133,23 @@ int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batc
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  kern<<<grid, warps * 32, smem, stream>>>(A, Aout, n, lda, batch, logabs, phase, parity, status,
+  kern<<<grid, warps * 32, smem, stream>>>(src, Aout, n, lda, batch, logabs, phase, parity, status,
                                            status_or);
   return check_cuda(cudaGetLastError(), "lup_plain_kernel launch");
+}
+
+int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batch, int arith,
+                 double *logabs, double *phase, int8_t *parity, int32_t *status,
+                 cudaStream_t stream, int status_or) {
+  return launch_plain_src(DenseSource{A, lda}, Aout, n, lda, batch, arith, logabs, phase, parity,
+                          status, stream, status_or);
+}
+
+int launch_plain_lll(const double2 *Z, int n, long long batch, int arith, double *logabs,
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
+                     int status_or) {
+  return launch_plain_src(LllSource{Z}, nullptr, n, n, batch, arith, logabs, phase, parity, status,
+                          stream, status_or);
 }
 
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,

@@ -454,17 +454,22 @@ struct DeferredOut {
 
 // Route of a matrix in the batched mixed mode: true = straight to FP64. A hash
 // of its first entry's bits, so the route depends on the content only.
-template <bool COHERENT = false>
-__device__ __forceinline__ bool route_fp64(const double2 *src, unsigned int share64k) {
+__device__ __forceinline__ bool route_fp64_entry(double2 v, unsigned int share64k) {
   if (share64k == 0) return false;
   if (share64k >= 65536u) return true;
-  const double2 v = COHERENT ? __ldcg(src) : __ldg(src);
   unsigned long long h = (unsigned long long)__double_as_longlong(v.x) * 0x9E3779B97F4A7C15ull ^
                          (unsigned long long)__double_as_longlong(v.y);
   h ^= h >> 29;
   h *= 0xBF58476D1CE4E5B9ull;
   h ^= h >> 32;
   return (unsigned int)(h & 0xffffu) < share64k;
+}
+
+template <bool COHERENT = false>
+__device__ __forceinline__ bool route_fp64(const double2 *src, unsigned int share64k) {
+  if (share64k == 0) return false;
+  if (share64k >= 65536u) return true;
+  return route_fp64_entry(COHERENT ? __ldcg(src) : __ldg(src), share64k);
 }
 
 __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *logabs,
@@ -477,13 +482,15 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
   }
 }
 
-// FP64 refactorisation of the original matrix (reloaded into M), status |= FALLBACK.
-template <bool COHERENT = false>
-__device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, int lds,
-                              double *hold, int lane, long long b, double *logabs, double *phase,
-                              int8_t *parity, int32_t *status, int flag = LUFQHE_ST_FALLBACK) {
+// FP64 refactorisation of matrix sb of `src` (reloaded into M), results into
+// slot b, status |= flag (FALLBACK, or FP64 for the routed share).
+template <class Src, bool COHERENT = false>
+__device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *M, int lds,
+                                  double *hold, int lane, long long b, double *logabs,
+                                  double *phase, int8_t *parity, int32_t *status,
+                                  int flag = LUFQHE_ST_FALLBACK) {
   __syncwarp();
-  load_matrix_fp64<COHERENT>(src, n, lda, M, lds, lane);
+  src.template load<COHERENT>(sb, n, M, lds, lane);
   int par = 0;
   int st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par);
   double la, ph;
@@ -503,6 +510,15 @@ __device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, in
     if (parity) parity[b] = (int8_t)par;
     if (status) status[b] = st | flag;
   }
+}
+
+// Same for one dense matrix at src (row stride lda).
+template <bool COHERENT = false>
+__device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, int lds,
+                              double *hold, int lane, long long b, double *logabs, double *phase,
+                              int8_t *parity, int32_t *status, int flag = LUFQHE_ST_FALLBACK) {
+  fallback_fp64_src<DenseSource, COHERENT>(DenseSource{src, lda}, 0, n, M, lds, hold, lane, b,
+                                           logabs, phase, parity, status, flag);
 }
 
 // ---------------------------------------------------------------------------

@@ -89,17 +89,6 @@ __device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) 
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void lll_row_dev(double2 z, int n, double2 *row) {
-  const double w = exp(-(z.x * z.x + z.y * z.y) * 0.25);
-  double px = 1.0, py = 0.0;
-  for (int k = 0; k < n; ++k) {
-    row[k] = make_double2(px * w, py * w);
-    const double nx = px * z.x - py * z.y;
-    const double ny = px * z.y + py * z.x;
-    px = nx;
-    py = ny;
-  }
-}
 
 // Apply the move to the tile's matrices: z_particle <- znew, then rebuild that
 // row (lane j handles matrix j); with t.build every row of every matrix is
@@ -112,7 +101,7 @@ __device__ void apply_move(const ServeTile &t, int n, int lane) {
       if (j < t.count) {
         const double2 z = __ldcv(t.znew + j);
         t.z[(size_t)j * n + t.particle] = z;
-        if (!t.build) lll_row_dev(z, n, t.mats + (size_t)j * n * n + (size_t)t.particle * n);
+        if (!t.build) lll_row_rn(z, n, t.mats + (size_t)j * n * n + (size_t)t.particle * n);
       }
     }
     __syncwarp();
@@ -120,7 +109,7 @@ __device__ void apply_move(const ServeTile &t, int n, int lane) {
   if (t.build) {
     for (int j = 0; j < t.count; ++j)
       for (int i = lane; i < n; i += 32)
-        lll_row_dev(__ldcg(t.z + (size_t)j * n + i), n, t.mats + (size_t)j * n * n + (size_t)i * n);
+        lll_row_rn(__ldcg(t.z + (size_t)j * n + i), n, t.mats + (size_t)j * n * n + (size_t)i * n);
   }
   __syncwarp();
   __threadfence_block();

@@ -78,6 +78,26 @@ def batch_lup_det(A, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | 
     return out
 
 
+def lll_det(z, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | None = None):
+    """Determinants of the LLL orbital matrices of (batch, n) complex128 CUDA
+    coordinates z, built inside the factorising kernels."""
+    import torch
+    if z.dim() != 2 or z.dtype != torch.complex128 or not z.is_cuda or not z.is_contiguous():
+        raise TypeError("z must be a contiguous (batch, n) complex128 CUDA tensor")
+    batch, n = z.shape
+    if out is None:
+        dev = z.device
+        out = DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
+                        torch.empty(batch, dtype=torch.float64, device=dev),
+                        torch.empty(batch, dtype=torch.int8, device=dev),
+                        torch.empty(batch, dtype=torch.int32, device=dev))
+    rc = lib().lufqhe_lll_det(z.data_ptr(), n, batch, mode, out.logabs.data_ptr(),
+                              out.phase.data_ptr(), out.parity.data_ptr(), out.status.data_ptr(),
+                              _stream_ptr(stream))
+    _native.check(rc, "lufqhe_lll_det")
+    return out
+
+
 def batch_lup_det_host(A, mode: int = MODE_PLAIN_FP64, stream=None,
                        out: DetResult | None = None) -> DetResult:
     """Determinants of a (batch, n, lda) complex128 tensor in HOST memory, results

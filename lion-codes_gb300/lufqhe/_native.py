@@ -23,6 +23,7 @@ F64 = _c.c_double
 SIGNATURES = {
     "lufqhe_batch_lup_det": (I32, [P, I32, I32, I64, I32, I32, P, P, P, P, P]),
     "lufqhe_batch_lup_det_host": (I32, [P, I32, I32, I64, I32, I32, P, P, P, P, P]),
+    "lufqhe_lll_det": (I32, [P, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_batch_lup_factor_inplace": (I32, [P, I32, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_lucoregpu_call": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),

@@ -77,6 +77,22 @@ def test_host_entry_argument_validation(lufqhe_mod, args, code):
         assert len(lib.lufqhe_last_error()) > 0
 
 
+@pytest.mark.parametrize("args,code", [
+    ((None, 8, 4, 0, FAKE, None, None, None, None), -1),     # null z
+    ((None, 8, 0, 0, None, None, None, None, None), 0),      # empty batch: no-op
+    ((FAKE, 8, 4, 0, None, None, None, None, None), -1),     # null logabs
+    ((FAKE, 0, 4, 0, FAKE, None, None, None, None), -1),     # n < 1
+    ((FAKE, 65, 4, 0, FAKE, None, None, None, None), -2),    # n too large
+    ((FAKE_ODD, 8, 4, 0, FAKE, None, None, None, None), -1),  # misaligned
+    ((FAKE, 8, 4, 9, FAKE, None, None, None, None), -4),     # unknown mode
+])
+def test_lll_entry_argument_validation(lufqhe_mod, args, code):
+    lib = lufqhe_mod.lib()
+    assert lib.lufqhe_lll_det(*args) == code
+    if code != 0:
+        assert len(lib.lufqhe_last_error()) > 0
+
+
 def test_inplace_rejects_mixed(lufqhe_mod):
     lib = lufqhe_mod.lib()
     rc = lib.lufqhe_batch_lup_factor_inplace(FAKE, 8, 8, 4, 2, FAKE, None, None, None, None)
