@@ -235,14 +235,15 @@ def measure_pipe_peaks(torch, lufqhe) -> dict:
     return out
 
 
-def make_inputs(torch, lufqhe, wl):
+def make_inputs(torch, lufqhe, wl, want_z=False):
     kind, n, batch, seed = WORKLOADS[wl]
+    z = None
     if kind == "lll":
-        A, _ = lufqhe.gen_lll(batch, n, seed=seed)
+        A, z = lufqhe.gen_lll(batch, n, seed=seed)
     else:
         A = lufqhe.gen_gaussian(batch, n, seed=seed)
     torch.cuda.synchronize()
-    return A, n, batch
+    return (A, n, batch, z) if want_z else (A, n, batch)
 
 
 def time_device(torch, lufqhe, A, mode, out, steps, warmup, stream):
@@ -495,7 +496,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
-        A, n, batch = make_inputs(torch, lufqhe, args.workload)
+        A, n, batch, z_dev = make_inputs(torch, lufqhe, args.workload, want_z=True)
     torch.cuda.synchronize()
     res = lufqhe.DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
                            torch.empty(batch, dtype=torch.float64, device=dev),
@@ -565,6 +566,42 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms_e2e = max_over_ranks(world, e2.elapsed_time(e3) / args.steps)
     launches += args.steps * host_chunks(n, n, batch) * mixed_launches_per_call(n)
+
+    # ---- e2e from particle coordinates (LLL workloads) ---------------------
+    # what a Monte Carlo driver holds is z, not the matrices: H2D of the
+    # coordinates, lufqhe_lll_det (matrices built inside the kernels), D2H of
+    # the results, every step
+    e2e_coords = None
+    if z_dev is not None:
+        z_host = z_dev.contiguous().cpu().pin_memory()
+        z_buf = torch.empty_like(z_dev.contiguous())
+        res_c = lufqhe.DetResult(*(torch.empty_like(getattr(res, k))
+                                   for k in ("logabs", "phase", "parity", "status")))
+
+        def coords_step():
+            with torch.cuda.stream(stream):
+                z_buf.copy_(z_host, non_blocking=True)
+                lufqhe.lll_det(z_buf, mode=mode, stream=stream, out=res_c)
+                for k in ("logabs", "phase", "parity", "status"):
+                    getattr(out_host, k).copy_(getattr(res_c, k), non_blocking=True)
+
+        for _ in range(max(3, args.warmup)):
+            coords_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e4 = torch.cuda.Event(enable_timing=True)
+        e5 = torch.cuda.Event(enable_timing=True)
+        e4.record(stream)
+        for _ in range(args.steps):
+            coords_step()
+        e5.record(stream)
+        torch.cuda.synchronize()
+        ms_c = max_over_ranks(world, e4.elapsed_time(e5) / args.steps)
+        launches += args.steps * mixed_launches_per_call(n)
+        e2e_coords = {"value": world * batch / (ms_c * 1e-3), "unit": "dets/s", "ms_per_step": ms_c,
+                      "h2d_bytes_per_step": z_host.numel() * z_host.element_size(),
+                      "d2h_bytes_per_step": d2h,
+                      "call": "lufqhe_lll_det (orbital matrices built in the kernels from z)"}
 
     # ---- kernel-only timing of the dominant kernel (roofline) --------------
     peaks_file = load_peaks()
@@ -640,6 +677,7 @@ def run_ours(args):
             "e2e": {"value": world * batch / (ms_e2e * 1e-3), "unit": "dets/s",
                     "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
+            "e2e_from_coordinates": e2e_coords,
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
