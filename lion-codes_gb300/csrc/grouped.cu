@@ -41,19 +41,38 @@ struct WorkItem {
   int n;
   int lda;
   unsigned int share64k;  // mixed mode: share routed straight to FP64 (1/65536)
+  int status_or;          // bits OR-ed into each status (FP64 route of a mixed plan)
 };
 
-size_t warp_smem_bytes(int nmax) {
-  const size_t lds = (size_t)nmax + 1;
-  return (size_t)nmax * lds * (sizeof(float4) + sizeof(float2)) + 2 * (size_t)nmax * sizeof(double) +
-         2 * (size_t)nmax * sizeof(int);
+// Shared memory of one warp, contiguous: [matrix area][F][hold][er, ec].
+//  * matrix area: the FP64 matrix (double2, nf x (nf+1)) for the FP64 routine,
+//    aliased by the FP32 path's hi/lo copy (float4, nm x (nm+1));
+//  * F: the FP32 factor (float2, nm x (nm+1)); hold: 2 nf doubles; er, ec:
+//    2 nm ints.
+// nf is the largest n of the plan, nm the largest n that takes the FP32 path
+// (0 in the plain modes and for groups the precision policy sends to FP64),
+// so a group that only runs the FP64 routine costs the plain kernel's bytes.
+struct WarpLayout {
+  size_t area, f, hold, total;
+};
+
+__host__ __device__ inline WarpLayout warp_layout(int nm, int nf) {
+  WarpLayout L;
+  const size_t a_fp64 = (size_t)nf * (nf + 1) * sizeof(double2);
+  const size_t a_fp32 = (size_t)nm * (nm + 1) * sizeof(float4);
+  L.area = a_fp64 > a_fp32 ? a_fp64 : a_fp32;
+  L.f = (size_t)nm * (nm + 1) * sizeof(float2);
+  L.hold = 2 * (size_t)nf * sizeof(double);
+  const size_t ints = 2 * (size_t)nm * sizeof(int);
+  L.total = (L.area + L.f + L.hold + ints + 15) & ~(size_t)15;
+  return L;
 }
 
 template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int lane, float theta2,
-                               unsigned int share64k, DeferredOut &out, double *logabs,
-                               double *phase, int8_t *parity, int32_t *status) {
+                               unsigned int share64k, int status_or, DeferredOut &out,
+                               double *logabs, double *phase, int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
   if (MODE == LUFQHE_MODE_MIXED && route_fp64(src, share64k)) {
@@ -110,30 +129,29 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
       logabs[ob] = la;
       if (phase) phase[ob] = ph;
       if (parity) parity[ob] = (int8_t)par;
-      if (status) status[ob] = st;
+      if (status) status[ob] = st | status_or;
     }
   }
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
-    grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nmax,
+    grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nm,
+                   int nf,
                    float theta2, double *__restrict__ logabs, double *__restrict__ phase,
                    int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const size_t nl = (size_t)nmax * (nmax + 1);
-  unsigned char *base = smem_raw;
-  float4 *HL = reinterpret_cast<float4 *>(base) + warp * nl;
-  base += warps * nl * sizeof(float4);
-  float2 *F = reinterpret_cast<float2 *>(base) + warp * nl;
-  base += warps * nl * sizeof(float2);
-  double *hold = reinterpret_cast<double *>(base) + warp * 2 * nmax;
-  base += warps * 2 * (size_t)nmax * sizeof(double);
-  int *er = reinterpret_cast<int *>(base) + warp * 2 * nmax;
-  int *ec = er + nmax;
+  (void)warps;
+  const WarpLayout L = warp_layout(nm, nf);
+  unsigned char *base = smem_raw + (size_t)warp * L.total;
+  float4 *HL = reinterpret_cast<float4 *>(base);
+  float2 *F = reinterpret_cast<float2 *>(base + L.area);
+  double *hold = reinterpret_cast<double *>(base + L.area + L.f);
+  int *er = reinterpret_cast<int *>(base + L.area + L.f + L.hold);
+  int *ec = er + nm;
 
   DeferredOut out;
   for (;;) {
@@ -146,13 +164,14 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, lane, theta2, w.share64k, out, logabs, phase, parity, status);
+                           ec, lane, theta2, w.share64k, w.status_or, out, logabs, phase, parity,
+                           status);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
 }
 
-using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, float, double *,
+using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, double *,
                                double *, int8_t *, int32_t *);
 
 GroupedKernel kernel_for(int mode) {
@@ -170,10 +189,19 @@ int default_tile(int n) {
   return std::max(1, std::min(256, v));
 }
 
+// One pass of a plan: a grouped kernel over its own work list. A mixed plan
+// runs two passes back to back: the mixed kernel over the groups that take the
+// FP32 path, then the plain fused kernel over the groups the precision policy
+// sends to FP64 (those need neither the FP32 path's shared memory nor its
+// registers, and get the plain kernel's occupancy). A plain plan has one pass.
 struct Launch {
+  int mode = LUFQHE_MODE_MIXED;
+  int nm = 0, nf = 1;  // warp_layout of the pass
   int warps = 4;
-  int ctas = 0;  // grid size
+  int ctas = 0;        // grid size
   size_t smem = 0;
+  int first = 0;       // first work item of the pass in the device list
+  int nitems = 0;
 };
 
 }  // namespace
@@ -185,7 +213,7 @@ using namespace lufqhe;
 struct lufqhe_plan_s {
   std::vector<lufqhe_group_t> groups;
   int mode = LUFQHE_MODE_MIXED;
-  int nmax = 1;
+  int nmax = 1;      // largest n of any group
   long long total = 0;
   double *logabs = nullptr, *phase = nullptr;
   int8_t *parity = nullptr;
@@ -194,7 +222,7 @@ struct lufqhe_plan_s {
   // per-group tile size and FP64 share (1/65536) chosen by the tuner
   std::vector<int> tile;
   std::vector<unsigned int> share;
-  Launch launch;
+  Launch launch[2];
   // device state
   WorkItem *d_items = nullptr;
   unsigned int *d_counter = nullptr;
@@ -208,15 +236,21 @@ struct lufqhe_plan_s {
 
 namespace {
 
+// Pass of group g: 1 for a mixed plan's FP64-only groups, else 0.
+int pass_of(const lufqhe_plan_s *p, size_t g) {
+  return p->mode == LUFQHE_MODE_MIXED && p->share[g] >= 65536u ? 1 : 0;
+}
+
 int build_items(lufqhe_plan_s *p, cudaStream_t s) {
   std::vector<int> order(p->groups.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return p->groups[a].n > p->groups[b].n; });
-  std::vector<WorkItem> items;
+  std::vector<WorkItem> items[2];
   for (int g : order) {
     const lufqhe_group_t &G = p->groups[g];
     const int T = p->tile[g];
+    const int pass = pass_of(p, g);
     for (long long f = 0; f < G.count; f += T) {
       WorkItem w;
       w.A = reinterpret_cast<const double2 *>(G.A);
@@ -225,21 +259,28 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
       w.count = (int)std::min<long long>(T, G.count - f);
       w.n = G.n;
       w.lda = G.lda;
-      w.share64k = p->mode == LUFQHE_MODE_MIXED ? p->share[g] : 0u;
-      items.push_back(w);
+      w.share64k = p->mode == LUFQHE_MODE_MIXED && pass == 0 ? p->share[g] : 0u;
+      w.status_or = pass == 1 ? LUFQHE_ST_FP64 : 0;
+      items[pass].push_back(w);
     }
   }
-  p->nitems = (int)items.size();
-  if (items.size() > p->items_cap) {
+  p->launch[0].first = 0;
+  p->launch[0].nitems = (int)items[0].size();
+  p->launch[1].first = (int)items[0].size();
+  p->launch[1].nitems = (int)items[1].size();
+  items[0].insert(items[0].end(), items[1].begin(), items[1].end());
+  const std::vector<WorkItem> &all = items[0];
+  p->nitems = (int)all.size();
+  if (all.size() > p->items_cap) {
     if (p->d_items) cudaFree(p->d_items);
     p->d_items = nullptr;
-    int rc = check_cuda(cudaMalloc(&p->d_items, sizeof(WorkItem) * std::max<size_t>(1, items.size())),
+    int rc = check_cuda(cudaMalloc(&p->d_items, sizeof(WorkItem) * std::max<size_t>(1, all.size())),
                         "cudaMalloc(work items)");
     if (rc) return rc;
-    p->items_cap = items.size();
+    p->items_cap = all.size();
   }
-  if (!items.empty()) {
-    int rc = check_cuda(cudaMemcpyAsync(p->d_items, items.data(), sizeof(WorkItem) * items.size(),
+  if (!all.empty()) {
+    int rc = check_cuda(cudaMemcpyAsync(p->d_items, all.data(), sizeof(WorkItem) * all.size(),
                                         cudaMemcpyHostToDevice, s),
                         "cudaMemcpyAsync(work items)");
     if (rc) return rc;
@@ -247,14 +288,30 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
   return check_cuda(cudaStreamSynchronize(s), "sync(work items)");
 }
 
-int configure_launch(lufqhe_plan_s *p, int warps) {
-  GroupedKernel k = kernel_for(p->mode);
-  const size_t per_warp = warp_smem_bytes(p->nmax);
+// Set up pass `pass` for its groups: layout, shared memory, grid. A pass
+// without groups is left empty.
+int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
+  Launch &L = p->launch[pass];
+  L.mode = pass == 1 ? LUFQHE_MODE_PLAIN_FP64_FUSED : p->mode;
+  L.nm = 0;
+  L.nf = 0;
+  for (size_t g = 0; g < p->groups.size(); ++g) {
+    const lufqhe_group_t &G = p->groups[g];
+    if (G.count == 0 || pass_of(p, g) != pass) continue;
+    L.nf = std::max(L.nf, G.n);
+    if (L.mode == LUFQHE_MODE_MIXED) L.nm = std::max(L.nm, G.n);
+  }
+  L.warps = warps;
+  L.ctas = 0;
+  L.smem = 0;
+  if (L.nf == 0) return LUFQHE_SUCCESS;
+  GroupedKernel k = kernel_for(L.mode);
+  const size_t per_warp = warp_layout(L.nm, L.nf).total;
   const size_t optin = device_smem_optin();
   int w = std::min<int>(warps, (int)(optin / per_warp));
   if (w < 1) {
     set_error("plan: n=%d needs %zu bytes of shared memory per warp; the device offers %zu",
-              p->nmax, per_warp, optin);
+              L.nf, per_warp, optin);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
   const size_t smem = per_warp * w;
@@ -267,23 +324,33 @@ int configure_launch(lufqhe_plan_s *p, int warps) {
                   "occupancy(grouped)");
   if (rc) return rc;
   if (per_sm < 1) per_sm = 1;
-  p->launch.warps = w;
-  p->launch.smem = smem;
-  p->launch.ctas = device_sm_count() * per_sm;
+  L.warps = w;
+  L.smem = smem;
+  L.ctas = device_sm_count() * per_sm;
   return LUFQHE_SUCCESS;
 }
 
+int configure_launch(lufqhe_plan_s *p, int warps) {
+  int rc = configure_pass(p, 0, warps);
+  if (!rc) rc = configure_pass(p, 1, warps);
+  return rc;
+}
+
 int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
-  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned int), s), "memset(counter)");
-  if (rc) return rc;
-  if (p->nitems == 0) return LUFQHE_SUCCESS;
-  GroupedKernel k = kernel_for(p->mode);
-  const int grid = std::min<long long>(p->launch.ctas, (p->nitems + p->launch.warps - 1) /
-                                                            p->launch.warps + 0LL);
-  k<<<std::max(1, grid), p->launch.warps * 32, p->launch.smem, s>>>(
-      p->d_items, p->nitems, p->d_counter, p->nmax, p->theta2, p->logabs, p->phase, p->parity,
-      p->status);
-  return check_cuda(cudaGetLastError(), "grouped_kernel launch");
+  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(unsigned int), s),
+                      "memset(counter)");
+  for (int pass = 0; pass < 2 && !rc; ++pass) {
+    const Launch &L = p->launch[pass];
+    if (L.nitems == 0 || L.ctas == 0) continue;
+    GroupedKernel k = kernel_for(L.mode);
+    const long long want = (L.nitems + L.warps - 1) / L.warps;
+    const int grid = (int)std::min<long long>(L.ctas, want);
+    k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
+                                                       p->d_counter + pass, L.nm, L.nf, p->theta2,
+                                                       p->logabs, p->phase, p->parity, p->status);
+    rc = check_cuda(cudaGetLastError(), "grouped_kernel launch");
+  }
+  return rc;
 }
 
 // Time one launch (ms) after one warm-up launch.
@@ -318,8 +385,6 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
     if (all[g].count == 0) continue;
     p->groups.assign(1, all[g]);
     p->nmax = all[g].n;
-    rc = configure_launch(p, 4);
-    if (rc) return rc;
     float best = 1e30f;
     int best_t = base_tile[g];
     unsigned int best_s = base_share[g];
@@ -334,6 +399,8 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
         int T = std::max(1, std::min(1024, (int)std::lround(base_tile[g] * f)));
         p->tile.assign(1, T);
         p->share.assign(1, sh);
+        rc = configure_launch(p, 4);
+        if (rc) return rc;
         rc = build_items(p, s);
         if (rc) return rc;
         float ms = 0.0f;
@@ -366,7 +433,7 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   for (int w : {2, 4, 8}) {
     rc = configure_launch(p, w);
     if (rc) return rc;
-    if (p->launch.warps != w) continue;  // does not fit
+    if (p->launch[0].warps != w && p->launch[1].warps != w) continue;  // does not fit
     float ms = 0.0f;
     rc = time_launch(p, s, &ms);
     if (rc) return rc;
@@ -380,8 +447,8 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   }
   rc = configure_launch(p, best_w);
   if (rc) return rc;
-  snprintf(line, sizeof(line), "}, \"chosen_warps\": %d, \"ctas\": %d}", p->launch.warps,
-           p->launch.ctas);
+  snprintf(line, sizeof(line), "}, \"chosen_warps\": %d, \"ctas\": %d, \"fp64_pass_ctas\": %d}",
+           p->launch[0].warps, p->launch[0].ctas, p->launch[1].ctas);
   p->report += line;
   return LUFQHE_SUCCESS;
 }
@@ -464,7 +531,8 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   cudaStream_t s = (cudaStream_t)stream;
   int rc = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking),
                       "cudaStreamCreate(plan)");
-  if (!rc) rc = check_cuda(cudaMalloc(&p->d_counter, sizeof(unsigned int)), "cudaMalloc(counter)");
+  if (!rc)
+    rc = check_cuda(cudaMalloc(&p->d_counter, 2 * sizeof(unsigned int)), "cudaMalloc(counter)");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sync(plan inputs)");
   if (!rc && (flags & LUFQHE_PLAN_AUTOTUNE) && p->total > 0) rc = autotune(p, p->cap_stream);
   if (!rc) rc = build_items(p, p->cap_stream);
@@ -472,7 +540,7 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
     rc = configure_launch(p, 4);
     char line[160];
     snprintf(line, sizeof(line), "{\"tiles\": \"default\", \"chosen_warps\": %d, \"ctas\": %d}",
-             p->launch.warps, p->launch.ctas);
+             p->launch[0].warps, p->launch[0].ctas);
     p->report = line;
   }
   if (!rc) rc = capture_graph(p);
