@@ -538,14 +538,14 @@ struct TileGeom {
   static constexpr int SB = (N + 7) / 8;  // column slots per lane
 };
 
-// Float-float residual for the row slots [A0, A1) of the 4 x 8 lane grid:
+// Float-float residual for the NA row slots from a0 of the 4 x 8 lane grid:
 // lane (r, c) owns entries (4a + r, 8b + c); R is written into the float2
-// view of HL (row stride N + 1).
-template <int N, int A0, int A1>
-__device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int lane) {
+// view of HL (row stride N + 1). a0 is a run-time value so that both halves
+// of the row slots can share one copy of this (large, unrolled) code.
+template <int N, int NA>
+__device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int lane, int A0) {
   constexpr int LDS = N + 1;
   constexpr int SB = TileGeom<N>::SB;
-  constexpr int NA = A1 - A0;
   if constexpr (NA > 0) {
     const int tr = lane >> 3, tc = lane & 7;
     float4 acc[NA][SB];
@@ -556,8 +556,8 @@ __device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int l
         const int i = 4 * (A0 + a) + tr, k = 8 * b + tc;
         acc[a][b] = (i < N && k < N) ? HL[i * LDS + k] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-    // rows of this pass end at 4 * A1; steps beyond their last row add nothing
-    constexpr int TEND = (4 * A1 < N) ? 4 * A1 : N;
+    // rows of this pass end at 4 (A0 + NA); steps beyond their last row add nothing
+    const int TEND = min(4 * (A0 + NA), N);
 #pragma unroll 1
     for (int t = 0; t < TEND; ++t) {
       float2 Lv[NA], Uv[SB];
@@ -927,8 +927,13 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
   //    passes over halves of the row slots (half the accumulator registers).
   //    R overwrites the front of HL as a float2 array; pass 1 writes rows
   //    below the ones pass 2 still reads, so the passes never collide.
-  residual_rows<N, 0, SA / 2>(HL, F, lane);
-  residual_rows<N, SA / 2, SA>(HL, F, lane);
+  if constexpr (SA % 2 == 0) {
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) residual_rows<N, SA / 2>(HL, F, lane, h * (SA / 2));
+  } else {
+    residual_rows<N, SA / 2>(HL, F, lane, 0);
+    residual_rows<N, SA - SA / 2>(HL, F, lane, SA / 2);
+  }
   float2 *Rm = reinterpret_cast<float2 *>(HL);  // R, then E, row stride LDS
 
   // 5-6. solves, acceptance, log det(I + E) and the diagonal product
