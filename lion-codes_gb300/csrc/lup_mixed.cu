@@ -14,7 +14,9 @@
 //     is an FP32 one;
 //  4. E = U^-1 L^-1 R by FP32 triangular solves;
 //  5. log det(I + E) by an unpivoted FP32 LU that keeps the identity implicit
-//     (only the small offsets are stored), log1p/atan2 of each pivot;
+//     (only the small offsets are stored), log1p/atan2 of each pivot, or, for
+//     the register-tiled sizes when ||E|| is small enough that the dropped
+//     terms stay below 1e-12 max(1, |log|det||), by tr E - tr(E^2)/2;
 //  6. log|det| = log|prod u_jj| (complex float-float product, one FP64 log
 //     and atan2 per matrix, deferred and done for 32 matrices at once by the
 //     32 lanes) + equilibration + Re log det(I+E); phase likewise.
@@ -31,9 +33,13 @@
 // (and the FP64 kernel's smaller shared-memory footprint): the FP32 pass
 // appends the index of a rejected matrix to a pending list in static device
 // memory, and the second kernel's warps claim the list's entries one at a
-// time. A matrix that finds the list full is refactorised where it is. For
-// n < 24 the FP64 refactorisations are cheap and rare enough that the second
-// launch costs more than it saves; there the FP32 pass does them in place.
+// time. If the list is full, the n >= 24 kernels (which hold no FP64
+// factorisation code) mark the matrix in logabs and the second kernel scans
+// for the marks; the others refactorise it in place. For n < 24 the FP64
+// refactorisations are cheap and rare enough that the second launch costs
+// more than it saves; there the FP32 pass does them in place. The kernels
+// take their matrices from a source: dense matrices in the reference layout,
+// or lowest-Landau-level orbital matrices built from particle coordinates.
 
 #include <atomic>
 #include <cmath>
