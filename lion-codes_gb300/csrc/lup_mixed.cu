@@ -57,9 +57,9 @@ float g_fp64_share = -1.0f;  // < 0: per-n default
 unsigned int fp64_share_64k(int n) {
   float s = g_fp64_share;
   if (s < 0.0f) {
-    // n <= 24: the FP32 path alone is fastest; n >= 25: the FP64 kernel
-    // beats the FP32 path outright
-    s = n <= 24 ? 0.0f : 1.0f;
+    // n <= 24 and n = 32 (a register-tiled size): the FP32 path is fastest;
+    // other n > 24 run the generic mixed kernel, which the FP64 kernel beats
+    s = (n <= 24 || n == 32) ? 0.0f : 1.0f;
   }
   if (s <= 0.0f) return 0u;
   if (s >= 1.0f) return 65536u;

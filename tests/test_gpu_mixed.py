@@ -134,15 +134,15 @@ def test_singular_and_nonfinite(cuda, lufqhe_mod):
     assert out["status"][2] == 0 and abs(out["logabs"][2]) < 1e-14
 
 
-@pytest.mark.parametrize("n", [8, 24, 32])
+@pytest.mark.parametrize("n", [8, 24, 28, 32, 48])
 def test_default_precision_policy(cuda, lufqhe_mod, oracle, fp64_share, n):
-    """Per-size defaults: n <= 24 all through the FP32 path, n >= 25 all
-    FP64; accuracy holds whatever the route."""
+    """Per-size defaults: n <= 24 and n = 32 all through the FP32 path, other
+    n > 24 (here 28, 48) all FP64; accuracy holds whatever the route."""
     fp64_share(-1.0)
     A, _ = lufqhe_mod.gen_lll(1024, n, seed=90 + n)
     out = check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.3)
     routed = ((out["status"] & lufqhe_mod.ST_FP64) != 0).mean()
-    want = {8: 0.0, 24: 0.0, 32: 1.0}[n]
+    want = {8: 0.0, 24: 0.0, 28: 1.0, 32: 0.0, 48: 1.0}[n]
     assert abs(routed - want) < 0.06
 
 
