@@ -196,3 +196,26 @@ def test_fp64_pass_list_overflow(cuda, lufqhe_mod, threshold, fp64_share, share)
     assert ((out["status"] & ~flags) == fused["status"]).all()
     del A
     cuda.cuda.empty_cache()
+
+
+def test_concurrent_calls_on_two_streams(cuda, lufqhe_mod):
+    """Mixed calls in flight together on two streams (n = 24, with FP64
+    refactorisations, and n = 32) each take their own work counters and
+    pending lists and give the results of calls made one at a time."""
+    A1, _ = lufqhe_mod.gen_lll(6000, 24, seed=31)
+    A2, _ = lufqhe_mod.gen_lll(3000, 32, seed=32)
+    A3, _ = lufqhe_mod.gen_lll(5000, 24, seed=33)
+    want = [host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED)) for A in (A1, A2, A3)]
+    cuda.cuda.synchronize()
+    s1, s2 = cuda.cuda.Stream(), cuda.cuda.Stream()
+    outs = []
+    for rep in range(3):
+        outs.append(lufqhe_mod.batch_lup_det(A1, mode=lufqhe_mod.MODE_MIXED, stream=s1))
+        outs.append(lufqhe_mod.batch_lup_det(A2, mode=lufqhe_mod.MODE_MIXED, stream=s2))
+        outs.append(lufqhe_mod.batch_lup_det(A3, mode=lufqhe_mod.MODE_MIXED, stream=s2 if rep % 2 else s1))
+    cuda.cuda.synchronize()
+    assert ((want[0]["status"] & lufqhe_mod.ST_FALLBACK) != 0).sum() > 100
+    for i, o in enumerate(outs):
+        got, w = host(o), want[i % 3]
+        assert np.array_equal(got["logabs"], w["logabs"], equal_nan=True)
+        assert (got["status"] == w["status"]).all() and (got["parity"] == w["parity"]).all()
