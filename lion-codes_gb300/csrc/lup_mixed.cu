@@ -95,10 +95,13 @@ __device__ __forceinline__ long long claim_matrix(int slot, int lane) {
   return (long long)__shfl_sync(kFull, b, 0);
 }
 
-// Pending lists of the FP64 pass: one per launch in flight, taken in turn
-// (a slot is busy from the FP32 pass to the end of the FP64 pass).
-constexpr int kPendSlots = 32;
-constexpr unsigned int kPendCap = 1u << 17;
+// Pending lists of the FP64 pass, taken in turn by the calls: 256 lists of
+// 16384 entries (16 MiB). A list is busy only from a call's FP32 pass to the
+// end of its FP64 pass, so 256 calls would have to be in flight at once for
+// two to share one; a call with more rejections than a list holds marks the
+// rest in logabs for the FP64 pass's scan.
+constexpr int kPendSlots = 256;
+constexpr unsigned int kPendCap = 1u << 14;
 __device__ unsigned int g_pend[kPendSlots][kPendCap];
 __device__ unsigned int g_pend_count[kPendSlots];
 __device__ unsigned int g_pend_over[kPendSlots];  // some matrix found the list full

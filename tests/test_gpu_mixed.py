@@ -179,11 +179,11 @@ def test_mixed_deterministic_across_batch_positions(cuda, lufqhe_mod):
 @pytest.mark.parametrize("share", [0.0, 0.5])
 def test_fp64_pass_list_overflow(cuda, lufqhe_mod, threshold, fp64_share, share):
     """n = 24 hands every FP64 factorisation to the second pass through a list
-    of 131072 entries per call; with every matrix rejected (threshold 0) a batch
+    of 16384 entries per call; with every matrix rejected (threshold 0) a batch
     just past that size overflows it, and the marked rest must be found too."""
     threshold(0.0)
     fp64_share(share)
-    batch = 131072 + 1028
+    batch = 16384 + 1028
     A, _ = lufqhe_mod.gen_lll(batch, 24, seed=13)
     out = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
     fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
