@@ -36,6 +36,25 @@ struct BlockWalk {
   }
 };
 
+// The same walk for any step (threads of a warp group).
+struct StrideWalk {
+  int i, k, di, dk;
+  __device__ __forceinline__ StrideWalk(int start, int step, int m) {
+    i = start / m;
+    k = start - i * m;
+    di = step / m;
+    dk = step - di * m;
+  }
+  __device__ __forceinline__ void next(int m) {
+    k += dk;
+    i += di;
+    if (k >= m) {
+      k -= m;
+      ++i;
+    }
+  }
+};
+
 // Coalesced load of an n x n complex128 matrix (row stride lda) into shared
 // memory (row stride lds). Returns true (warp-uniform) if any entry is NaN/Inf.
 // COHERENT loads through L2 only (no read-only / L1 path), for matrices that
@@ -96,6 +115,20 @@ struct DenseSource {
   __device__ __forceinline__ double2 first(long long b, int n) const {
     return __ldg(A + (size_t)b * n * lda);
   }
+  // all threads of the CTA; true (CTA-uniform) if an entry is NaN/Inf
+  __device__ __forceinline__ bool load_group(long long b, int n, double2 *M, int lds, int tid,
+                                             int nthr) const {
+    const double2 *src = A + (size_t)b * n * lda;
+    bool bad = false;
+    StrideWalk w(tid, nthr, n);
+    for (int e = tid; e < n * n; e += nthr) {
+      const double2 v = __ldg(src + (size_t)w.i * lda + w.k);
+      bad |= !finite_c(v);
+      M[w.i * lds + w.k] = v;
+      w.next(n);
+    }
+    return __syncthreads_or(bad);
+  }
 };
 
 struct LllSource {
@@ -115,6 +148,12 @@ struct LllSource {
     const double2 z = __ldg(Z + (size_t)b * n);
     const double w = exp(__dmul_rn(-__dadd_rn(__dmul_rn(z.x, z.x), __dmul_rn(z.y, z.y)), 0.25));
     return make_double2(__dmul_rn(1.0, w), __dmul_rn(0.0, w));
+  }
+  __device__ __forceinline__ bool load_group(long long b, int n, double2 *M, int lds, int tid,
+                                             int nthr) const {
+    bool bad = false;
+    for (int i = tid; i < n; i += nthr) bad |= !lll_row_rn(__ldg(Z + (size_t)b * n + i), n, M + i * lds);
+    return __syncthreads_or(bad);
   }
 };
 
@@ -272,6 +311,156 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
       w.next(m);
     }
     __syncwarp();
+  }
+  *parity = par;
+  return 0;
+}
+
+// The same factorisation by all threads of a CTA (a warp group), for n > 32
+// where one warp per matrix leaves too few warps on an SM to keep the FP64
+// pipe busy. Every pivot decision is taken on the same candidate keys with
+// the same rule (ties to the larger row) and every entry sees the same
+// operations in the same order as in lup_fp64_warp, so the factors, pivots
+// and parity are bit-identical to it. `red` is 3 x (warps) words of shared
+// scratch for the cross-warp reductions. CTA-uniform return value.
+template <int ARITH>
+__device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid, int nthr,
+                              long long *red, int *parity) {
+  const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+  long long *red_k = red;
+  int *red_i = reinterpret_cast<int *>(red + nw);
+  unsigned *red_n = reinterpret_cast<unsigned *>(red_i + nw);
+  int par = 0;
+  double *rhold = hold + n;
+  {
+    bool tiny = false;
+    const long long tiny_bits = __double_as_longlong(1e-24);
+    for (int i = tid; i < n; i += nthr) {
+      long long big = 0;
+      for (int k = 0; k < n; ++k) big = max(big, abs_bits(M[i * lds + k].x));
+      const double h = __longlong_as_double(big);
+      hold[i] = h;
+      rhold[i] = __drcp_rn(h);
+      tiny |= big < tiny_bits;
+    }
+    if (__syncthreads_or(tiny)) {
+      *parity = 0;
+      return LUFQHE_ST_SCALE_TINY;
+    }
+  }
+  // argmax over the CTA of (key, row), ties to the larger row
+  auto argmax = [&](long long &bk, int &bi) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      long long ok = __shfl_xor_sync(kFull, bk, off);
+      int oi = __shfl_xor_sync(kFull, bi, off);
+      if (ok > bk || (ok == bk && oi > bi)) {
+        bk = ok;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      red_k[warp] = bk;
+      red_i[warp] = bi;
+    }
+    __syncthreads();
+    bk = red_k[0];
+    bi = red_i[0];
+    for (int q = 1; q < nw; ++q) {
+      if (red_k[q] > bk || (red_k[q] == bk && red_i[q] > bi)) {
+        bk = red_k[q];
+        bi = red_i[q];
+      }
+    }
+    __syncthreads();
+  };
+  const long long safe_lo = 0x0170000000000000ll;  // 2^-1000
+  const long long safe_hi = 0x7e70000000000000ll;  // 2^+1000
+  for (int j = 0; j < n; ++j) {
+    long long bk = -1;
+    int bi = j;
+    for (int i = j + tid; i < n; i += nthr) {
+      double a = __dmul_rn(fabs(M[i * lds + j].x), rhold[i]);
+      long long key = (a == a) ? __double_as_longlong(a) : -2ll;
+      if (key >= bk) {
+        bk = key;
+        bi = i;
+      }
+    }
+    argmax(bk, bi);
+    unsigned near = 0;
+    for (int i = j + tid; i < n; i += nthr) {
+      double a = __dmul_rn(fabs(M[i * lds + j].x), rhold[i]);
+      long long key = (a == a) ? __double_as_longlong(a) : -2ll;
+      near += key >= bk - 16;
+    }
+    near = __reduce_add_sync(kFull, near);
+    if (lane == 0) red_n[warp] = near;
+    __syncthreads();
+    near = 0;
+    for (int q = 0; q < nw; ++q) near += red_n[q];
+    __syncthreads();
+    if (near != 1 || bk < safe_lo || bk > safe_hi) {
+      bk = -1;
+      bi = j;
+      for (int i = j + tid; i < n; i += nthr) {
+        double q = __ddiv_rn(fabs(M[i * lds + j].x), hold[i]);
+        long long key = (q == q) ? __double_as_longlong(q) : -2ll;
+        if (key >= bk) {
+          bk = key;
+          bi = i;
+        }
+      }
+      argmax(bk, bi);
+    }
+    const int p = bi;
+    if (p != j) {
+      for (int k = tid; k < n; k += nthr) {
+        double2 t = M[p * lds + k];
+        M[p * lds + k] = M[j * lds + k];
+        M[j * lds + k] = t;
+      }
+      if (tid == 0) {
+        hold[p] = hold[j];
+        rhold[p] = rhold[j];
+      }
+      par ^= 1;
+    }
+    __syncthreads();
+    const double2 piv = M[j * lds + j];
+    if (is_zero_c(piv)) {
+      *parity = par;
+      return LUFQHE_ST_SINGULAR;
+    }
+    if (j == n - 1) break;
+    if (ARITH == ARITH_REF) {
+      const double den = pivot_den<ARITH_REF>(piv);
+      const double y = __drcp_rn(den);
+      const long long db = abs_bits(den);
+      const bool den_safe = db >= 0x03f0000000000000ll && db <= 0x7bf0000000000000ll;
+      for (int i = j + 1 + tid; i < n; i += nthr) {
+        const double2 a = M[i * lds + j];
+        const double nx = __dadd_rn(__dmul_rn(a.x, piv.x), __dmul_rn(a.y, piv.y));
+        const double ny = __dsub_rn(__dmul_rn(a.y, piv.x), __dmul_rn(a.x, piv.y));
+        M[i * lds + j] = make_double2(div_rn_markstein(nx, den, y, den_safe),
+                                      div_rn_markstein(ny, den, y, den_safe));
+      }
+    } else {
+      const double d = pivot_den<ARITH>(piv);
+      for (int i = j + 1 + tid; i < n; i += nthr)
+        M[i * lds + j] = cdiv_pivot<ARITH>(M[i * lds + j], piv, d);
+    }
+    __syncthreads();
+    const int m = n - 1 - j;
+    const int mm = m * m;
+    const int j1 = j + 1;
+    StrideWalk w(tid, nthr, m);
+    for (int e = tid; e < mm; e += nthr) {
+      const int ii = j1 + w.i, kk = j1 + w.k;
+      M[ii * lds + kk] = cmsub<ARITH>(M[ii * lds + kk], M[ii * lds + j], M[j * lds + kk]);
+      w.next(m);
+    }
+    __syncthreads();
   }
   *parity = par;
   return 0;

@@ -100,6 +100,61 @@ __global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
 
 }  // namespace
 
+// n > 32: one matrix per CTA of kGroupWarps warps (lup_fp64_group). With one
+// warp per matrix an SM holds only the 3-4 matrices its shared memory fits
+// (n=64: 66 KB each), too few warps to cover the FP64 pipe's latency.
+constexpr int kGroupWarps = 4;
+constexpr int kGroupMinN = 33;
+
+template <int ARITH, class Src>
+__global__ void __launch_bounds__(kGroupWarps * 32)
+    lup_plain_group_kernel(Src src, double2 *__restrict__ Aout, int n, int lda, long long batch,
+                           double *__restrict__ logabs, double *__restrict__ phase,
+                           int8_t *__restrict__ parity, int32_t *__restrict__ status,
+                           int status_or) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long red[3 * kGroupWarps];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lds = n + 1;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw);
+  double *hold = reinterpret_cast<double *>(M + (size_t)n * lds);
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    __syncthreads();
+    int par = 0;
+    int st = src.load_group(b, n, M, lds, tid, nthr) ? LUFQHE_ST_NONFINITE : 0;
+    if (!st) st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par);
+    __syncthreads();
+    if (Aout && (st == 0 || st == LUFQHE_ST_SINGULAR)) {
+      double2 *dst = Aout + (size_t)b * n * lda;
+      StrideWalk w(tid, nthr, n);
+      for (int e = tid; e < n * n; e += nthr) {
+        dst[(size_t)w.i * lda + w.k] = M[w.i * lds + w.k];
+        w.next(n);
+      }
+    }
+    if (tid < 32) {
+      // warp 0, with the warp routine's own summation order
+      double la, ph;
+      if (st == 0) {
+        logdet_from_diag(M, lds, n, tid, par, &la, &ph);
+      } else if (st == LUFQHE_ST_SINGULAR) {
+        la = -INFINITY;
+        ph = 0.0;
+      } else {
+        la = NAN;
+        ph = NAN;
+        par = 0;
+      }
+      if (tid == 0) {
+        logabs[b] = la;
+        if (phase) phase[b] = ph;
+        if (parity) parity[b] = (int8_t)par;
+        if (status) status[b] = st | status_or;
+      }
+    }
+  }
+}
+
 size_t plain_smem_per_warp(int n) {
   return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
 }
@@ -109,6 +164,29 @@ int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, in
                      double *logabs, double *phase, int8_t *parity, int32_t *status,
                      cudaStream_t stream, int status_or) {
   if (batch == 0) return LUFQHE_SUCCESS;
+  if (n >= kGroupMinN) {
+    const size_t smem = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
+    auto kern = arith == ARITH_REF ? lup_plain_group_kernel<ARITH_REF, Src>
+                                   : lup_plain_group_kernel<ARITH_FUSED, Src>;
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem),
+                        "cudaFuncSetAttribute(plain group)");
+    if (rc) return rc;
+    int per_sm = 0;
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kGroupWarps * 32,
+                                                                  smem),
+                    "occupancy(plain group)");
+    if (rc) return rc;
+    if (per_sm < 1) {
+      set_error("n=%d needs %zu bytes of shared memory per matrix", n, smem);
+      return LUFQHE_ERR_UNSUPPORTED_N;
+    }
+    const long long cap = (long long)device_sm_count() * per_sm;
+    const int grid = (int)(batch < cap ? batch : cap);
+    kern<<<grid, kGroupWarps * 32, smem, stream>>>(src, Aout, n, lda, batch, logabs, phase, parity,
+                                                   status, status_or);
+    return check_cuda(cudaGetLastError(), "lup_plain_group_kernel launch");
+  }
   const size_t per_warp = plain_smem_per_warp(n);
   const size_t optin = device_smem_optin();
   int warps = (int)(optin / per_warp);
