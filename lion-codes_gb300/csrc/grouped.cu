@@ -189,11 +189,77 @@ int default_tile(int n) {
   return std::max(1, std::min(256, v));
 }
 
-// One pass of a plan: a grouped kernel over its own work list. A mixed plan
-// runs two passes back to back: the mixed kernel over the groups that take the
-// FP32 path, then the plain fused kernel over the groups the precision policy
-// sends to FP64 (those need neither the FP32 path's shared memory nor its
-// registers, and get the plain kernel's occupancy). A plain plan has one pass.
+// Warp-group form of the grouped kernel for the FP64 route at n > 32: each CTA
+// claims work items and factorises their matrices with all its threads
+// (lup_fp64_group), as the batched plain kernel does for those sizes.
+template <int ARITH>
+__global__ void __launch_bounds__(kFp64GroupWarps * 32)
+    grouped_group_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter,
+                         int nm, int nf, float theta2, double *__restrict__ logabs,
+                         double *__restrict__ phase, int8_t *__restrict__ parity,
+                         int32_t *__restrict__ status) {
+  (void)nm;
+  (void)theta2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long red[3 * kFp64GroupWarps];
+  __shared__ unsigned int item;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw);
+  double *hold = reinterpret_cast<double *>(M + (size_t)nf * (nf + 1));
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const unsigned int it = item;
+    if (it >= (unsigned int)nitems) break;
+    const WorkItem w = items[it];
+    const int n = w.n, lds = n + 1;
+    const DenseSource src{w.A, w.lda};
+    for (int j = 0; j < w.count; ++j) {
+      __syncthreads();
+      const long long ob = w.out + j;
+      int par = 0;
+      int st = src.load_group(w.first + j, n, M, lds, tid, nthr) ? LUFQHE_ST_NONFINITE : 0;
+      if (!st) st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par);
+      __syncthreads();
+      if (tid < 32) {
+        double la, ph;
+        if (st == 0) {
+          logdet_from_diag(M, lds, n, tid, par, &la, &ph);
+        } else if (st == LUFQHE_ST_SINGULAR) {
+          la = -INFINITY;
+          ph = 0.0;
+        } else {
+          la = NAN;
+          ph = NAN;
+          par = 0;
+        }
+        if (tid == 0) {
+          logabs[ob] = la;
+          if (phase) phase[ob] = ph;
+          if (parity) parity[ob] = (int8_t)par;
+          if (status) status[ob] = st | w.status_or;
+        }
+      }
+    }
+  }
+}
+
+GroupedKernel group_kernel_for(int mode) {
+  return mode == LUFQHE_MODE_PLAIN_FP64 ? grouped_group_kernel<ARITH_REF>
+                                        : grouped_group_kernel<ARITH_FUSED>;
+}
+
+// One pass of a plan: a grouped kernel over its own work list. A plan runs up
+// to three passes back to back:
+//  0. the plan's mode over the groups on the warp-per-matrix path (a mixed
+//     plan's FP32-path groups; a plain plan's groups with n <= 32);
+//  1. (mixed plans) the plain fused kernel over the groups with n <= 32 that
+//     the precision policy sends to FP64;
+//  2. the warp-group kernel over the FP64-route groups with n > 32 (fused
+//     arithmetic for a mixed plan, the plan's arithmetic for a plain one).
+// Groups routed to FP64 need neither the FP32 path's shared memory nor its
+// registers, and get the plain kernels' occupancy.
 struct Launch {
   int mode = LUFQHE_MODE_MIXED;
   int nm = 0, nf = 1;  // warp_layout of the pass
@@ -222,7 +288,7 @@ struct lufqhe_plan_s {
   // per-group tile size and FP64 share (1/65536) chosen by the tuner
   std::vector<int> tile;
   std::vector<unsigned int> share;
-  Launch launch[2];
+  Launch launch[3];
   // device state
   WorkItem *d_items = nullptr;
   unsigned int *d_counter = nullptr;
@@ -236,9 +302,12 @@ struct lufqhe_plan_s {
 
 namespace {
 
-// Pass of group g: 1 for a mixed plan's FP64-only groups, else 0.
+// Pass of group g: 2 for an FP64-route group with n >= kFp64GroupMinN, 1 for
+// a mixed plan's other FP64-only groups, else 0.
 int pass_of(const lufqhe_plan_s *p, size_t g) {
-  return p->mode == LUFQHE_MODE_MIXED && p->share[g] >= 65536u ? 1 : 0;
+  const bool fp64 = p->mode != LUFQHE_MODE_MIXED || p->share[g] >= 65536u;
+  if (fp64 && p->groups[g].n >= kFp64GroupMinN) return 2;
+  return p->mode == LUFQHE_MODE_MIXED && fp64 ? 1 : 0;
 }
 
 int build_items(lufqhe_plan_s *p, cudaStream_t s) {
@@ -246,7 +315,7 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return p->groups[a].n > p->groups[b].n; });
-  std::vector<WorkItem> items[2];
+  std::vector<WorkItem> items[3];
   for (int g : order) {
     const lufqhe_group_t &G = p->groups[g];
     const int T = p->tile[g];
@@ -260,16 +329,16 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
       w.n = G.n;
       w.lda = G.lda;
       w.share64k = p->mode == LUFQHE_MODE_MIXED && pass == 0 ? p->share[g] : 0u;
-      w.status_or = pass == 1 ? LUFQHE_ST_FP64 : 0;
+      w.status_or = p->mode == LUFQHE_MODE_MIXED && pass > 0 ? LUFQHE_ST_FP64 : 0;
       items[pass].push_back(w);
     }
   }
-  p->launch[0].first = 0;
-  p->launch[0].nitems = (int)items[0].size();
-  p->launch[1].first = (int)items[0].size();
-  p->launch[1].nitems = (int)items[1].size();
-  items[0].insert(items[0].end(), items[1].begin(), items[1].end());
-  const std::vector<WorkItem> &all = items[0];
+  std::vector<WorkItem> all;
+  for (int q = 0; q < 3; ++q) {
+    p->launch[q].first = (int)all.size();
+    p->launch[q].nitems = (int)items[q].size();
+    all.insert(all.end(), items[q].begin(), items[q].end());
+  }
   p->nitems = (int)all.size();
   if (all.size() > p->items_cap) {
     if (p->d_items) cudaFree(p->d_items);
@@ -292,7 +361,7 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
 // without groups is left empty.
 int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
   Launch &L = p->launch[pass];
-  L.mode = pass == 1 ? LUFQHE_MODE_PLAIN_FP64_FUSED : p->mode;
+  L.mode = pass > 0 && p->mode == LUFQHE_MODE_MIXED ? LUFQHE_MODE_PLAIN_FP64_FUSED : p->mode;
   L.nm = 0;
   L.nf = 0;
   for (size_t g = 0; g < p->groups.size(); ++g) {
@@ -305,6 +374,29 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
   L.ctas = 0;
   L.smem = 0;
   if (L.nf == 0) return LUFQHE_SUCCESS;
+  if (pass == 2) {
+    // one matrix per CTA of kFp64GroupWarps warps
+    GroupedKernel k = group_kernel_for(L.mode);
+    const size_t smem =
+        (size_t)L.nf * (L.nf + 1) * sizeof(double2) + 2 * (size_t)L.nf * sizeof(double);
+    int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem),
+                        "cudaFuncSetAttribute(grouped group)");
+    if (rc) return rc;
+    int per_sm = 0;
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k,
+                                                                  kFp64GroupWarps * 32, smem),
+                    "occupancy(grouped group)");
+    if (rc) return rc;
+    if (per_sm < 1) {
+      set_error("plan: n=%d needs %zu bytes of shared memory per matrix", L.nf, smem);
+      return LUFQHE_ERR_UNSUPPORTED_N;
+    }
+    L.warps = kFp64GroupWarps;
+    L.smem = smem;
+    L.ctas = device_sm_count() * per_sm;
+    return LUFQHE_SUCCESS;
+  }
   GroupedKernel k = kernel_for(L.mode);
   const size_t per_warp = warp_layout(L.nm, L.nf).total;
   const size_t optin = device_smem_optin();
@@ -331,19 +423,20 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
 }
 
 int configure_launch(lufqhe_plan_s *p, int warps) {
-  int rc = configure_pass(p, 0, warps);
-  if (!rc) rc = configure_pass(p, 1, warps);
+  int rc = 0;
+  for (int pass = 0; pass < 3 && !rc; ++pass) rc = configure_pass(p, pass, warps);
   return rc;
 }
 
 int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
-  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(unsigned int), s),
+  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 3 * sizeof(unsigned int), s),
                       "memset(counter)");
-  for (int pass = 0; pass < 2 && !rc; ++pass) {
+  for (int pass = 0; pass < 3 && !rc; ++pass) {
     const Launch &L = p->launch[pass];
     if (L.nitems == 0 || L.ctas == 0) continue;
-    GroupedKernel k = kernel_for(L.mode);
-    const long long want = (L.nitems + L.warps - 1) / L.warps;
+    GroupedKernel k = pass == 2 ? group_kernel_for(L.mode) : kernel_for(L.mode);
+    // a warp-group CTA takes one item at a time
+    const long long want = pass == 2 ? L.nitems : (L.nitems + L.warps - 1) / L.warps;
     const int grid = (int)std::min<long long>(L.ctas, want);
     k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
@@ -447,8 +540,10 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   }
   rc = configure_launch(p, best_w);
   if (rc) return rc;
-  snprintf(line, sizeof(line), "}, \"chosen_warps\": %d, \"ctas\": %d, \"fp64_pass_ctas\": %d}",
-           p->launch[0].warps, p->launch[0].ctas, p->launch[1].ctas);
+  snprintf(line, sizeof(line),
+           "}, \"chosen_warps\": %d, \"ctas\": %d, \"fp64_pass_ctas\": %d, "
+           "\"group_pass_ctas\": %d}",
+           p->launch[0].warps, p->launch[0].ctas, p->launch[1].ctas, p->launch[2].ctas);
   p->report += line;
   return LUFQHE_SUCCESS;
 }
@@ -532,7 +627,7 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   int rc = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking),
                       "cudaStreamCreate(plan)");
   if (!rc)
-    rc = check_cuda(cudaMalloc(&p->d_counter, 2 * sizeof(unsigned int)), "cudaMalloc(counter)");
+    rc = check_cuda(cudaMalloc(&p->d_counter, 3 * sizeof(unsigned int)), "cudaMalloc(counter)");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sync(plan inputs)");
   if (!rc && (flags & LUFQHE_PLAN_AUTOTUNE) && p->total > 0) rc = autotune(p, p->cap_stream);
   if (!rc) rc = build_items(p, p->cap_stream);

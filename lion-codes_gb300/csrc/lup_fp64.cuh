@@ -316,6 +316,10 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
   return 0;
 }
 
+// Warps of the CTA that factorises one matrix for n >= kFp64GroupMinN.
+constexpr int kFp64GroupWarps = 4;
+constexpr int kFp64GroupMinN = 33;
+
 // The same factorisation by all threads of a CTA (a warp group), for n > 32
 // where one warp per matrix leaves too few warps on an SM to keep the FP64
 // pipe busy. Every pivot decision is taken on the same candidate keys with

@@ -103,8 +103,8 @@ __global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
 // n > 32: one matrix per CTA of kGroupWarps warps (lup_fp64_group). With one
 // warp per matrix an SM holds only the 3-4 matrices its shared memory fits
 // (n=64: 66 KB each), too few warps to cover the FP64 pipe's latency.
-constexpr int kGroupWarps = 4;
-constexpr int kGroupMinN = 33;
+constexpr int kGroupWarps = kFp64GroupWarps;
+constexpr int kGroupMinN = kFp64GroupMinN;
 
 template <int ARITH, class Src>
 __global__ void __launch_bounds__(kGroupWarps * 32)

@@ -98,3 +98,28 @@ def test_plan_empty_and_invalid(cuda, lufqhe_mod):
     A = lufqhe_mod.gen_gaussian(4, 16, seed=1)
     with pytest.raises(RuntimeError):
         lufqhe_mod.Plan([(A, 0)], out, mode=7)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_plan_large_sizes(cuda, lufqhe_mod, mode):
+    """Sizes above 32 only (the warp-group pass), with a size-33 edge group, in
+    one plan: results equal the batched calls bit for bit."""
+    sizes, counts = (33, 40, 64), (29, 11, 7)
+    groups, off = [], 0
+    for n, c in zip(sizes, counts):
+        A, _ = lufqhe_mod.gen_lll(c, n, seed=700 + n, sigma=math.sqrt(n))
+        groups.append((A, off))
+        off += c
+    out = alloc(lufqhe_mod, cuda, off)
+    plan = lufqhe_mod.Plan(groups, out, mode=mode, autotune=False)
+    plan.execute()
+    cuda.cuda.synchronize()
+    got = host(out)
+    for A, o in groups:
+        ref = host(lufqhe_mod.batch_lup_det(A, mode=mode))
+        sl = slice(o, o + A.shape[0])
+        for k in ("logabs", "phase", "parity", "status"):
+            a, b = np.ascontiguousarray(got[k][sl]), ref[k]
+            same = (a == b) | (np.isnan(a) & np.isnan(b)) if a.dtype.kind == "f" else a == b
+            assert same.all(), (k, A.shape[1])
+    plan.close()
