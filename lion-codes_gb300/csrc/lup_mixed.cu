@@ -118,6 +118,8 @@ std::atomic<unsigned int> g_pend_seq{0};
 int next_pend_slot() { return (int)(g_pend_seq.fetch_add(1u) % kPendSlots); }
 
 constexpr int kDeferMinN = 24;
+// Warps of the FP64 pass's CTA (one CTA per SM).
+constexpr int kFallbackMaxWarps = 20;
 
 // Hand matrix b to the FP64 pass; false (warp-uniform) if there is none
 // (pslot < 0) or its list is full.
@@ -262,13 +264,20 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   release_slot(slot, lane);
 }
 
-// The FP64 pass: warps claim the pending list's entries one at a time and
-// refactorise those matrices (reference pivot rule, fused arithmetic, status
-// flag LUFQHE_ST_FALLBACK, or LUFQHE_ST_FP64 for the routed share). If the
-// list overflowed, claims past its end are chunks of 32 matrices whose logabs
-// the FP32 pass marked. The last CTA out empties the list for its next user.
+// The FP64 pass: one CTA per SM; its warps refactorise the pending list's
+// matrices (reference pivot rule, fused arithmetic, status flag
+// LUFQHE_ST_FALLBACK, or LUFQHE_ST_FP64 for the routed share). Every
+// factorisation of one n costs the same, so the entries are dealt out at a
+// fixed stride: entry j goes to warp j / G of CTA j % G (G CTAs), so the first
+// G entries land on warp 0 of every SM, the next G on warp 1 (the next SM
+// sub-partition), and no sub-partition's FP64 pipe holds more than
+// ceil(count / (4 G)) of them when the list is short. (First-come claims
+// piled up to five matrices on some sub-partitions while others idled.) If
+// the list overflowed, the matrices past it are found in chunks of 32 whose
+// logabs the FP32 pass marked, claimed from a counter. The last CTA out
+// empties the list for its next user.
 template <class Src>
-__global__ void __launch_bounds__(4 * 32)
+__global__ void __launch_bounds__(kFallbackMaxWarps * 32)
     lup_mixed_fallback_kernel(Src src, int n, long long batch,
                               int slot, int pslot, double *__restrict__ logabs,
                               double *__restrict__ phase, int8_t *__restrict__ parity,
@@ -289,23 +298,21 @@ __global__ void __launch_bounds__(4 * 32)
       min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
   const unsigned long long chunks =
       *(volatile unsigned int *)&g_pend_over[pslot] ? (unsigned long long)(batch + 31) / 32 : 0ull;
-  const unsigned long long claims = listed + chunks;
+  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
+  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
+       j += stride) {
+    const unsigned int e = g_pend[pslot][j];
+    const long long b = e & ~kPendRouted;
+    fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
+                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+  }
   for (;;) {
-    // look before claiming: in a grid sized for a long list, most warps find
-    // a short one already taken and leave without touching the counter
-    unsigned long long j = claims;
-    if (lane == 0 && *(volatile unsigned long long *)&g_work[slot][0] < claims)
-      j = atomicAdd(&g_work[slot][0], 1ull);
+    if (chunks == 0) break;
+    unsigned long long j = chunks;
+    if (lane == 0) j = atomicAdd(&g_work[slot][0], 1ull);
     j = __shfl_sync(kFull, j, 0);
-    if (j >= claims) break;
-    if (j < listed) {
-      const unsigned int e = g_pend[pslot][j];
-      const long long b = e & ~kPendRouted;
-      fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
-                        (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
-      continue;
-    }
-    const long long b0 = (long long)(j - listed) * 32;
+    if (j >= chunks) break;
+    const long long b0 = (long long)j * 32;
     long long bits = 0;
     if (b0 + lane < batch) bits = __double_as_longlong(logabs[b0 + lane]);
     const unsigned int routed = __ballot_sync(kFull, bits == kOverRoutedBits);
@@ -334,7 +341,7 @@ int launch_fallback(Src src, int n, long long batch, int pslot, double *logabs, 
                     int8_t *parity, int32_t *status, cudaStream_t stream) {
   const size_t per_warp = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
   int warps = (int)(device_smem_optin() / per_warp);
-  if (warps > 4) warps = 4;
+  if (warps > kFallbackMaxWarps) warps = kFallbackMaxWarps;
   if (warps < 1) warps = 1;
   const size_t smem = per_warp * warps;
   auto kern = lup_mixed_fallback_kernel<Src>;
@@ -346,10 +353,13 @@ int launch_fallback(Src src, int n, long long batch, int pslot, double *logabs, 
   rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
                   "occupancy(mixed fallback)");
   if (rc) return rc;
-  if (per_sm < 1) per_sm = 1;
-  // sized for the whole list; warps with nothing to claim leave at once
+  if (per_sm < 1) {
+    set_error("mixed fallback: n=%d does not fit on an SM", n);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  // one CTA per SM (the list's length is known only on the device)
   long long want = (batch + warps - 1) / warps;
-  long long cap = (long long)device_sm_count() * per_sm;
+  long long cap = (long long)device_sm_count();
   int grid = (int)(want < cap ? want : cap);
   kern<<<grid, warps * 32, smem, stream>>>(src, n, batch, next_work_slot(), pslot, logabs, phase,
                                            parity, status);
