@@ -42,6 +42,79 @@ __device__ __forceinline__ double wrap_phase(double x) {
   return r;
 }
 
+// ---- compact FP64 log|u| and arg u --------------------------------------------
+// Per-entry logs of an LU diagonal cost as much FP64-pipe time as a sizeable
+// share of the factorisation itself at n <= 32 (each is one SIMT pass of the
+// whole routine). These routines are shorter than the library's log(hypot())
+// and atan2: no hypot, quotients as a * RN(1/b), short series after exact
+// range reductions. Both are accurate to a few ulps. Entries with a component
+// outside [2^-500, 2^500] (where |u|^2 or 1/max(|x|,|y|) could leave the
+// normal range) take the library routines.
+//
+// log m for m in [1, 2) (k: the caller's power of two): m > sqrt(2) is halved
+// into [sqrt(1/2), sqrt(2)); log m = 2 atanh(s) = 2 (s + s^3/3 + ...),
+// s = (m - 1) / (m + 1), |s| <= 0.1716; the terms to s^23 leave a relative
+// remainder below 1e-19.
+__device__ __forceinline__ double log_mantissa(double a, int &k) {
+  long long bits = __double_as_longlong(a);
+  k = (int)((bits >> 52) & 0x7ff) - 1023;
+  bits = (bits & 0x000fffffffffffffll) | 0x3ff0000000000000ll;  // m in [1, 2)
+  double m = __longlong_as_double(bits);
+  if (m > 1.4142135623730951) {
+    m = __dmul_rn(m, 0.5);
+    k += 1;
+  }
+  const double s = __dmul_rn(__dadd_rn(m, -1.0), __drcp_rn(__dadd_rn(m, 1.0)));
+  const double z = __dmul_rn(s, s);
+  double t = 1.0 / 23.0;
+#pragma unroll
+  for (int j = 21; j >= 1; j -= 2) t = __fma_rn(t, z, 1.0 / (double)j);
+  return __dmul_rn(2.0 * s, t);
+}
+
+// atan2(y, x) for (x, y) != (0, 0) with max(|x|, |y|) in [2^-500, 2^500].
+// Octant reduction to t = min(|x|,|y|) / max(|x|,|y|) in [0, 1]; with
+// c_i = tan(i pi/16) the nearest of five points (i = 0..4),
+// atan t = i pi/16 + atan v, v = (t - c_i) / (1 + t c_i), |v| <= tan(pi/32)
+// < 0.0985, and the Taylor series v - v^3/3 + ... to v^17 (remainder below
+// 5e-21).
+__device__ __forceinline__ double atan2_reduced(double y, double x) {
+  const double ax = fabs(x), ay = fabs(y);
+  const bool swap = ay > ax;
+  const double t = __dmul_rn(swap ? ax : ay, __drcp_rn(swap ? ay : ax));
+  // the midpoints tan((2i + 1) pi/32) pick the nearest c_i
+  const int i = (t > 0.09849140335716425) + (t > 0.3033466836073424) +
+                (t > 0.5345111359507916) + (t > 0.8206787908286602);
+  const double c = i == 0   ? 0.0
+                   : i == 1 ? 0.198912367379658
+                   : i == 2 ? 0.41421356237309503
+                   : i == 3 ? 0.6681786379192989
+                            : 1.0;
+  const double v = __dmul_rn(__dadd_rn(t, -c), __drcp_rn(__fma_rn(t, c, 1.0)));
+  const double z = __dmul_rn(v, v);
+  double p = 1.0 / 17.0;
+#pragma unroll
+  for (int j = 15; j >= 1; j -= 2) p = __fma_rn(p, -z, 1.0 / (double)j);
+  double r = __fma_rn(v, p, (double)i * (kPi / 16.0));
+  if (swap) r = __dadd_rn(0.5 * kPi, -r);
+  if (x < 0.0) r = __dadd_rn(kPi, -r);
+  return y < 0.0 ? -r : r;
+}
+
+// log|u| and arg u of a nonzero finite complex number.
+__device__ __forceinline__ void log_arg_c(double2 u, double &lg, double &ar) {
+  const long long big = max(abs_bits(u.x), abs_bits(u.y));
+  if (big >= 0x20b0000000000000ll && big < 0x5f30000000000000ll) {  // [2^-500, 2^500)
+    int k;
+    const double lm = log_mantissa(__fma_rn(u.x, u.x, __dmul_rn(u.y, u.y)), k);
+    lg = __fma_rn((double)k, 0.5 * kLn2, __dmul_rn(0.5, lm));
+    ar = atan2_reduced(u.y, u.x);
+  } else {
+    lg = log(hypot(u.x, u.y));
+    ar = atan2(u.y, u.x);
+  }
+}
+
 // ---- complex arithmetic in the two operation orders -------------------------
 // ARITH_REF reproduces the reference's CPU Crout arithmetic
 // (LU-fqhe/src/LUCoreCPU.cu:173-177 and :243-247) operation for operation:

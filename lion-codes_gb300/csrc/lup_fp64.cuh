@@ -475,9 +475,10 @@ __device__ __forceinline__ void logdet_from_diag(const double2 *M, int lds, int 
                                                  int par, double *la_out, double *ph_out) {
   double la = 0.0, ph = 0.0;
   for (int j = lane; j < n; j += 32) {
-    double2 u = M[j * lds + j];
-    la += log(hypot(u.x, u.y));
-    ph += atan2(u.y, u.x);
+    double lg, ar;
+    log_arg_c(M[j * lds + j], lg, ar);
+    la += lg;
+    ph += ar;
   }
 #pragma unroll
   for (int off = 16; off; off >>= 1) {
