@@ -101,14 +101,18 @@ int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode, double *d_
 /*
  * Same call on HOST buffers: the batch and the four result arrays are in host
  * memory. Replaces the copy-in / LUCoreGPU::CALL / copy-out sequence of the
- * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329). The
- * batch is cut into chunks that three internal streams carry through
- * host-to-device copy, the batched kernels and device-to-host copy, so copies
- * of one chunk overlap the factorisation of another. Device staging comes from
- * the stream-ordered allocator and is released on `stream`. Host buffers
- * should be page-locked (cudaHostAlloc / cudaHostRegister) for the copies to
- * overlap; pageable memory works but serialises them. Asynchronous on
- * `stream`: the results are in host memory once `stream` has completed.
+ * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329).
+ * In mixed mode with a page-locked batch (cudaHostAlloc / cudaHostRegister)
+ * the kernels read the matrices over the host link themselves, with no copy,
+ * and write page-locked result arrays directly (pageable result arrays are
+ * filled by copies from device memory). Otherwise the batch is cut into
+ * chunks that three internal streams carry through host-to-device copy, the
+ * batched kernels and device-to-host copy, so copies of one chunk overlap the
+ * factorisation of another; pageable memory works but serialises the copies.
+ * Device memory comes from the stream-ordered allocator and is released on
+ * `stream`. Results are bit-identical to lufqhe_batch_lup_det's either way.
+ * Asynchronous on `stream`: the results are in host memory once `stream` has
+ * completed, and the batch must stay unchanged until then.
  * d_parity / d_status may be NULL as in lufqhe_batch_lup_det.
  */
 int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long long batch, int dtype,

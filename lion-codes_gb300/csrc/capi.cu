@@ -84,7 +84,8 @@ namespace lufqhe {
 
 // The batched kernels for one mode (arguments already checked).
 int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
-                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s) {
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s,
+                     bool host_link) {
   switch (mode) {
     case LUFQHE_MODE_PLAIN_FP64:
       return launch_plain(A, nullptr, n, lda, batch, ARITH_REF, logabs, phase, parity, status, s);
@@ -92,7 +93,7 @@ int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode
       return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity, status,
                           s);
     case LUFQHE_MODE_MIXED:
-      return launch_mixed(A, n, lda, batch, logabs, phase, parity, status, s);
+      return launch_mixed(A, n, lda, batch, logabs, phase, parity, status, s, host_link);
     default:
       set_error("lufqhe_batch_lup_det: unknown mode %d", mode);
       return LUFQHE_ERR_UNSUPPORTED_MODE;
@@ -111,7 +112,7 @@ extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long b
     return LUFQHE_ERR_UNSUPPORTED_MODE;
   }
   return batch_det_device(reinterpret_cast<const double2 *>(d_A), n, lda, batch, mode, d_logabs,
-                          d_phase, d_parity, d_status, (cudaStream_t)stream);
+                          d_phase, d_parity, d_status, (cudaStream_t)stream, false);
 }
 
 extern "C" int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode,

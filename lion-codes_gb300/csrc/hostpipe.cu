@@ -1,5 +1,18 @@
-// Host-buffer form of the batched determinant: chunked copy / compute / copy
-// pipeline over three internal streams.
+// Host-buffer form of the batched determinant.
+//
+// Mixed mode on a page-locked batch: no copies at all. The kernels read the
+// matrices over the host link themselves (the mapped device view of the
+// pinned buffer) and keep their FP64 refactorisations in the FP32 pass: the
+// pass waits on the link (about 210 GB/s host-to-device on GB300, against
+// about 1.3 TB/s of matrices the FP32 pass could take from HBM), so it has
+// compute to spare for them, and a second kernel would re-read the rejected
+// matrices after the link has gone idle. Results go straight to pinned output
+// arrays, or to device memory and back by copies. There is no pipeline fill
+// or drain and no chunk tail.
+//
+// Otherwise (pageable input, or the plain modes, whose kernels are
+// compute-bound and gain nothing from the link): a chunked copy / compute /
+// copy pipeline over three internal streams.
 //
 // The reference's Monte Carlo loop copies the batch to the device, runs the
 // LU kernel and copies the result back, one step after the other on one
@@ -52,7 +65,62 @@ int pipe_streams(PipeStreams *out) {
 int g_host_chunk_mb = 32;  // input bytes per chunk, MiB
 
 int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
-                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s);
+                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s,
+                     bool host_link);
+
+namespace {
+
+// Device view of page-locked host memory, or null (pageable, device or null p).
+void *mapped_view(const void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error some drivers report for unregistered memory
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Mixed mode on a pinned batch: one launch reading over the host link.
+int det_over_link(const double2 *dA, int n, int lda, long long batch, double *h_logabs,
+                  double *h_phase, int8_t *h_parity, int32_t *h_status, cudaStream_t s) {
+  double *la = static_cast<double *>(mapped_view(h_logabs));
+  double *ph = static_cast<double *>(mapped_view(h_phase));
+  int8_t *pa = static_cast<int8_t *>(mapped_view(h_parity));
+  int32_t *st = static_cast<int32_t *>(mapped_view(h_status));
+  if (la && (!h_phase || ph) && (!h_parity || pa) && (!h_status || st))
+    return batch_det_device(dA, n, lda, batch, LUFQHE_MODE_MIXED, la, ph, pa, st, s, true);
+  // pageable outputs: device results, then copies
+  const size_t nb = (size_t)batch;
+  unsigned char *buf = nullptr;
+  int rc = check_cuda(cudaMallocAsync((void **)&buf, nb * (2 * sizeof(double) + sizeof(int32_t) +
+                                                          sizeof(int8_t)),
+                                      s),
+                      "cudaMallocAsync(results)");
+  if (rc) return rc;
+  double *dla = reinterpret_cast<double *>(buf);
+  double *dph = dla + nb;
+  int32_t *dst = reinterpret_cast<int32_t *>(dph + nb);
+  int8_t *dpa = reinterpret_cast<int8_t *>(dst + nb);
+  rc = batch_det_device(dA, n, lda, batch, LUFQHE_MODE_MIXED, dla, h_phase ? dph : nullptr,
+                        h_parity ? dpa : nullptr, h_status ? dst : nullptr, s, true);
+  if (!rc)
+    rc = check_cuda(cudaMemcpyAsync(h_logabs, dla, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
+                    "D2H logabs");
+  if (!rc && h_phase)
+    rc = check_cuda(cudaMemcpyAsync(h_phase, dph, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
+                    "D2H phase");
+  if (!rc && h_status)
+    rc = check_cuda(cudaMemcpyAsync(h_status, dst, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+                    "D2H status");
+  if (!rc && h_parity)
+    rc = check_cuda(cudaMemcpyAsync(h_parity, dpa, nb * sizeof(int8_t), cudaMemcpyDeviceToHost, s),
+                    "D2H parity");
+  const int r2 = check_cuda(cudaFreeAsync(buf, s), "cudaFreeAsync(results)");
+  return rc ? rc : r2;
+}
+
+}  // namespace
 
 }  // namespace lufqhe
 
@@ -81,6 +149,10 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   }
   if (batch == 0) return LUFQHE_SUCCESS;
   cudaStream_t user = (cudaStream_t)stream;
+  if (mode == LUFQHE_MODE_MIXED)
+    if (const void *dA = mapped_view(h_A))
+      return det_over_link(static_cast<const double2 *>(dA), n, lda, batch, h_logabs, h_phase,
+                           h_parity, h_status, user);
   PipeStreams ps;
   int rc = pipe_streams(&ps);
   if (rc) return rc;
@@ -123,7 +195,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
                     "H2D chunk");
     if (!rc)
       rc = batch_det_device(dA, n, lda, cnt, mode, dla, h_phase ? dph : nullptr,
-                            h_parity ? dpa : nullptr, h_status ? dst : nullptr, s);
+                            h_parity ? dpa : nullptr, h_status ? dst : nullptr, s, false);
     if (!rc)
       rc = check_cuda(cudaMemcpyAsync(h_logabs + lo, dla, (size_t)cnt * sizeof(double),
                                       cudaMemcpyDeviceToHost, s),

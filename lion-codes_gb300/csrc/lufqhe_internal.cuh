@@ -190,8 +190,11 @@ int launch_plain_lll(const double2 *Z, int n, long long batch, int arith, double
                      int status_or = 0);
 int launch_mixed_lll(const double2 *Z, int n, long long batch, double *logabs, double *phase,
                      int8_t *parity, int32_t *status, cudaStream_t stream);
+// inplace: FP64 refactorisations stay in the FP32 pass (no second kernel);
+// used when A is read over the host link.
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
-                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream);
+                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
+                 bool inplace = false);
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,
                      const double *phase, const int32_t *status, int pair_product,
                      cudaStream_t stream);

@@ -43,6 +43,7 @@
 
 #include <atomic>
 #include <cmath>
+#include <type_traits>
 
 #include "mixed_core.cuh"
 
@@ -206,17 +207,19 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
 }
 
 
-template <int N, class Src>
+template <int N, class Src, bool INPLACE = false>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     lup_mixed_tile_kernel(Src src, long long batch, float theta2,
-                          unsigned int share64k, int slot, int pslot,
+                          unsigned int share64k, int slot, int pslot, double2 *spill,
                           double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // n >= 24: every FP64 factorisation goes to the FP64 pass, so this kernel
-  // carries no FP64 factorisation code (a smaller instruction footprint)
-  constexpr bool DEFER = N >= kDeferMinN;
+  // carries no FP64 factorisation code (a smaller instruction footprint).
+  // INPLACE keeps them in this kernel: for a batch read over the host link,
+  // where the FP32 pass waits on the link and has compute to spare.
+  constexpr bool DEFER = !INPLACE && N >= kDeferMinN;
   constexpr int LDS = N + 1;
   constexpr size_t NL = (size_t)N * LDS;
   const int warps = blockDim.x >> 5;
@@ -231,6 +234,10 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   base += warps * 2 * (size_t)N * sizeof(double);
   int *er = reinterpret_cast<int *>(base) + warp * 2 * N;
   int *ec = er + N;
+  // INPLACE: this warp's copy of its current matrix in global memory (a few
+  // KB per warp, so the copies stay in L2); an FP64 refactorisation reloads
+  // it from there instead of reading the matrix over the host link again
+  double2 *own = INPLACE ? spill + ((size_t)blockIdx.x * warps + warp) * N * N : nullptr;
 
   DeferredOut out;
   for (;;) {
@@ -250,6 +257,13 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
     }
+    if constexpr (INPLACE) {
+      BlockWalk w(lane, N);
+      for (int e = lane; e < N * N; e += 32) {
+        own[e] = M[w.i * LDS + w.k];
+        w.next(N);
+      }
+    }
     CFF prod;
     int exp_sum, par;
     float2 corr;
@@ -257,6 +271,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
       out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
     else if constexpr (DEFER)
       defer_fp64_always(pslot, b, lane, false, logabs);
+    else if constexpr (INPLACE)
+      fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
+                                           logabs, phase, parity, status);
     else
       fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
   }
@@ -368,7 +385,10 @@ int launch_fallback(Src src, int n, long long batch, int pslot, double *logabs, 
 
 template <int N, class Src>
 int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, double *phase,
-                      int8_t *parity, int32_t *status, cudaStream_t stream) {
+                      int8_t *parity, int32_t *status, cudaStream_t stream, bool inplace) {
+  // only dense batches of the deferring sizes have an in-place variant
+  constexpr bool kHasInplace = N >= kDeferMinN && std::is_same<Src, DenseSource>::value;
+  if (!kHasInplace) inplace = false;
   const size_t per_warp = tile_smem_per_warp<N>();
   // small CTAs: the register-heavy residual tile limits residency, and
   // smaller CTAs let the scheduler fill an SM with several of them
@@ -377,7 +397,9 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   if (g_tile_warps > 0 && g_tile_warps < wcap) wcap = g_tile_warps;
   if (warps > wcap) warps = wcap;
   const size_t smem = per_warp * warps;
-  auto kern = lup_mixed_tile_kernel<N, Src>;
+  auto kern = lup_mixed_tile_kernel<N, Src, false>;
+  if constexpr (kHasInplace)
+    if (inplace) kern = lup_mixed_tile_kernel<N, Src, true>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
                       "cudaFuncSetAttribute(mixed tile)");
@@ -390,10 +412,21 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
-  const int pslot = N >= kDeferMinN ? next_pend_slot() : -1;
+  const int pslot = N >= kDeferMinN && !inplace ? next_pend_slot() : -1;
+  double2 *spill = nullptr;
+  if (inplace) {
+    rc = check_cuda(cudaMallocAsync((void **)&spill, (size_t)grid * warps * N * N * sizeof(double2),
+                                    stream),
+                    "cudaMallocAsync(mixed spill)");
+    if (rc) return rc;
+  }
   kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), next_work_slot(),
-                                           pslot, logabs, phase, parity, status);
+                                           pslot, spill, logabs, phase, parity, status);
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
+  if (spill) {
+    const int r2 = check_cuda(cudaFreeAsync(spill, stream), "cudaFreeAsync(mixed spill)");
+    if (!rc) rc = r2;
+  }
   if (rc || pslot < 0) return rc;
   return launch_fallback(src, N, batch, pslot, logabs, phase, parity, status, stream);
 }
@@ -413,7 +446,8 @@ namespace {
 // plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
 template <class Src, class PlainFn>
 int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *phase,
-                     int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64) {
+                     int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64,
+                     bool inplace = false) {
   if (batch == 0) return LUFQHE_SUCCESS;
   // every matrix on the FP64 route: the plain fused kernel, whose shared
   // memory layout holds more warps per SM than the mixed kernels'
@@ -421,12 +455,12 @@ int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *ph
     return plain_fp64();
   const float th2 = g_mixed_theta * g_mixed_theta;
   switch (n) {
-    case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream);
-    case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream);
-    case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream);
-    case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream);
-    case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream);
-    case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream);
+    case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+    case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+    case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+    case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+    case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+    case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
     default: break;
   }
   const size_t per_warp = mixed_smem_per_warp(n);
@@ -465,12 +499,15 @@ int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *ph
 }  // namespace
 
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
-                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream) {
-  return launch_mixed_src(DenseSource{A, lda}, n, batch, logabs, phase, parity, status, stream,
-                          [&] {
-                            return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs,
-                                                phase, parity, status, stream, LUFQHE_ST_FP64);
-                          });
+                 double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
+                 bool inplace) {
+  return launch_mixed_src(
+      DenseSource{A, lda}, n, batch, logabs, phase, parity, status, stream,
+      [&] {
+        return launch_plain(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity, status,
+                            stream, LUFQHE_ST_FP64);
+      },
+      inplace);
 }
 
 int launch_mixed_lll(const double2 *Z, int n, long long batch, double *logabs, double *phase,

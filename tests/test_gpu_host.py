@@ -42,3 +42,26 @@ def test_host_entry_repeated_calls_share_nothing(cuda, lufqhe_mod):
     s.synchronize()
     for o in outs:
         assert np.array_equal(host_dict(o)["logabs"], want["logabs"], equal_nan=True)
+
+
+@pytest.mark.parametrize("n,batch", [(24, 6000), (16, 5000), (32, 3000)])
+@pytest.mark.parametrize("out_pinned", [True, False])
+def test_mixed_over_host_link(cuda, lufqhe_mod, n, batch, out_pinned):
+    """Mixed mode on a pinned batch: the kernels read the matrices over the
+    host link and refactorise rejected ones in place; results equal the device
+    entry point's (FP32 pass + separate FP64 pass) bit for bit, with pinned or
+    pageable result arrays."""
+    import torch
+    A, _ = lufqhe_mod.gen_lll(batch, n, seed=400 + n)
+    want = dev_dict(lufqhe_mod.batch_lup_det(A, mode=2))
+    A_host = A.cpu().pin_memory()
+    out = lufqhe_mod.DetResult(*(torch.empty(batch, dtype=d, pin_memory=out_pinned)
+                                 for d in (torch.float64, torch.float64, torch.int8, torch.int32)))
+    s = cuda.cuda.Stream()
+    lufqhe_mod.batch_lup_det_host(A_host, mode=2, stream=s, out=out)
+    s.synchronize()
+    got = host_dict(out)
+    for k in ("logabs", "phase"):
+        assert np.array_equal(got[k], want[k], equal_nan=True), k
+    assert (got["parity"] == want["parity"]).all() and (got["status"] == want["status"]).all()
+    assert ((got["status"] & lufqhe_mod.ST_FALLBACK) != 0).any() or n < 24
