@@ -74,9 +74,20 @@ def mixed_launches_per_call(n: int) -> int:
 
 
 def host_chunks(n: int, lda: int, batch: int, chunk_mb: int = 32) -> int:
-    """Chunks lufqhe_batch_lup_det_host cuts a batch into (chunk_mb MiB of input each)."""
+    """Chunks lufqhe_batch_lup_det_host cuts a batch into (chunk_mb MiB of input each)
+    when it stages the batch through device memory (pageable input, plain modes)."""
     per = max(1, (chunk_mb << 20) // (n * lda * 16))
     return (batch + per - 1) // per
+
+
+def host_launches_per_call(n: int, lda: int, batch: int, mode: int, pinned: bool) -> int:
+    """Kernels one lufqhe_batch_lup_det_host call launches. Mixed mode on a
+    pinned batch is one launch reading over the host link (FP64
+    refactorisations in place, or the plain kernel when the policy sends the
+    size to FP64); otherwise the staged pipeline runs the batched call per chunk."""
+    if mode == 2 and pinned:
+        return 1
+    return host_chunks(n, lda, batch) * (mixed_launches_per_call(n) if mode == 2 else 1)
 
 
 def bytes_per_matrix(n: int) -> float:
@@ -575,7 +586,7 @@ def run_ours(args):
     e3.record(stream)
     torch.cuda.synchronize()
     ms_e2e = max_over_ranks(world, e2.elapsed_time(e3) / args.steps)
-    launches += args.steps * host_chunks(n, n, batch) * mixed_launches_per_call(n)
+    launches += args.steps * host_launches_per_call(n, n, batch, mode, A_host.is_pinned())
 
     # ---- e2e from particle coordinates (LLL workloads) ---------------------
     # what a Monte Carlo driver holds is z, not the matrices: H2D of the

@@ -320,16 +320,41 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
 constexpr int kFp64GroupWarps = 4;
 constexpr int kFp64GroupMinN = 33;
 
-// The same factorisation by all threads of a CTA (a warp group), for n > 32
-// where one warp per matrix leaves too few warps on an SM to keep the FP64
-// pipe busy. Every pivot decision is taken on the same candidate keys with
-// the same rule (ties to the larger row) and every entry sees the same
-// operations in the same order as in lup_fp64_warp, so the factors, pivots
-// and parity are bit-identical to it. `red` is 3 x (warps) words of shared
-// scratch for the cross-warp reductions. CTA-uniform return value.
-template <int ARITH>
+// Barrier of the threads that factorise one matrix together: the whole CTA,
+// or a named barrier (id 1..15) of `count` threads, a multiple of 32, so that
+// several warp groups of one CTA can factorise different matrices.
+struct CtaBarrier {
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ bool sync_or(bool v) const { return __syncthreads_or(v) != 0; }
+};
+struct NamedBarrier {
+  int id, count;
+  __device__ __forceinline__ void sync() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+  __device__ __forceinline__ bool sync_or(bool v) const {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, %2, %3, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+  }
+};
+
+// The same factorisation by all threads of a warp group (a CTA, or part of
+// one behind a named barrier), for n > 32 where one warp per matrix leaves too
+// few warps on an SM to keep the FP64 pipe busy. Every pivot decision is taken
+// on the same candidate keys with the same rule (ties to the larger row) and
+// every entry sees the same operations in the same order as in lup_fp64_warp,
+// so the factors, pivots and parity are bit-identical to it. `red` is
+// 3 x (warps) words of shared scratch for the cross-warp reductions; tid and
+// nthr number the group's threads. Group-uniform return value.
+template <int ARITH, class Bar = CtaBarrier>
 __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid, int nthr,
-                              long long *red, int *parity) {
+                              long long *red, int *parity, Bar bar = Bar()) {
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   long long *red_k = red;
   int *red_i = reinterpret_cast<int *>(red + nw);
@@ -347,7 +372,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       rhold[i] = __drcp_rn(h);
       tiny |= big < tiny_bits;
     }
-    if (__syncthreads_or(tiny)) {
+    if (bar.sync_or(tiny)) {
       *parity = 0;
       return LUFQHE_ST_SCALE_TINY;
     }
@@ -367,7 +392,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       red_k[warp] = bk;
       red_i[warp] = bi;
     }
-    __syncthreads();
+    bar.sync();
     bk = red_k[0];
     bi = red_i[0];
     for (int q = 1; q < nw; ++q) {
@@ -376,7 +401,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
         bi = red_i[q];
       }
     }
-    __syncthreads();
+    bar.sync();
   };
   const long long safe_lo = 0x0170000000000000ll;  // 2^-1000
   const long long safe_hi = 0x7e70000000000000ll;  // 2^+1000
@@ -400,10 +425,10 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
     }
     near = __reduce_add_sync(kFull, near);
     if (lane == 0) red_n[warp] = near;
-    __syncthreads();
+    bar.sync();
     near = 0;
     for (int q = 0; q < nw; ++q) near += red_n[q];
-    __syncthreads();
+    bar.sync();
     if (near != 1 || bk < safe_lo || bk > safe_hi) {
       bk = -1;
       bi = j;
@@ -430,7 +455,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       }
       par ^= 1;
     }
-    __syncthreads();
+    bar.sync();
     const double2 piv = M[j * lds + j];
     if (is_zero_c(piv)) {
       *parity = par;
@@ -454,7 +479,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       for (int i = j + 1 + tid; i < n; i += nthr)
         M[i * lds + j] = cdiv_pivot<ARITH>(M[i * lds + j], piv, d);
     }
-    __syncthreads();
+    bar.sync();
     const int m = n - 1 - j;
     const int mm = m * m;
     const int j1 = j + 1;
@@ -464,7 +489,7 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       M[ii * lds + kk] = cmsub<ARITH>(M[ii * lds + kk], M[ii * lds + j], M[j * lds + kk]);
       w.next(m);
     }
-    __syncthreads();
+    bar.sync();
   }
   *parity = par;
   return 0;

@@ -262,8 +262,150 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
   }
 }
 
+// Claim the next published tile of a class (one thread): a compare-and-swap
+// on the claim counter while it is below the published count. Returns false
+// when the class has had no claim for kIdleNs or the server is stopping.
+__device__ bool claim_tile(const unsigned int *published, const unsigned int *stop, ClassCtl *ctl,
+                           unsigned int &idx) {
+  const unsigned long long t0 = global_ns();
+  volatile unsigned int *claimed = &ctl->claimed;
+  for (;;) {
+    const unsigned int c = *claimed;
+    const unsigned int p = ld_acquire_sys(published);
+    if ((int)(p - c) > 0) {
+      if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
+        idx = c;
+        atomicMax(&ctl->last_ns, global_ns());
+        return true;
+      }
+      continue;
+    }
+    if (ld_acquire_sys(stop)) return false;
+    const unsigned long long now = global_ns();
+    const unsigned long long last = *(volatile unsigned long long *)&ctl->last_ns;
+    if (now - (last > t0 ? last : t0) > kIdleNs) return false;
+    __nanosleep(256);
+  }
+}
+
+// FP64-only classes with n >= kFp64GroupMinN: the CTA's warps work in groups
+// of kFp64GroupWarps. Each group claims tiles like a warp of serve_kernel and
+// factorises their matrices one at a time with all its threads
+// (lup_fp64_group behind the group's named barrier), as the batched FP64
+// kernel does for these sizes: with one warp per n=64 matrix only three warps
+// fit in an SM's shared memory and the FP64 pipe starves. Results are
+// bit-identical to the warp routine's.
+constexpr int kServeGroupsMax = 4;
+
+template <int NC>
+__global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
+    serve_group_kernel(const ServeTile *ring, const unsigned int *published,
+                       const unsigned int *stop, ClassCtl *ctl, int mode, float theta2,
+                       unsigned int share64k) {
+  (void)theta2;
+  (void)share64k;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LDS = NC + 1;
+  constexpr size_t NL = (size_t)NC * LDS;
+  constexpr int GT = kFp64GroupWarps * 32;  // threads per group
+  constexpr int TW = (int)(sizeof(ServeTile) / 8);
+  __shared__ long long red_s[kServeGroupsMax][3 * kFp64GroupWarps];
+  __shared__ unsigned long long tile_s[kServeGroupsMax][TW];
+  __shared__ int go_s[kServeGroupsMax];
+  const int groups = blockDim.x / GT;
+  const int g = threadIdx.x / GT;
+  const int tid = threadIdx.x - g * GT, lane = tid & 31;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw) + g * NL;
+  double *hold =
+      reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) + groups * NL) + g * 2 * NC;
+  const NamedBarrier bar{1 + g, GT};
+  for (;;) {
+    if (tid == 0) {
+      unsigned int idx = 0;
+      const bool go = claim_tile(published, stop, ctl, idx);
+      go_s[g] = go;
+      if (go) {
+        // the ring lives in mapped host memory: read it uncached, word by word
+        const unsigned long long *srcw =
+            reinterpret_cast<const unsigned long long *>(ring + (idx % kRing));
+#pragma unroll
+        for (int q = 0; q < TW; ++q) tile_s[g][q] = __ldcv(srcw + q);
+      }
+    }
+    bar.sync();
+    if (!go_s[g]) {
+      if (tid == 0) atomicAdd(&ctl->exited, 1u);
+      return;
+    }
+    ServeTile t;
+    {
+      unsigned long long *dstw = reinterpret_cast<unsigned long long *>(&t);
+#pragma unroll
+      for (int q = 0; q < TW; ++q) dstw[q] = tile_s[g][q];
+    }
+    if (tid < 32) apply_move(t, NC, lane);
+    for (int j = 0; j < t.count; ++j) {
+      bar.sync();  // the move's rows are written; M is free again
+      const double2 *src = t.mats + (size_t)j * NC * NC;
+      bool bad = false;
+      StrideWalk w(tid, GT, NC);
+      for (int e = tid; e < NC * NC; e += GT) {
+        const double2 v = __ldcg(src + (size_t)w.i * NC + w.k);
+        bad |= !finite_c(v);
+        M[w.i * LDS + w.k] = v;
+        w.next(NC);
+      }
+      bad = bar.sync_or(bad);
+      int par = 0;
+      const int st = bad ? LUFQHE_ST_NONFINITE
+                         : lup_fp64_group<ARITH_FUSED>(M, LDS, hold, NC, tid, GT, red_s[g], &par,
+                                                       bar);
+      bar.sync();
+      if (tid < 32) {
+        double la, ph;
+        if (st == 0) {
+          logdet_from_diag(M, LDS, NC, lane, par, &la, &ph);
+        } else if (st == LUFQHE_ST_SINGULAR) {
+          la = -INFINITY;
+          ph = 0.0;
+        } else {
+          la = NAN;
+          ph = NAN;
+        }
+        if (tid == 0) {
+          t.logabs[j] = la;
+          t.phase[j] = ph;
+          // a non-finite input carries no route flag, as in serve_kernel
+          t.status[j] = bad ? st : st | (mode == LUFQHE_MODE_MIXED ? LUFQHE_ST_FP64 : 0);
+        }
+      }
+    }
+    if (tid == 0) {
+      __threadfence_system();  // the result stores before the count
+      const unsigned int done = atomicAdd(t.req_done, 1u) + 1u;
+      if (done == t.req_tiles) {
+        atomicExch(t.req_done, 0u);
+        __threadfence_system();
+        st_release_sys(t.completion, t.seq);
+      }
+    }
+    bar.sync();  // tile_s and go_s are rewritten by the next claim
+  }
+}
+
 using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
                              ClassCtl *, int, float, unsigned int);
+
+ServeKernel serve_group_kernel_for(int n) {
+  switch (n) {
+    case 64: return serve_group_kernel<64>;
+    default: return nullptr;
+  }
+}
+
+size_t serve_group_smem(int n) {
+  return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
+}
 
 ServeKernel serve_kernel_for(int n) {
   switch (n) {
@@ -489,16 +631,33 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     sc.share64k = mode == LUFQHE_MODE_MIXED ? fp64_share_64k(sc.n) : 0u;
     const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u;
     const size_t optin = device_smem_optin();
-    const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only);
-    sc.warps = std::max(1, std::min<int>(serve_max_warps(sc.n), (int)(optin / per_warp)));
-    if (per_warp * sc.warps > optin) {
-      set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per warp", sc.n,
-                per_warp);
-      rc = LUFQHE_ERR_UNSUPPORTED_N;
-      break;
+    size_t used = 0;
+    if (fp64_only && serve_group_kernel_for(sc.n)) {
+      // warp groups, one matrix each
+      sc.kern = serve_group_kernel_for(sc.n);
+      const size_t per_group = serve_group_smem(sc.n);
+      const int groups = std::min<int>(kServeGroupsMax, (int)((optin - 4096) / per_group));
+      if (groups < 1) {
+        set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per matrix", sc.n,
+                  per_group);
+        rc = LUFQHE_ERR_UNSUPPORTED_N;
+        break;
+      }
+      sc.warps = groups * kFp64GroupWarps;
+      used = per_group * groups;
+    } else {
+      const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only);
+      sc.warps = std::max(1, std::min<int>(serve_max_warps(sc.n), (int)(optin / per_warp)));
+      if (per_warp * sc.warps > optin) {
+        set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per warp", sc.n,
+                  per_warp);
+        rc = LUFQHE_ERR_UNSUPPORTED_N;
+        break;
+      }
+      used = per_warp * sc.warps;
     }
     // above half the SM's shared memory: one class CTA per SM
-    sc.smem = std::max(per_warp * sc.warps, optin / 2 + 1024);
+    sc.smem = std::max(used, optin / 2 + 1024);
     rc = check_cuda(cudaFuncSetAttribute(sc.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sc.smem),
                     "cudaFuncSetAttribute(serve)");
@@ -773,8 +932,36 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
     bool in_flight;
   };
   std::vector<Active> act;
-  std::vector<double> zbuf;
   const int nclass = (int)s->classes.size();
+  // The client's coordinates come from tables of Gaussian draws made before
+  // the clock starts (one per class, scaled by its sigma, in page-locked
+  // memory), read at a rolling offset: drawing up to 2 k n normals per new
+  // walker inside the loop took milliseconds of host time and delayed every
+  // other request's submission and completion polling.
+  const size_t kTable = (size_t)1 << 20;
+  std::vector<double *> table(nclass, nullptr);
+  std::vector<size_t> table_off(nclass, 0);
+  auto release_tables = [&] {
+    for (double *t : table)
+      if (t) cudaFreeHost(t);
+  };
+  for (int c = 0; c < nclass; ++c) {
+    int rc = check_cuda(cudaMallocHost((void **)&table[c], kTable * sizeof(double)),
+                        "run_stream tables");
+    if (rc) {
+      release_tables();
+      return rc;
+    }
+    const double sig = std::sqrt((double)s->classes[c].n / 2.0);
+    for (size_t i = 0; i < kTable; ++i) table[c][i] = gauss(rng) * sig;
+  }
+  auto draws = [&](int n, size_t count) -> const double * {
+    const int c = class_index(s, n);
+    if (table_off[c] + count > kTable) table_off[c] = 0;
+    const double *p = table[c] + table_off[c];
+    table_off[c] += count;
+    return p;
+  };
   long long issued = 0, recorded = 0, mats = 0;
   double next_arrival = now_s();
   const double start = next_arrival;
@@ -801,25 +988,25 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
         const double lk = std::log((double)k_min) +
                           uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
         const int k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
-        const double sig = std::sqrt((double)n / 2.0);
-        zbuf.resize((size_t)2 * k * n);
-        for (auto &v : zbuf) v = gauss(rng) * sig;
         int id = -1;
-        int rc = lufqhe_server_walker_create(s, n, k, zbuf.data(), &id);
+        int rc = lufqhe_server_walker_create(s, n, k, draws(n, (size_t)2 * k * n), &id);
         if (rc == LUFQHE_ERR_BUSY) break;  // HBM budget: wait for walkers to finish
-        if (rc) return rc;
+        if (rc) {
+          release_tables();
+          return rc;
+        }
         act.push_back({id, n, k, moves, 0, 0.0, false});
         use = (int)act.size() - 1;
       }
       Active &A = act[use];
       const int particle = (int)(uni(rng) * A.n) % A.n;
-      zbuf.resize((size_t)2 * A.k);
-      const double sig = std::sqrt((double)A.n / 2.0);
-      for (auto &v : zbuf) v = gauss(rng) * sig;
       long long ticket = 0;
-      int rc = lufqhe_server_submit(s, A.id, particle, zbuf.data(), &ticket);
+      int rc = lufqhe_server_submit(s, A.id, particle, draws(A.n, (size_t)2 * A.k), &ticket);
       if (rc == LUFQHE_ERR_BUSY) break;  // ring or slots full: retry next pass
-      if (rc) return rc;
+      if (rc) {
+        release_tables();
+        return rc;
+      }
       A.ticket = ticket;
       A.arrival = pending[p];
       A.in_flight = true;
@@ -841,11 +1028,15 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
           A.in_flight = false;
           if (--A.moves_left == 0) {
             rc = lufqhe_server_walker_destroy(s, A.id);
-            if (rc) return rc;
+            if (rc) {
+              release_tables();
+              return rc;
+            }
             act.erase(act.begin() + a);
             continue;
           }
         } else if (rc != LUFQHE_ERR_BUSY) {
+          release_tables();
           return rc;
         }
       }
@@ -856,5 +1047,6 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
   if (matrices) *matrices = mats;
   // retire the remaining walkers
   for (auto &A : act) lufqhe_server_walker_destroy(s, A.id);
+  release_tables();
   return std::min(recorded, max_records);
 }

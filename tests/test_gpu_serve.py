@@ -127,3 +127,32 @@ def test_large_class_follows_precision_policy(lufqhe_mod, cuda, oracle):
         assert (np.abs(la - want) / np.maximum(1, np.abs(want))).max() < 1e-8
     finally:
         srv.close()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_large_class_matches_batched_fp64_bits(lufqhe_mod, cuda, mode):
+    """The n = 64 class factorises each matrix with a warp group (one named
+    barrier per group, several groups per CTA): results equal the batched FP64
+    fused kernel's on the same matrices bit for bit, before and after a move,
+    with many tiles in flight at once."""
+    import torch
+    srv = lufqhe_mod.Server(1 << 30, mode=mode, classes=(64,), max_k=512, tile=8)
+    try:
+        rng = np.random.default_rng(8)
+        z = zdraw(rng, 300, 64)
+        w = srv.walker(z)
+        la, ph, st = srv.result(srv.submit(w, -1), 300)
+        ref = lufqhe_mod.lll_det(torch.from_numpy(z).cuda(), mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED)
+        flag = lufqhe_mod.ST_FP64 if mode == lufqhe_mod.MODE_MIXED else 0
+        assert np.array_equal(la, ref.logabs.cpu().numpy())
+        assert np.array_equal(ph, ref.phase.cpu().numpy())
+        assert (st == (ref.status.cpu().numpy() | flag)).all()
+        znew = zdraw(rng, 300, 1)[:, 0]
+        la2, ph2, _ = srv.result(srv.submit(w, 11, znew), 300)
+        z[:, 11] = znew
+        ref2 = lufqhe_mod.lll_det(torch.from_numpy(z).cuda(), mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED)
+        assert np.array_equal(la2, ref2.logabs.cpu().numpy())
+        assert np.array_equal(ph2, ref2.phase.cpu().numpy())
+        srv.destroy_walker(w)
+    finally:
+        srv.close()
