@@ -174,7 +174,7 @@ int lufqhe_pair_sum(const double *d_logabs, const double *d_phase, long long bat
 /* One group of same-size matrices of a mixed-size batch. Its results go to
  * indices out_offset .. out_offset + count - 1 of the output arrays. */
 typedef struct {
-  const void *A;        /* device pointer, complex128, layout as above */
+  const void *A;        /* device or page-locked host pointer, complex128, layout as above */
   int n;
   int lda;
   long long count;
@@ -187,8 +187,10 @@ typedef struct lufqhe_plan_s lufqhe_plan_t;
 #define LUFQHE_PLAN_AUTOTUNE 1
 
 /*
- * Build a plan for fixed groups and output buffers (device pointers, length =
- * max out_offset + count). The work list (tiles of same-n matrices, largest n
+ * Build a plan for fixed groups and output buffers (length = max out_offset +
+ * count). Inputs and outputs are device memory or page-locked host memory;
+ * the kernels read and write page-locked host memory over the host link, so a
+ * plan on host buffers needs no copies. The work list (tiles of same-n matrices, largest n
  * first) and a CUDA graph of the persistent launch are made once; the input
  * matrices may change between executions, their addresses may not. The
  * reference factorises one size per CALL (LU-fqhe/src/LUCoreGPU.cu:38-106);

@@ -83,6 +83,16 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
 namespace lufqhe {
 
 // The batched kernels for one mode (arguments already checked).
+const void *device_address(const void *p) {
+  if (!p) return p;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error some drivers report for unregistered memory
+    return p;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : p;
+}
+
 int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
                      double *phase, int8_t *parity, int32_t *status, cudaStream_t s,
                      bool host_link) {

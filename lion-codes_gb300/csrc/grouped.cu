@@ -598,10 +598,11 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   *plan = nullptr;
   lufqhe_plan_s *p = new lufqhe_plan_s();
   p->mode = mode;
-  p->logabs = d_logabs;
-  p->phase = d_phase;
-  p->parity = d_parity;
-  p->status = d_status;
+  // outputs and inputs may be page-locked host memory: kernels use its device view
+  p->logabs = static_cast<double *>(const_cast<void *>(device_address(d_logabs)));
+  p->phase = static_cast<double *>(const_cast<void *>(device_address(d_phase)));
+  p->parity = static_cast<int8_t *>(const_cast<void *>(device_address(d_parity)));
+  p->status = static_cast<int32_t *>(const_cast<void *>(device_address(d_status)));
   p->theta2 = g_mixed_theta * g_mixed_theta;
   for (int g = 0; g < ngroups; ++g) {
     const lufqhe_group_t &G = groups[g];
@@ -617,6 +618,7 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
       return LUFQHE_ERR_UNSUPPORTED_N;
     }
     p->groups.push_back(G);
+    p->groups.back().A = device_address(G.A);
     p->tile.push_back(default_tile(G.n));
     // the per-n FP64 share of the batched mixed kernels
     p->share.push_back(fp64_share_64k(G.n));

@@ -18,6 +18,9 @@ void set_error(const char *fmt, ...);
 int check_cuda(cudaError_t e, const char *what);
 int device_sm_count();
 size_t device_smem_optin();
+// Device address of p: p itself for device memory, the mapped view for
+// page-locked host memory (which kernels then read and write over the host link).
+const void *device_address(const void *p);
 
 // ---- IEEE helpers ----------------------------------------------------------
 __device__ __forceinline__ bool finite_d(double v) {

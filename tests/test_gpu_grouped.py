@@ -123,3 +123,35 @@ def test_plan_large_sizes(cuda, lufqhe_mod, mode):
             same = (a == b) | (np.isnan(a) & np.isnan(b)) if a.dtype.kind == "f" else a == b
             assert same.all(), (k, A.shape[1])
     plan.close()
+
+
+def test_plan_on_host_buffers(cuda, lufqhe_mod):
+    """A plan whose groups and outputs are page-locked host memory: the kernels
+    read and write over the host link; results equal the device plan's bit
+    for bit, and new host inputs at the same addresses are picked up."""
+    torch = cuda
+    groups, total = make_groups(lufqhe_mod, cuda, (40, 33, 21, 17, 30, 12, 9))
+    out = alloc(lufqhe_mod, cuda, total)
+    plan = lufqhe_mod.Plan(groups, out, mode=lufqhe_mod.MODE_MIXED, autotune=False)
+    plan.execute()
+    hosts = [(A.cpu().pin_memory(), o) for A, o in groups]
+    out_h = lufqhe_mod.DetResult(*(torch.empty(total, dtype=d, pin_memory=True)
+                                   for d in (torch.float64, torch.float64, torch.int8, torch.int32)))
+    plan_h = lufqhe_mod.Plan(hosts, out_h, mode=lufqhe_mod.MODE_MIXED, autotune=False)
+    plan_h.execute()
+    torch.cuda.synchronize()
+    want = host(out)
+    for k in ("logabs", "phase", "parity", "status"):
+        a, b = getattr(out_h, k).numpy(), want[k]
+        assert (((a == b) | (np.isnan(a) & np.isnan(b))) if a.dtype.kind == "f" else a == b).all(), k
+    # new matrices in the same host buffers
+    for (H, o), n in zip(hosts, SIZES):
+        B, _ = lufqhe_mod.gen_lll(H.shape[0], n, seed=950 + n)
+        H.copy_(B.cpu())
+    plan_h.execute()
+    torch.cuda.synchronize()
+    for (H, o) in hosts:
+        ref = host(lufqhe_mod.batch_lup_det(H.cuda(), mode=lufqhe_mod.MODE_MIXED))
+        assert np.array_equal(out_h.logabs.numpy()[o:o + H.shape[0]], ref["logabs"], equal_nan=True)
+    plan.close()
+    plan_h.close()
