@@ -94,6 +94,8 @@ int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int d
  * builder (LU-fqhe/src/mkMatrixElements.cu:169-358, compiled out there) fused
  * into the LUP prologue; the results are bit-identical to lufqhe_gen_lll's
  * matrices passed to lufqhe_batch_lup_det. Modes and outputs as there.
+ * d_z and the outputs may also be page-locked host memory, which the kernels
+ * then read and write over the host link (16n bytes in, 21 out per matrix).
  */
 int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode, double *d_logabs,
                    double *d_phase, int8_t *d_parity, int32_t *d_status, void *stream);

@@ -132,7 +132,12 @@ extern "C" int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode,
   if (rc) return rc;
   if (batch == 0) return LUFQHE_SUCCESS;
   cudaStream_t s = (cudaStream_t)stream;
-  const double2 *Z = reinterpret_cast<const double2 *>(d_z);
+  // page-locked host coordinates and results: their device views
+  const double2 *Z = reinterpret_cast<const double2 *>(device_address(d_z));
+  d_logabs = static_cast<double *>(const_cast<void *>(device_address(d_logabs)));
+  d_phase = static_cast<double *>(const_cast<void *>(device_address(d_phase)));
+  d_parity = static_cast<int8_t *>(const_cast<void *>(device_address(d_parity)));
+  d_status = static_cast<int32_t *>(const_cast<void *>(device_address(d_status)));
   switch (mode) {
     case LUFQHE_MODE_PLAIN_FP64:
       return launch_plain_lll(Z, n, batch, ARITH_REF, d_logabs, d_phase, d_parity, d_status, s);

@@ -79,18 +79,19 @@ def batch_lup_det(A, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | 
 
 
 def lll_det(z, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | None = None):
-    """Determinants of the LLL orbital matrices of (batch, n) complex128 CUDA
-    coordinates z, built inside the factorising kernels."""
+    """Determinants of the LLL orbital matrices of (batch, n) complex128
+    coordinates z, built inside the factorising kernels. z and out may be CUDA
+    tensors or page-locked host tensors (read and written over the host link)."""
     import torch
-    if z.dim() != 2 or z.dtype != torch.complex128 or not z.is_cuda or not z.is_contiguous():
-        raise TypeError("z must be a contiguous (batch, n) complex128 CUDA tensor")
+    if z.dim() != 2 or z.dtype != torch.complex128 or not z.is_contiguous() or \
+            not (z.is_cuda or z.is_pinned()):
+        raise TypeError("z must be a contiguous (batch, n) complex128 CUDA or pinned tensor")
     batch, n = z.shape
     if out is None:
         dev = z.device
-        out = DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
-                        torch.empty(batch, dtype=torch.float64, device=dev),
-                        torch.empty(batch, dtype=torch.int8, device=dev),
-                        torch.empty(batch, dtype=torch.int32, device=dev))
+        pin = not z.is_cuda
+        out = DetResult(*(torch.empty(batch, dtype=d, device=dev, pin_memory=pin)
+                          for d in (torch.float64, torch.float64, torch.int8, torch.int32)))
     rc = lib().lufqhe_lll_det(z.data_ptr(), n, batch, mode, out.logabs.data_ptr(),
                               out.phase.data_ptr(), out.parity.data_ptr(), out.status.data_ptr(),
                               _stream_ptr(stream))

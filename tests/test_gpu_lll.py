@@ -43,3 +43,18 @@ def test_lll_det_fp64_share_and_nonfinite(cuda, lufqhe_mod):
     assert (got["status"] == want["status"]).all()
     assert np.array_equal(got["logabs"], want["logabs"], equal_nan=True)
     assert ((got["status"] & lufqhe_mod.ST_FP64) != 0).mean() > 0.3
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_lll_det_on_host_buffers(cuda, lufqhe_mod, mode):
+    """Page-locked host coordinates and results (read and written over the
+    host link) give the device call's results bit for bit."""
+    A, z = lufqhe_mod.gen_lll(5000, 24, seed=77)
+    z = z.contiguous()
+    want = lufqhe_mod.lll_det(z, mode=mode)
+    zh = z.cpu().pin_memory()
+    got = lufqhe_mod.lll_det(zh, mode=mode)
+    cuda.cuda.synchronize()
+    for k in ("logabs", "phase", "parity", "status"):
+        a, b = getattr(got, k).numpy(), getattr(want, k).cpu().numpy()
+        assert (((a == b) | (np.isnan(a) & np.isnan(b))) if a.dtype.kind == "f" else a == b).all(), k
