@@ -21,6 +21,39 @@ constexpr int kMaxWarpsMixed = 8;
 // 5e-5 keeps that near 5e-11 relative, half the 1e-10 target.
 constexpr float kCorrRelCap = 5e-5f;
 
+// Packed FP32 pairs: one instruction for both components, each rounded
+// exactly as the scalar __fadd_rn / __fsub_rn / __fmul_rn / __fmaf_rn.
+__device__ __forceinline__ unsigned long long pk2(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 up2(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pk2(a)), "l"(pk2(b)), "l"(pk2(c)));
+  return up2(r);
+}
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk2(a)), "l"(pk2(b)));
+  return up2(r);
+}
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk2(a)), "l"(pk2(b)));
+  return up2(r);
+}
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk2(a)), "l"(pk2(b)));
+  return up2(r);
+}
+
 // ---- float-float building blocks (never contracted: explicit _rn ops) ------
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = __fadd_rn(a, b);
@@ -32,21 +65,27 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
   e = __fmaf_rn(a, b, -p);
 }
 
-// s + c -= l*u exactly up to the compensation's own rounding (Dot2 step).
+// s + c -= l*u exactly up to the compensation's own rounding (Dot2 step), the
+// real and imaginary parts side by side in packed pairs: sc.xy is the high
+// part, sc.zw the compensation. A = -(lx ux, lx uy), B = (ly uy, -ly ux) with
+// their exact product errors from FMAs, each added by TwoSum.
 __device__ __forceinline__ void dot2_csub(float4 &sc, float2 l, float2 u) {
-  float p1, e1, p2, e2, p3, e3, p4, e4, s, t1, t2;
-  two_prod(l.x, u.x, p1, e1);
-  two_prod(l.y, u.y, p2, e2);
-  two_prod(l.x, u.y, p3, e3);
-  two_prod(l.y, u.x, p4, e4);
-  // real: s - p1 + p2
-  two_sum(sc.x, -p1, s, t1);
-  two_sum(s, p2, sc.x, t2);
-  sc.z = __fadd_rn(sc.z, __fadd_rn(__fsub_rn(t1, e1), __fadd_rn(t2, e2)));
-  // imag: s - p3 - p4
-  two_sum(sc.y, -p3, s, t1);
-  two_sum(s, -p4, sc.y, t2);
-  sc.w = __fadd_rn(sc.w, __fsub_rn(__fadd_rn(t1, t2), __fadd_rn(e3, e4)));
+  const float2 lx = make_float2(l.x, l.x), lxn = make_float2(-l.x, -l.x);
+  const float2 lys = make_float2(l.y, -l.y), lysn = make_float2(-l.y, l.y);
+  const float2 us = make_float2(u.y, u.x);
+  const float2 A = f2mul(lxn, u);       // (-p1, -p3)
+  const float2 EA = f2fma(lx, u, A);    // (e1, e3), lx u = p + e
+  const float2 B = f2mul(lys, us);      // (p2, -p4)
+  const float2 EBn = f2fma(lysn, us, B);  // (-e2, e4)
+  const float2 hi = make_float2(sc.x, sc.y);
+  const float2 s1 = f2add(hi, A);
+  float2 bb = f2sub(s1, hi);
+  const float2 t1 = f2add(f2sub(hi, f2sub(s1, bb)), f2sub(A, bb));
+  const float2 s2 = f2add(s1, B);
+  bb = f2sub(s2, s1);
+  const float2 t2 = f2add(f2sub(s1, f2sub(s2, bb)), f2sub(B, bb));
+  const float2 lo = f2add(make_float2(sc.z, sc.w), f2add(f2sub(t1, EA), f2sub(t2, EBn)));
+  sc = make_float4(s2.x, s2.y, lo.x, lo.y);
 }
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
