@@ -394,7 +394,9 @@ def run_mixedn(args, world, rank, local):
                                        "count_above_1e-10": int((rel > 1e-10).sum())},
             "fallbacks": {"count": int(((mixed_st & 8) != 0).sum()), "of": total},
             "e2e": {"value": world * total / (ms_e2e * 1e-3), "unit": "dets/s",
-                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "call": "lufqhe_plan_execute on a plan over page-locked host buffers (the "
+                            "kernels read the matrices and write the results over the host link)"},
             "gpu_launches": launches,
             # the n=48 group (FP64 route, warp-group pass) takes most of the step:
             # its F.dets/s alone against the FP64 FMA peak; "step" is the whole
@@ -694,7 +696,9 @@ def run_ours(args):
             "fallbacks": {"count": fallback, "of": batch},
             "e2e": {"value": world * batch / (ms_e2e * 1e-3), "unit": "dets/s",
                     "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "call": "lufqhe_batch_lup_det_host on page-locked host buffers (mixed mode: "
+                            "the kernels read the matrices over the host link, no staging copies)"},
             "e2e_from_coordinates": e2e_coords,
             "gpu_launches": launches,
             "roofline": roof,
