@@ -125,7 +125,8 @@ def test_plan_large_sizes(cuda, lufqhe_mod, mode):
     plan.close()
 
 
-def test_plan_on_host_buffers(cuda, lufqhe_mod):
+@pytest.mark.parametrize("autotune", [False, True])
+def test_plan_on_host_buffers(cuda, lufqhe_mod, autotune):
     """A plan whose groups and outputs are page-locked host memory: the kernels
     read and write over the host link; results equal the device plan's bit
     for bit, and new host inputs at the same addresses are picked up."""
@@ -137,10 +138,19 @@ def test_plan_on_host_buffers(cuda, lufqhe_mod):
     hosts = [(A.cpu().pin_memory(), o) for A, o in groups]
     out_h = lufqhe_mod.DetResult(*(torch.empty(total, dtype=d, pin_memory=True)
                                    for d in (torch.float64, torch.float64, torch.int8, torch.int32)))
-    plan_h = lufqhe_mod.Plan(hosts, out_h, mode=lufqhe_mod.MODE_MIXED, autotune=False)
+    plan_h = lufqhe_mod.Plan(hosts, out_h, mode=lufqhe_mod.MODE_MIXED, autotune=autotune)
     plan_h.execute()
     torch.cuda.synchronize()
     want = host(out)
+    if autotune:
+        # the tuner may send a size to the FP64 routine (status FP64), so the
+        # bits can differ from the untuned device plan: check accuracy instead
+        la, ref = out_h.logabs.numpy(), want["logabs"]
+        ok = np.isfinite(ref)
+        assert (np.abs(la[ok] - ref[ok]) / np.maximum(1, np.abs(ref[ok]))).max() < 1e-9
+        plan.close()
+        plan_h.close()
+        return
     for k in ("logabs", "phase", "parity", "status"):
         a, b = getattr(out_h, k).numpy(), want[k]
         assert (((a == b) | (np.isnan(a) & np.isnan(b))) if a.dtype.kind == "f" else a == b).all(), k

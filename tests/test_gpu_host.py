@@ -44,7 +44,7 @@ def test_host_entry_repeated_calls_share_nothing(cuda, lufqhe_mod):
         assert np.array_equal(host_dict(o)["logabs"], want["logabs"], equal_nan=True)
 
 
-@pytest.mark.parametrize("n,batch", [(24, 6000), (16, 5000), (32, 3000)])
+@pytest.mark.parametrize("n,batch", [(24, 6000), (16, 5000), (32, 3000), (8, 4000), (48, 700)])
 @pytest.mark.parametrize("out_pinned", [True, False])
 def test_mixed_over_host_link(cuda, lufqhe_mod, n, batch, out_pinned):
     """Mixed mode on a pinned batch: the kernels read the matrices over the
@@ -64,4 +64,25 @@ def test_mixed_over_host_link(cuda, lufqhe_mod, n, batch, out_pinned):
     for k in ("logabs", "phase"):
         assert np.array_equal(got[k], want[k], equal_nan=True), k
     assert (got["parity"] == want["parity"]).all() and (got["status"] == want["status"]).all()
-    assert ((got["status"] & lufqhe_mod.ST_FALLBACK) != 0).any() or n < 24
+    assert ((got["status"] & lufqhe_mod.ST_FALLBACK) != 0).any() or n < 24 or n > 32
+
+
+def test_mixed_over_host_link_special_matrices(cuda, lufqhe_mod):
+    """Zero, singular, non-finite and tiny-scaled matrices in a pinned batch
+    read over the host link: the same results and status flags as the device
+    entry point."""
+    import torch
+    A, _ = lufqhe_mod.gen_lll(2000, 24, seed=31)
+    A[3] = 0                                  # zero matrix
+    A[10, 5] = A[10, 7]                       # two equal rows: singular
+    A[20, 2, 2] = float("nan")                # non-finite
+    A[30] *= 1e-30                            # rows below the reference's 1e-24 scale test
+    A[40, :, 4] = 0                           # a zero column
+    want = dev_dict(lufqhe_mod.batch_lup_det(A, mode=2))
+    out = lufqhe_mod.batch_lup_det_host(A.cpu().pin_memory(), mode=2)
+    cuda.cuda.synchronize()
+    got = host_dict(out)
+    for k in ("logabs", "phase"):
+        assert np.array_equal(got[k], want[k], equal_nan=True), k
+    assert (got["parity"] == want["parity"]).all() and (got["status"] == want["status"]).all()
+    assert got["status"][20] == lufqhe_mod.ST_NONFINITE
