@@ -9,9 +9,9 @@
 //     operations (48 significant bits kept);
 //  3. FP32 complex LUP of hi with partial pivoting on |Re|+|Im|; alongside,
 //     the residual R = P A^ - L U is accumulated exactly in float-float
-//     (Ogita-Rump-Oishi Dot2: TwoProd + TwoSum per real product), starting
-//     from hi + lo, so R carries FP64-level accuracy although every operation
-//     is an FP32 one;
+//     (Ogita-Rump-Oishi Dot2: TwoProd + TwoSum per real product, the real
+//     and imaginary parts as packed FP32 pairs), starting from hi + lo, so R
+//     carries FP64-level accuracy although every operation is an FP32 one;
 //  4. E = U^-1 L^-1 R by FP32 triangular solves;
 //  5. log det(I + E) by an unpivoted FP32 LU that keeps the identity implicit
 //     (only the small offsets are stored), log1p/atan2 of each pivot, or, for
@@ -32,14 +32,16 @@
 // the FP32 pass, in a second kernel on the same stream that has the whole GPU
 // (and the FP64 kernel's smaller shared-memory footprint): the FP32 pass
 // appends the index of a rejected matrix to a pending list in static device
-// memory, and the second kernel's warps claim the list's entries one at a
-// time. If the list is full, the n >= 24 kernels (which hold no FP64
+// memory, and the second kernel deals the list's entries out to its warps at
+// a fixed stride. If the list is full, the n >= 24 kernels (which hold no FP64
 // factorisation code) mark the matrix in logabs and the second kernel scans
 // for the marks; the others refactorise it in place. For n < 24 the FP64
 // refactorisations are cheap and rare enough that the second launch costs
-// more than it saves; there the FP32 pass does them in place. The kernels
-// take their matrices from a source: dense matrices in the reference layout,
-// or lowest-Landau-level orbital matrices built from particle coordinates.
+// more than it saves; there the FP32 pass does them in place, and so does the
+// n >= 24 variant that reads its batch over the host link (INPLACE). The
+// kernels take their matrices from a source: dense matrices in the reference
+// layout, or lowest-Landau-level orbital matrices built from particle
+// coordinates.
 
 #include <atomic>
 #include <cmath>
