@@ -294,6 +294,11 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
 /* Input bytes per chunk of lufqhe_batch_lup_det_host, in MiB (1..1024; default
  * 32). */
 #define LUFQHE_OPT_HOST_CHUNK_MB 4
+/* Mixed mode, n = 24 and 32: 1 (default) refines the back substitution of the
+ * matrices whose correction the FP32 solves cannot carry to 1e-10 but whose
+ * ||E||_F is within the threshold, in a pass of its own, before sending the
+ * rest to FP64; 0 sends them all to FP64. */
+#define LUFQHE_OPT_MIXED_REFINE 5
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "lufqhe_internal.cuh"
 
@@ -83,6 +84,47 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
 namespace lufqhe {
 
 // The batched kernels for one mode (arguments already checked).
+// The library's own stream-ordered memory pool, per device: blocks freed on
+// a stream stay in the pool for the next call instead of going back to the
+// driver at the next synchronisation (the default pool's release threshold
+// is 0, which made every first call after a synchronise map its memory again).
+int lib_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= 64) {
+    set_error("device %d out of range", dev);
+    return LUFQHE_ERR_CUDA;
+  }
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      rc = check_cuda(cudaMemPoolCreate(&pools[dev], &props), "cudaMemPoolCreate");
+      if (rc) {
+        pools[dev] = nullptr;
+        return rc;
+      }
+      unsigned long long keep = ~0ull;
+      rc = check_cuda(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep),
+                      "cudaMemPoolSetAttribute");
+      if (rc) return rc;
+    }
+    pool = pools[dev];
+  }
+  return check_cuda(cudaMallocFromPoolAsync(p, bytes, pool, s), "cudaMallocFromPoolAsync");
+}
+
+int lib_free_async(void *p, cudaStream_t s) {
+  return check_cuda(cudaFreeAsync(p, s), "cudaFreeAsync");
+}
+
 const void *device_address(const void *p) {
   if (!p) return p;
   cudaPointerAttributes a{};
@@ -201,6 +243,7 @@ extern float g_mixed_theta;
 extern int g_tile_warps;
 extern float g_fp64_share;
 extern int g_host_chunk_mb;
+extern int g_mixed_refine;
 }
 
 extern "C" int lufqhe_set_option(int option, double value) {
@@ -236,6 +279,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_host_chunk_mb = (int)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_MIXED_REFINE) {
+    if (!(value == 0.0 || value == 1.0)) {
+      set_error("lufqhe_set_option: refine must be 0 or 1");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_mixed_refine = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   set_error("lufqhe_set_option: unknown option %d", option);
   return LUFQHE_ERR_INVALID_ARG;
 }
@@ -245,6 +296,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_TILE_WARPS) return (double)g_tile_warps;
   if (option == LUFQHE_OPT_FP64_SHARE) return (double)g_fp64_share;
   if (option == LUFQHE_OPT_HOST_CHUNK_MB) return (double)g_host_chunk_mb;
+  if (option == LUFQHE_OPT_MIXED_REFINE) return (double)g_mixed_refine;
   return NAN;
 }
 

@@ -71,7 +71,7 @@ __host__ __device__ inline WarpLayout warp_layout(int nm, int nf) {
 template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int lane, float theta2,
-                               unsigned int share64k, int status_or, DeferredOut &out,
+                               bool refine, unsigned int share64k, int status_or, DeferredOut &out,
                                double *logabs, double *phase, int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
@@ -90,12 +90,12 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
     float2 corr;
     bool ok;
     switch (n) {
-      case 6: ok = mixed_factor_tile<6>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
-      case 8: ok = mixed_factor_tile<8>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
-      case 12: ok = mixed_factor_tile<12>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
-      case 16: ok = mixed_factor_tile<16>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
-      case 24: ok = mixed_factor_tile<24>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
-      case 32: ok = mixed_factor_tile<32>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par); break;
+      case 6: ok = mixed_factor_tile<6>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      case 8: ok = mixed_factor_tile<8>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      case 12: ok = mixed_factor_tile<12>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      case 16: ok = mixed_factor_tile<16>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      case 24: ok = mixed_factor_tile<24>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      case 32: ok = mixed_factor_tile<32>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
       default: {
         MixedSmem S;
         S.SC = HL;
@@ -138,7 +138,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nm,
                    int nf,
-                   float theta2, double *__restrict__ logabs, double *__restrict__ phase,
+                   float theta2, int refine, double *__restrict__ logabs, double *__restrict__ phase,
                    int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
@@ -164,15 +164,15 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, lane, theta2, w.share64k, w.status_or, out, logabs, phase, parity,
-                           status);
+                           ec, lane, theta2, refine != 0, w.share64k, w.status_or, out, logabs,
+                           phase, parity, status);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
 }
 
-using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, double *,
-                               double *, int8_t *, int32_t *);
+using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, int,
+                               double *, double *, int8_t *, int32_t *);
 
 GroupedKernel kernel_for(int mode) {
   switch (mode) {
@@ -195,11 +195,12 @@ int default_tile(int n) {
 template <int ARITH>
 __global__ void __launch_bounds__(kFp64GroupWarps * 32)
     grouped_group_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter,
-                         int nm, int nf, float theta2, double *__restrict__ logabs,
+                         int nm, int nf, float theta2, int refine, double *__restrict__ logabs,
                          double *__restrict__ phase, int8_t *__restrict__ parity,
                          int32_t *__restrict__ status) {
   (void)nm;
   (void)theta2;
+  (void)refine;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long red[3 * kFp64GroupWarps];
   __shared__ unsigned int item;
@@ -285,6 +286,7 @@ struct lufqhe_plan_s {
   int8_t *parity = nullptr;
   int32_t *status = nullptr;
   float theta2 = 0.01f;
+  int refine = 1;  // in-place refinement of the tile path (option 5)
   // per-group tile size and FP64 share (1/65536) chosen by the tuner
   std::vector<int> tile;
   std::vector<unsigned int> share;
@@ -440,6 +442,7 @@ int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
     const int grid = (int)std::min<long long>(L.ctas, want);
     k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
+                                                       p->refine,
                                                        p->logabs, p->phase, p->parity, p->status);
     rc = check_cuda(cudaGetLastError(), "grouped_kernel launch");
   }
@@ -581,6 +584,7 @@ void destroy_plan(lufqhe_plan_s *p) {
 
 namespace lufqhe {
 extern float g_mixed_theta;
+extern int g_mixed_refine;
 }
 
 extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *groups, int ngroups,
@@ -604,6 +608,7 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   p->parity = static_cast<int8_t *>(const_cast<void *>(device_address(d_parity)));
   p->status = static_cast<int32_t *>(const_cast<void *>(device_address(d_status)));
   p->theta2 = g_mixed_theta * g_mixed_theta;
+  p->refine = g_mixed_refine;
   for (int g = 0; g < ngroups; ++g) {
     const lufqhe_group_t &G = groups[g];
     if (G.count < 0 || G.n < 1 || G.lda < G.n || G.out_offset < 0 || (G.count > 0 && !G.A) ||

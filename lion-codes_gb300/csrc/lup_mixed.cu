@@ -43,6 +43,7 @@
 // layout, or lowest-Landau-level orbital matrices built from particle
 // coordinates.
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <type_traits>
@@ -52,6 +53,7 @@
 namespace lufqhe {
 
 int g_tile_warps = 0;
+extern int g_mixed_refine;  // refinement pass for n >= 24 (option 5)
 float g_fp64_share = -1.0f;  // < 0: per-n default
 
 // Share of matrices routed straight to FP64, per n, in 1/65536 units. The
@@ -158,6 +160,56 @@ __device__ __forceinline__ void release_slot(int slot, int lane) {
   }
 }
 
+// Matrices the FP32 pass leaves for a refinement of the back substitution
+// (TILE_REFINE): per matrix a header and the warp's L\U and Y = L^-1 R as they
+// lie in shared memory (row stride N + 1), in a call-local device buffer that
+// starts with three counters {saved, claimed, spare}.
+struct RefineHead {
+  long long b;
+  int exp_sum, par, prod_e, pad;
+  float xh, xl, yh, yl;
+};
+constexpr size_t kRefineHeadBytes = 256;  // the counters, before entry 0
+template <int N>
+constexpr size_t refine_entry_bytes() {
+  return (sizeof(RefineHead) + 2 * (size_t)N * (N + 1) * sizeof(float2) + 15) & ~(size_t)15;
+}
+// Share of a batch the refinement buffer has room for (the rest go straight
+// to the FP64 pass): on lowest-Landau-level n = 24 matrices about 9% qualify.
+constexpr double kRefineShare = 0.25;
+
+// Save a TILE_REFINE matrix; false (warp-uniform) if the buffer is full.
+template <int N>
+__device__ bool save_refine(unsigned char *buf, long long cap, long long b, const float2 *F,
+                            const float2 *Rm, const CFF &prod, int exp_sum, int par, int lane) {
+  constexpr int NL = N * (N + 1);
+  unsigned long long k = 0;
+  if (lane == 0) k = atomicAdd(reinterpret_cast<unsigned long long *>(buf), 1ull);
+  k = __shfl_sync(kFull, k, 0);
+  if (k >= (unsigned long long)cap) return false;
+  unsigned char *e = buf + kRefineHeadBytes + k * refine_entry_bytes<N>();
+  float2 *dF = reinterpret_cast<float2 *>(e + sizeof(RefineHead));
+  float2 *dY = dF + NL;
+  for (int q = lane; q < NL; q += 32) {
+    dF[q] = F[q];
+    dY[q] = Rm[q];
+  }
+  if (lane == 0) {
+    RefineHead h;
+    h.b = b;
+    h.exp_sum = exp_sum;
+    h.par = par;
+    h.prod_e = prod.e;
+    h.pad = 0;
+    h.xh = prod.xh;
+    h.xl = prod.xl;
+    h.yh = prod.yh;
+    h.yl = prod.yl;
+    *reinterpret_cast<RefineHead *>(e) = h;
+  }
+  return true;
+}
+
 template <class Src>
 __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     lup_mixed_kernel(Src src, int n, long long batch,
@@ -213,6 +265,7 @@ template <int N, class Src, bool INPLACE = false>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     lup_mixed_tile_kernel(Src src, long long batch, float theta2,
                           unsigned int share64k, int slot, int pslot, double2 *spill,
+                          unsigned char *refine, long long refine_cap,
                           double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
@@ -269,18 +322,85 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     CFF prod;
     int exp_sum, par;
     float2 corr;
-    if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par))
-      out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else if constexpr (DEFER)
-      defer_fp64_always(pslot, b, lane, false, logabs);
-    else if constexpr (INPLACE)
-      fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
-                                           logabs, phase, parity, status);
-    else
-      fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
+    if constexpr (DEFER) {
+      const int code =
+          mixed_factor_tile_ex<N, true>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
+      if (code == TILE_ACCEPT)
+        out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
+      // a matrix within theta but above the FP32 solves' cap gets its back
+      // substitution refined in the next pass, if the buffer has room
+      else if (!(code == TILE_REFINE && refine &&
+                 save_refine<N>(refine, refine_cap, b, F, reinterpret_cast<const float2 *>(HL),
+                                prod, exp_sum, par, lane)))
+        defer_fp64_always(pslot, b, lane, false, logabs);
+    } else {
+      // in place: the refinement (refine_cap != 0), then FP64 (n < 24, where
+      // both are rare, and the host-link variant, which has compute to spare)
+      if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par,
+                               refine_cap != 0))
+        out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
+      else if constexpr (INPLACE)
+        fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
+                                             logabs, phase, parity, status);
+      else
+        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
+    }
   }
   out.flush(lane, logabs, phase, parity, status);
   release_slot(slot, lane);
+}
+
+// The refinement pass (n >= 24): warps claim the saved matrices, reload
+// their L\U and Y into the FP32 pass's shared-memory layout and refine the
+// back substitution (mixed_refine_tile). Accepted ones get their results
+// here; the others go on to the FP64 pass's list.
+template <int N>
+__global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
+    lup_mixed_refine_kernel(const unsigned char *refine, long long refine_cap, float theta2,
+                            int pslot, double *__restrict__ logabs, double *__restrict__ phase,
+                            int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LDS = N + 1;
+  constexpr size_t NL = (size_t)N * LDS;
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  unsigned char *base = smem_raw;
+  float2 *Rm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(base) + warp * NL);
+  float2 *Eb = Rm + NL;
+  base += warps * NL * sizeof(float4);
+  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
+  base += warps * NL * sizeof(float2);
+  base += warps * 2 * (size_t)N * sizeof(double);
+  float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
+  unsigned long long *ctr =
+      reinterpret_cast<unsigned long long *>(const_cast<unsigned char *>(refine));
+  const unsigned long long saved = min(*(volatile unsigned long long *)ctr,
+                                       (unsigned long long)refine_cap);
+  DeferredOut out;
+  for (;;) {
+    unsigned long long k = saved;
+    if (lane == 0 && *(volatile unsigned long long *)(ctr + 1) < saved) k = atomicAdd(ctr + 1, 1ull);
+    k = __shfl_sync(kFull, k, 0);
+    if (k >= saved) break;
+    const unsigned char *e = refine + kRefineHeadBytes + k * refine_entry_bytes<N>();
+    const RefineHead h = *reinterpret_cast<const RefineHead *>(e);
+    const float2 *sF = reinterpret_cast<const float2 *>(e + sizeof(RefineHead));
+    const float2 *sY = sF + NL;
+    __syncwarp();
+    for (int q = lane; q < (int)NL; q += 32) {
+      F[q] = __ldcg(sF + q);
+      Rm[q] = __ldcg(sY + q);
+    }
+    __syncwarp();
+    const CFF prod = {h.xh, h.xl, h.yh, h.yl, h.prod_e};
+    float2 corr;
+    if (mixed_refine_tile<N>(F, Rm, Eb, diag, lane, theta2, tile_la_est(prod, h.exp_sum), corr))
+      out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
+    else
+      defer_fp64_always(pslot, h.b, lane, false, logabs);
+  }
+  out.flush(lane, logabs, phase, parity, status);
 }
 
 // The FP64 pass: one CTA per SM; its warps refactorise the pending list's
@@ -415,7 +535,20 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
   const int pslot = N >= kDeferMinN && !inplace ? next_pend_slot() : -1;
+  // the refinement pass's buffer (n >= 24, device batches)
+  unsigned char *refine = nullptr;
+  long long refine_cap = 0;
+  if (pslot >= 0 && g_mixed_refine) {
+    refine_cap = std::max<long long>(256, (long long)(kRefineShare * (double)batch));
+    refine_cap = std::min<long long>(refine_cap, batch);
+    rc = lib_malloc_async((void **)&refine, kRefineHeadBytes + (size_t)refine_cap * refine_entry_bytes<N>(),
+                          stream);
+    if (!rc)
+      rc = check_cuda(cudaMemsetAsync(refine, 0, kRefineHeadBytes, stream), "memset(refine)");
+    if (rc) return rc;
+  }
   double2 *spill = nullptr;
+  if (!refine) refine_cap = g_mixed_refine;  // in-place kernels: the refinement on or off
   if (inplace) {
     rc = check_cuda(cudaMallocAsync((void **)&spill, (size_t)grid * warps * N * N * sizeof(double2),
                                     stream),
@@ -423,8 +556,26 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     if (rc) return rc;
   }
   kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), next_work_slot(),
-                                           pslot, spill, logabs, phase, parity, status);
+                                           pslot, spill, refine, refine_cap, logabs, phase, parity,
+                                           status);
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
+  if (!rc && refine) {
+    if constexpr (N >= kDeferMinN) {
+      auto rk = lup_mixed_refine_kernel<N>;
+      rc = check_cuda(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
+                      "cudaFuncSetAttribute(mixed refine)");
+      if (!rc) {
+        rk<<<grid, warps * 32, smem, stream>>>(refine, refine_cap, theta2, pslot, logabs, phase,
+                                               parity, status);
+        rc = check_cuda(cudaGetLastError(), "lup_mixed_refine_kernel launch");
+      }
+    }
+  }
+  if (refine) {
+    const int r2 = lib_free_async(refine, stream);
+    if (!rc) rc = r2;
+  }
   if (spill) {
     const int r2 = check_cuda(cudaFreeAsync(spill, stream), "cudaFreeAsync(mixed spill)");
     if (!rc) rc = r2;
@@ -442,6 +593,7 @@ size_t mixed_smem_per_warp(int n) {
 }
 
 float g_mixed_theta = 0.1f;
+int g_mixed_refine = 1;
 
 namespace {
 

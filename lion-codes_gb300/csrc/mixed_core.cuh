@@ -20,6 +20,12 @@ constexpr int kMaxWarpsMixed = 8;
 // (measured on lowest-Landau-level matrices against a double-double oracle);
 // 5e-5 keeps that near 5e-11 relative, half the 1e-10 target.
 constexpr float kCorrRelCap = 5e-5f;
+// The same cap after one refinement step of the back substitution
+// (mixed_refine_tile): an emulation of the method on lowest-Landau-level
+// matrices against a double-double oracle puts the error left in
+// log det(I + E) at about 1.2e-7 ||E||_F at most, so 3e-4 keeps it near
+// 4e-11 relative; above max(1, |log|det||) ~ 300 the absolute cap theta binds.
+constexpr float kRefinedRelCap = 3e-4f;
 
 // Packed FP32 pairs: one instruction for both components, each rounded
 // exactly as the scalar __fadd_rn / __fsub_rn / __fmul_rn / __fmaf_rn.
@@ -639,6 +645,60 @@ __device__ __forceinline__ void residual_rows(float4 *HL, const float2 *F, int l
   }
 }
 
+// The residual of the back substitution E1 = U^-1 Y, G = Y - U E1, in
+// float-float for the NA row slots from A0 of the 4 x 8 lane grid, written
+// over Y in Rm (each lane reads and writes only the entries it owns there; E1
+// is read from Eb by all lanes). The same Dot2 steps as residual_rows; U is
+// the upper triangle of F, so row i sums over j >= i.
+template <int N, int NA>
+__device__ __forceinline__ void refine_rows(float2 *Rm, const float2 *F, const float2 *Eb,
+                                            int lane, int A0) {
+  constexpr int LDS = N + 1;
+  constexpr int SB = TileGeom<N>::SB;
+  if constexpr (NA > 0) {
+    const int tr = lane >> 3, tc = lane & 7;
+    float4 acc[NA][SB];
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * (A0 + a) + tr, k = 8 * b + tc;
+        const float2 y = (i < N && k < N) ? Rm[i * LDS + k] : make_float2(0.f, 0.f);
+        acc[a][b] = make_float4(y.x, y.y, 0.f, 0.f);
+      }
+#pragma unroll 1
+    for (int j = 4 * A0; j < N; ++j) {
+      float2 Uv[NA], Ev[SB];
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        const int i = 4 * (A0 + a) + tr;
+        Uv[a] = (i <= j) ? F[i * LDS + j] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int k = 8 * b + tc;
+        Ev[b] = k < N ? Eb[j * LDS + k] : make_float2(0.f, 0.f);
+      }
+      // slots whose rows all lie below j have nothing to add
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        if (4 * (A0 + a) > j) continue;
+#pragma unroll
+        for (int b = 0; b < SB; ++b) dot2_csub(acc[a][b], Uv[a], Ev[b]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < SB; ++b) {
+        const int i = 4 * (A0 + a) + tr, k = 8 * b + tc;
+        if (i < N && k < N)
+          Rm[i * LDS + k] = make_float2(__fadd_rn(acc[a][b].x, acc[a][b].z),
+                                        __fadd_rn(acc[a][b].y, acc[a][b].w));
+      }
+  }
+}
+
 __device__ __forceinline__ float2 shfl2(float2 v, int src) {
   return make_float2(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src));
 }
@@ -656,24 +716,54 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
 //    never read after step t, so the update runs over whole slots without
 //    masks; the pivots 1 + d_t go to `diag` and their logs are taken one per
 //    lane at the end.
+// Outcome of the tile path for one matrix.
+enum { TILE_REJECT = 0, TILE_ACCEPT = 1, TILE_REFINE = 2 };
+
 template <int N>
-__device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int lane,
-                                  float theta2, int exp_sum, CFF &prod, float2 &corr) {
-  constexpr int LDS = N + 1;
-  constexpr int SA = (N + 3) / 4;
-  constexpr int SB = (N + 7) / 8;
+struct TileRegs {
+  static constexpr int LDS = N + 1;
+  static constexpr int SA = (N + 3) / 4;
+  static constexpr int SB = (N + 7) / 8;
+};
+
+// This lane's entries of an N x N float2 array (row stride N + 1) to or from
+// registers on the lane grid; entries outside the matrix read as zero.
+template <int N>
+__device__ __forceinline__ void tile_load(const float2 *Rm, float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
+                                          int lane) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
   const int r = lane >> 3, c = lane & 7;
-  const float2 zero = make_float2(0.f, 0.f);
-  float2 Y[SA][SB];
 #pragma unroll
   for (int a = 0; a < SA; ++a)
 #pragma unroll
     for (int b = 0; b < SB; ++b) {
       const int i = 4 * a + r, k = 8 * b + c;
-      Y[a][b] = (i < N && k < N) ? Rm[i * LDS + k] : zero;
+      Y[a][b] = (i < N && k < N) ? Rm[i * LDS + k] : make_float2(0.f, 0.f);
     }
+}
+template <int N>
+__device__ __forceinline__ void tile_store(float2 *Rm,
+                                           const float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
+                                           int lane) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  const int r = lane >> 3, c = lane & 7;
+#pragma unroll
+  for (int a = 0; a < SA; ++a)
+#pragma unroll
+    for (int b = 0; b < SB; ++b) {
+      const int i = 4 * a + r, k = 8 * b + c;
+      if (i < N && k < N) Rm[i * LDS + k] = Y[a][b];
+    }
+}
 
-  // 4a. Y = L^-1 R (unit lower)
+// 4a. Y = L^-1 Y (unit lower) in place on the lane grid.
+template <int N>
+__device__ __forceinline__ void tile_fwd_solve(const float2 *F,
+                                               float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
+                                               int lane) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  const int r = lane >> 3, c = lane & 7;
+  const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
   for (int s = 0; s < SA; ++s) {
 #pragma unroll 1
@@ -701,7 +791,17 @@ __device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int
       }
     }
   }
-  // 4b. E = U^-1 Y: row t is scaled by 1/u_tt, then removed from the rows above
+}
+
+// 4b. E = U^-1 Y in place: row t is scaled by 1/u_tt, then removed from the
+// rows above.
+template <int N>
+__device__ __forceinline__ void tile_bwd_solve(const float2 *F,
+                                               float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
+                                               int lane) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  const int r = lane >> 3, c = lane & 7;
+  const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
   for (int s = SA - 1; s >= 0; --s) {
 #pragma unroll 1
@@ -732,42 +832,53 @@ __device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int
       }
     }
   }
+}
 
-  // 6 (first half). complex float-float product of the diagonal of U
-  {
-    CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
-    if (lane < N) {
-      const float2 u = F[lane * LDS + lane];
-      CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
-      ff_renorm(v);
-      acc = ff_cmul(acc, v);
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
-    prod = shfl_cff(acc, 0, false);
+// 6 (first half). Complex float-float product of the diagonal of U.
+template <int N>
+__device__ __forceinline__ CFF tile_diag_product(const float2 *F, int lane) {
+  constexpr int LDS = N + 1;
+  CFF acc = {1.0f, 0.0f, 0.0f, 0.0f, 0};
+  if (lane < N) {
+    const float2 u = F[lane * LDS + lane];
+    CFF v = {u.x, 0.0f, u.y, 0.0f, 0};
+    ff_renorm(v);
+    acc = ff_cmul(acc, v);
   }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) acc = ff_cmul(acc, shfl_cff(acc, off, true));
+  return shfl_cff(acc, 0, false);
+}
 
-  // acceptance (as in mixed_finish), decided on lane 0's sum
-  bool series;
-  {
-    float f = 0.0f;
+// ||E||_F^2, summed on lane 0's order and broadcast.
+template <int N>
+__device__ __forceinline__ float tile_frob2(const float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB]) {
+  constexpr int SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  float f = 0.0f;
 #pragma unroll
-    for (int a = 0; a < SA; ++a)
+  for (int a = 0; a < SA; ++a)
 #pragma unroll
-      for (int b = 0; b < SB; ++b) f = __fmaf_rn(Y[a][b].x, Y[a][b].x, __fmaf_rn(Y[a][b].y, Y[a][b].y, f));
+    for (int b = 0; b < SB; ++b) f = __fmaf_rn(Y[a][b].x, Y[a][b].x, __fmaf_rn(Y[a][b].y, Y[a][b].y, f));
 #pragma unroll
-    for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
-    f = __shfl_sync(kFull, f, 0);
-    const float la_est = fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
-    const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
-    if (!(f <= theta2) || !(f <= rel_cap * rel_cap)) return false;
-    // Small E: log det(I + E) = tr E - tr(E^2)/2 + r with |r| <= ||E||_F^3 / (3 (1 - ||E||_F)).
-    // Take the two terms when that bound is below 1e-12 max(1, |log|det||) (la_est is
-    // within 1 of |log|det|| here, so la_est - 1 is a safe lower bound).
-    const float nf = sqrtf(f);
-    series = nf * f <= 3e-12f * fmaxf(1.0f, la_est - 1.0f) * (1.0f - nf);
-  }
-  if (series) {
+  for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
+  return __shfl_sync(kFull, f, 0);
+}
+
+// 5. log det(I + E) for an accepted E (||E||_F^2 = f). Small E: the series
+// tr E - tr(E^2)/2 + r with |r| <= ||E||_F^3 / (3 (1 - ||E||_F)), taken when
+// that bound is below 1e-12 max(1, |log|det||) (la_est is within 1 of
+// |log|det|| here, so la_est - 1 is a safe lower bound). Otherwise the
+// unpivoted elimination of I + E on the lane grid, its pivots 1 + d_t to
+// `diag` and their logs taken one per lane.
+template <int N>
+__device__ __forceinline__ void tile_logdet_ipe(float2 *Rm, float2 *diag,
+                                                float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
+                                                int lane, float f, float la_est, float2 &corr) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  const int r = lane >> 3, c = lane & 7;
+  const float2 zero = make_float2(0.f, 0.f);
+  const float nf = sqrtf(f);
+  if (nf * f <= 3e-12f * fmaxf(1.0f, la_est - 1.0f) * (1.0f - nf)) {
     // tr E: entry (t, t) sits in slot (t / 4, t / 8) of lane (t % 4, t % 8), so slot a
     // holds a diagonal entry in the lanes with c = 4 (a % 2) + r
     float2 tr = zero, t2 = zero;
@@ -779,13 +890,7 @@ __device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int
       }
     // tr(E^2) = sum_ik E_ik E_ki, the transposed entries through shared memory
     __syncwarp();
-#pragma unroll
-    for (int a = 0; a < SA; ++a)
-#pragma unroll
-      for (int b = 0; b < SB; ++b) {
-        const int i = 4 * a + r, k = 8 * b + c;
-        if (i < N && k < N) Rm[i * LDS + k] = Y[a][b];
-      }
+    tile_store<N>(Rm, Y, lane);
     __syncwarp();
 #pragma unroll
     for (int a = 0; a < SA; ++a)
@@ -807,10 +912,8 @@ __device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int
     }
     corr = make_float2(__shfl_sync(kFull, __fmaf_rn(-0.5f, t2.x, tr.x), 0),
                        __shfl_sync(kFull, __fmaf_rn(-0.5f, t2.y, tr.y), 0));
-    return true;
+    return;
   }
-
-  // 5. log det(I + E)
 #pragma unroll
   for (int s = 0; s < SA; ++s) {
     const int q = s >> 1;  // column slot of t = 4s + u (compile-time)
@@ -847,12 +950,92 @@ __device__ bool mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int
     cim += __shfl_xor_sync(kFull, cim, off);
   }
   corr = make_float2(__shfl_sync(kFull, cre, 0), __shfl_sync(kFull, cim, 0));
+}
+
+__device__ __forceinline__ float tile_la_est(const CFF &prod, int exp_sum) {
+  return fabsf((float)(prod.e + exp_sum)) * 0.6931472f;
+}
+
+// Steps 4-6 of the tile path with E in registers on the 4 x 8 lane grid of
+// the residual (lane (r, c) holds entries (4a + r, 8b + c)). Every element
+// update is the same cfms / cmulf as in mixed_finish, so E and log det(I + E)
+// come out bit for bit as there; only the order of the ||E||_F sum differs.
+//  * Step t = 4s + u of a solve or of the elimination: the outer loop over the
+//    row slot s is unrolled, the inner loop over u is not, so register indices
+//    are compile-time while the code stays small. Row t lives in lanes (u, *)
+//    at slot s and reaches the other lanes by shuffle; l_it and u_it are
+//    shared-memory reads that 8 lanes share.
+//  * log det(I + E): unpivoted elimination. Rows and columns up to t are
+//    never read after step t, so the update runs over whole slots without
+//    masks.
+// REFINE: a matrix whose ||E||_F is within theta but above the relative cap
+// returns TILE_REFINE with Y = L^-1 R left in Rm (for a refinement of the back
+// substitution elsewhere); without it such a matrix is rejected.
+template <int N, bool REFINE>
+__device__ int mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int lane, float theta2,
+                                 int exp_sum, CFF &prod, float2 &corr) {
+  float2 Y[TileRegs<N>::SA][TileRegs<N>::SB];
+  tile_load<N>(Rm, Y, lane);
+  tile_fwd_solve<N>(F, Y, lane);
+  if constexpr (REFINE) tile_store<N>(Rm, Y, lane);  // own entries only
+  tile_bwd_solve<N>(F, Y, lane);
+  prod = tile_diag_product<N>(F, lane);
+  const float f = tile_frob2<N>(Y);
+  const float la_est = tile_la_est(prod, exp_sum);
+  if (!(f <= theta2)) return TILE_REJECT;
+  const float rel_cap = kCorrRelCap * fmaxf(1.0f, la_est);
+  if (!(f <= rel_cap * rel_cap)) return REFINE ? TILE_REFINE : TILE_REJECT;
+  tile_logdet_ipe<N>(Rm, diag, Y, lane, f, la_est, corr);
+  return TILE_ACCEPT;
+}
+
+// One refinement step of the back substitution for a matrix the FP32 pass
+// left as TILE_REFINE: F holds L\U, Rm holds Y = L^-1 R, Eb is N (N + 1)
+// float2 of scratch. E1 = U^-1 Y in FP32; the residual G = Y - U E1 in
+// float-float (the LU residual's Dot2 steps); E = E1 + U^-1 G. Against the
+// double-double oracle the error left in log det(I + E) is then about
+// 1.2e-7 ||E||_F at most on lowest-Landau-level matrices, so the relative cap
+// is kRefinedRelCap instead of kCorrRelCap. True if accepted (corr set).
+template <int N>
+__device__ bool mixed_refine_tile(const float2 *F, float2 *Rm, float2 *Eb, float2 *diag, int lane,
+                                  float theta2, float la_est, float2 &corr) {
+  constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
+  float2 Y[SA][SB];
+  tile_load<N>(Rm, Y, lane);
+  tile_bwd_solve<N>(F, Y, lane);
+  tile_store<N>(Eb, Y, lane);
+  __syncwarp();
+  if constexpr (SA % 2 == 0) {
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) refine_rows<N, SA / 2>(Rm, F, Eb, lane, h * (SA / 2));
+  } else {
+    refine_rows<N, SA / 2>(Rm, F, Eb, lane, 0);
+    refine_rows<N, SA - SA / 2>(Rm, F, Eb, lane, SA / 2);
+  }
+  tile_load<N>(Rm, Y, lane);  // G, own entries
+  tile_bwd_solve<N>(F, Y, lane);
+  const int r = lane >> 3, c = lane & 7;
+#pragma unroll
+  for (int a = 0; a < SA; ++a)
+#pragma unroll
+    for (int b = 0; b < SB; ++b) {
+      const int i = 4 * a + r, k = 8 * b + c;
+      if (i < N && k < N) {
+        const float2 e1 = Eb[i * LDS + k];
+        Y[a][b] = make_float2(__fadd_rn(e1.x, Y[a][b].x), __fadd_rn(e1.y, Y[a][b].y));
+      }
+    }
+  const float f = tile_frob2<N>(Y);
+  if (!(f <= theta2)) return false;
+  const float rel_cap = kRefinedRelCap * fmaxf(1.0f, la_est);
+  if (!(f <= rel_cap * rel_cap)) return false;
+  tile_logdet_ipe<N>(Rm, diag, Y, lane, f, la_est, corr);
   return true;
 }
 
-template <int N>
-__device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane, float theta2,
-                                  CFF &prod, int &exp_sum, float2 &corr, int &par) {
+template <int N, bool REFINE = false>
+__device__ int mixed_factor_tile_ex(float4 *HL, float2 *F, int *er, int *ec, int lane,
+                                    float theta2, CFF &prod, int &exp_sum, float2 &corr, int &par) {
   constexpr int LDS = TileGeom<N>::LDS;
   constexpr int SA = TileGeom<N>::SA;
   constexpr int SB = TileGeom<N>::SB;
@@ -917,7 +1100,7 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
       }
       key = __reduce_max_sync(kFull, key);
       const float best = __uint_as_float(key & ~31u);
-      if (!(best > 0.0f) || !(best < INFINITY)) return false;  // zero/NaN/Inf pivot
+      if (!(best > 0.0f) || !(best < INFINITY)) return TILE_REJECT;  // zero/NaN/Inf pivot
       const int bi = 31 - (int)(key & 31u);
       if (bi != t) {
         if (lane < N) {
@@ -977,8 +1160,24 @@ __device__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int l
 
   // 5-6. solves, acceptance, log det(I + E) and the diagonal product
   // (the exponent arrays are free again: they hold the pivots of step 5)
-  return mixed_finish_tile<N>(F, Rm, reinterpret_cast<float2 *>(er), lane, theta2, exp_sum, prod,
-                              corr);
+  return mixed_finish_tile<N, REFINE>(F, Rm, reinterpret_cast<float2 *>(er), lane, theta2, exp_sum,
+                                      prod, corr);
+}
+
+// Tile path for kernels that keep their FP64 refactorisations in place: a
+// TILE_REFINE matrix has its back substitution refined right here (refine
+// true), so the outcome is the batched call's (FP32 pass, refinement pass).
+template <int N>
+__device__ __forceinline__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane,
+                                                  float theta2, CFF &prod, int &exp_sum,
+                                                  float2 &corr, int &par, bool refine) {
+  const int code =
+      mixed_factor_tile_ex<N, true>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
+  if (code == TILE_ACCEPT) return true;
+  if (code != TILE_REFINE || !refine) return false;
+  float2 *Rm = reinterpret_cast<float2 *>(HL);
+  return mixed_refine_tile<N>(F, Rm, Rm + N * (N + 1), reinterpret_cast<float2 *>(er), lane, theta2,
+                              tile_la_est(prod, exp_sum), corr);
 }
 
 template <int N>

@@ -128,7 +128,7 @@ size_t serve_smem_per_warp(int n, bool fp64_only) {
 template <int NC>
 __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
     serve_kernel(const ServeTile *ring, const unsigned int *published, const unsigned int *stop,
-                 ClassCtl *ctl, int mode, float theta2, unsigned int share64k) {
+                 ClassCtl *ctl, int mode, float theta2, unsigned int share64k, int refine) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = NC + 1;
   constexpr size_t NL = (size_t)NC * LDS;
@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
         float2 corr;
         bool ok;
         if constexpr (NC <= 32) {
-          ok = mixed_factor_tile<NC>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
+          ok = mixed_factor_tile<NC>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par,
+                                     refine != 0);
         } else {
           MixedSmem S;
           S.SC = HL;
@@ -301,9 +302,10 @@ template <int NC>
 __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
     serve_group_kernel(const ServeTile *ring, const unsigned int *published,
                        const unsigned int *stop, ClassCtl *ctl, int mode, float theta2,
-                       unsigned int share64k) {
+                       unsigned int share64k, int refine) {
   (void)theta2;
   (void)share64k;
+  (void)refine;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = NC + 1;
   constexpr size_t NL = (size_t)NC * LDS;
@@ -394,7 +396,7 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
 }
 
 using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
-                             ClassCtl *, int, float, unsigned int);
+                             ClassCtl *, int, float, unsigned int, int);
 
 ServeKernel serve_group_kernel_for(int n) {
   switch (n) {
@@ -475,6 +477,7 @@ struct lufqhe_server_s {
   int max_k = 4096;
   int tile = 8;
   float theta2 = 0.01f;
+  int refine = 1;  // in-place refinement of the tile path (option 5)
   std::vector<SClass> classes;
   // HBM pool with a first-fit free list
   unsigned char *pool = nullptr;
@@ -549,7 +552,7 @@ int ensure_running(lufqhe_server_s *s, SClass &c) {
   // (the shared memory of an FP64-only class holds no FP32 arrays, so the
   // share is the one fixed when the class was created)
   c.kern<<<c.grid, c.warps * 32, c.smem, c.stream>>>(c.ring_d, c.pub_d, s->stop_d, c.ctl, s->mode,
-                                                     s->theta2, c.share64k);
+                                                     s->theta2, c.share64k, s->refine);
   int rc = check_cuda(cudaGetLastError(), "serve kernel launch");
   if (rc) return rc;
   c.running = true;
@@ -593,6 +596,7 @@ int host_mapped(T **h, T **d, size_t count, const char *what) {
 
 namespace lufqhe {
 extern float g_mixed_theta;
+extern int g_mixed_refine;
 }
 
 extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
@@ -612,6 +616,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
   s->max_k = max_k;
   s->tile = tile;
   s->theta2 = g_mixed_theta * g_mixed_theta;
+  s->refine = g_mixed_refine;
   s->slots.resize(kReqSlots);
   int rc = LUFQHE_SUCCESS;
   const int sms = device_sm_count();

@@ -219,3 +219,25 @@ def test_concurrent_calls_on_two_streams(cuda, lufqhe_mod):
         got, w = host(o), want[i % 3]
         assert np.array_equal(got["logabs"], w["logabs"], equal_nan=True)
         assert (got["status"] == w["status"]).all() and (got["parity"] == w["parity"]).all()
+
+
+@pytest.mark.parametrize("n", [24, 32])
+def test_refinement_pass(cuda, lufqhe_mod, oracle, n):
+    """n = 24 and 32: matrices whose correction the FP32 solves cannot carry to
+    1e-10 get their back substitution refined in a pass of their own; far
+    fewer then need the FP64 kernel, and every accepted result stays within
+    1e-10 of the double-double oracle. Option 5 = 0 restores the two-pass
+    behaviour."""
+    lib = lufqhe_mod.lib()
+    A, _ = lufqhe_mod.gen_lll(3000, n, seed=90 + n)
+    old = lib.lufqhe_get_option(5)
+    try:
+        lib.lufqhe_set_option(5, 0.0)
+        off = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+        lib.lufqhe_set_option(5, 1.0)
+        on = check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.5)
+    finally:
+        lib.lufqhe_set_option(5, old)
+    fb_off = int(((off["status"] & lufqhe_mod.ST_FALLBACK) != 0).sum())
+    fb_on = int(((on["status"] & lufqhe_mod.ST_FALLBACK) != 0).sum())
+    assert fb_on < 0.7 * fb_off, (fb_on, fb_off)
