@@ -68,10 +68,10 @@ def mixed_fp32_ops_per_matrix(n: int) -> float:
 
 def mixed_launches_per_call(n: int) -> int:
     """Kernels one mixed-mode batched call launches: the FP32 pass, plus for
-    n = 24 and n = 32 the refinement pass and the FP64 refactorisation pass
-    (other n > 24 go straight to the FP64 kernel, n < 24 refines and
-    refactorises inside the FP32 pass)."""
-    return 3 if n in (24, 32) else 1
+    n = 24 and n = 32 the kernel that refines the saved matrices and
+    refactorises the rejected ones in FP64 (other n > 24 go straight to the
+    FP64 kernel, n < 24 refines and refactorises inside the FP32 pass)."""
+    return 2 if n in (24, 32) else 1
 
 
 def host_chunks(n: int, lda: int, batch: int, chunk_mb: int = 32) -> int:

@@ -28,17 +28,22 @@
 // Warps take matrices from a work counter rather than a fixed grid stride: a
 // matrix refactorised in FP64 costs many times an accepted one, and a fixed
 // share of the batch per warp would leave the kernel waiting on the warps
-// that drew the most of them. The FP64 refactorisations themselves run after
-// the FP32 pass, in a second kernel on the same stream that has the whole GPU
-// (and the FP64 kernel's smaller shared-memory footprint): the FP32 pass
-// appends the index of a rejected matrix to a pending list in static device
-// memory, and the second kernel deals the list's entries out to its warps at
-// a fixed stride. If the list is full, the n >= 24 kernels (which hold no FP64
-// factorisation code) mark the matrix in logabs and the second kernel scans
-// for the marks; the others refactorise it in place. For n < 24 the FP64
+// that drew the most of them. For n >= 24 the refinements and FP64
+// refactorisations run after the FP32 pass, in a second kernel on the same
+// stream that has the whole GPU: the FP32 pass saves a matrix whose
+// correction is within theta but beyond what FP32 solves carry (its L\U and
+// Y = L^-1 R) for one refinement step of the back substitution, and appends
+// the index of a rejected matrix to a pending list in static device memory;
+// the second kernel deals the list's entries out to its warps at a fixed
+// stride for FP64 while the other warps refine the saved matrices, so the FP64
+// and FP32 pipes work side by side. If the list is full, the n >= 24 FP32
+// kernels (which hold no FP64 factorisation code) mark the matrix in logabs
+// and the second kernel scans for the marks; the others refactorise it in
+// place. For n < 24 the FP64
 // refactorisations are cheap and rare enough that the second launch costs
-// more than it saves; there the FP32 pass does them in place, and so does the
-// n >= 24 variant that reads its batch over the host link (INPLACE). The
+// more than it saves; there the FP32 pass refines and refactorises in place,
+// and so does the n >= 24 variant that reads its batch over the host link
+// (INPLACE). The
 // kernels take their matrices from a source: dense matrices in the reference
 // layout, or lowest-Landau-level orbital matrices built from particle
 // coordinates.
@@ -53,7 +58,7 @@
 namespace lufqhe {
 
 int g_tile_warps = 0;
-extern int g_mixed_refine;  // refinement pass for n >= 24 (option 5)
+extern int g_mixed_refine;  // refinement of the back substitution (option 5)
 float g_fp64_share = -1.0f;  // < 0: per-n default
 
 // Share of matrices routed straight to FP64, per n, in 1/65536 units. The
@@ -350,14 +355,19 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   release_slot(slot, lane);
 }
 
-// The refinement pass (n >= 24): warps claim the saved matrices, reload
-// their L\U and Y into the FP32 pass's shared-memory layout and refine the
-// back substitution (mixed_refine_tile). Accepted ones get their results
-// here; the others go on to the FP64 pass's list.
-template <int N>
+// The passes after the FP32 pass, as one kernel in the FP32 pass's
+// shared-memory layout (n >= 24): the FP64 refactorisations of the matrices
+// the FP32 pass rejected, dealt out at a fixed stride over the grid's warps
+// first, while the warps without one refine the saved matrices (claimed one at
+// a time; a refinement that fails is refactorised in FP64 on the spot). The
+// FP64 pipe and the FP32 pipes then work side by side instead of one pass
+// after the other. Matrices past a full pending list are found in chunks of
+// 32 whose logabs the FP32 pass marked. The last CTA out empties the list.
+template <int N, class Src>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
-    lup_mixed_refine_kernel(const unsigned char *refine, long long refine_cap, float theta2,
-                            int pslot, double *__restrict__ logabs, double *__restrict__ phase,
+    lup_mixed_finish_kernel(Src src, long long batch, const unsigned char *refine,
+                            long long refine_cap, float theta2, int slot, int pslot,
+                            double *__restrict__ logabs, double *__restrict__ phase,
                             int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = N + 1;
@@ -366,41 +376,93 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   unsigned char *base = smem_raw;
-  float2 *Rm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(base) + warp * NL);
-  float2 *Eb = Rm + NL;
+  float4 *HL = reinterpret_cast<float4 *>(base) + warp * NL;
+  double2 *M = reinterpret_cast<double2 *>(HL);
+  float2 *Rm = reinterpret_cast<float2 *>(HL);
   base += warps * NL * sizeof(float4);
   float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
   base += warps * NL * sizeof(float2);
+  double *hold = reinterpret_cast<double *>(base) + warp * 2 * N;
   base += warps * 2 * (size_t)N * sizeof(double);
   float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
-  unsigned long long *ctr =
-      reinterpret_cast<unsigned long long *>(const_cast<unsigned char *>(refine));
-  const unsigned long long saved = min(*(volatile unsigned long long *)ctr,
-                                       (unsigned long long)refine_cap);
+  __shared__ unsigned int cta_done;
+  if (threadIdx.x == 0) cta_done = 0u;
+  __syncthreads();
+  // 1. the FP32 pass's rejections, dealt out
+  const unsigned long long listed =
+      min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
+  const unsigned long long chunks =
+      *(volatile unsigned int *)&g_pend_over[pslot] ? (unsigned long long)(batch + 31) / 32 : 0ull;
+  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
+  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
+       j += stride) {
+    const unsigned int e = g_pend[pslot][j];
+    const long long b = e & ~kPendRouted;
+    fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+  }
+  // 2. the saved matrices, claimed; a failed refinement is refactorised here
   DeferredOut out;
-  for (;;) {
-    unsigned long long k = saved;
-    if (lane == 0 && *(volatile unsigned long long *)(ctr + 1) < saved) k = atomicAdd(ctr + 1, 1ull);
-    k = __shfl_sync(kFull, k, 0);
-    if (k >= saved) break;
-    const unsigned char *e = refine + kRefineHeadBytes + k * refine_entry_bytes<N>();
-    const RefineHead h = *reinterpret_cast<const RefineHead *>(e);
-    const float2 *sF = reinterpret_cast<const float2 *>(e + sizeof(RefineHead));
-    const float2 *sY = sF + NL;
-    __syncwarp();
-    for (int q = lane; q < (int)NL; q += 32) {
-      F[q] = __ldcg(sF + q);
-      Rm[q] = __ldcg(sY + q);
+  if (refine) {
+    unsigned long long *ctr =
+        reinterpret_cast<unsigned long long *>(const_cast<unsigned char *>(refine));
+    const unsigned long long saved =
+        min(*(volatile unsigned long long *)ctr, (unsigned long long)refine_cap);
+    for (;;) {
+      unsigned long long k = saved;
+      if (lane == 0 && *(volatile unsigned long long *)(ctr + 1) < saved)
+        k = atomicAdd(ctr + 1, 1ull);
+      k = __shfl_sync(kFull, k, 0);
+      if (k >= saved) break;
+      const unsigned char *e = refine + kRefineHeadBytes + k * refine_entry_bytes<N>();
+      const RefineHead h = *reinterpret_cast<const RefineHead *>(e);
+      const float2 *sF = reinterpret_cast<const float2 *>(e + sizeof(RefineHead));
+      const float2 *sY = sF + NL;
+      __syncwarp();
+      for (int q = lane; q < (int)NL; q += 32) {
+        F[q] = __ldcg(sF + q);
+        Rm[q] = __ldcg(sY + q);
+      }
+      __syncwarp();
+      const CFF prod = {h.xh, h.xl, h.yh, h.yl, h.prod_e};
+      float2 corr;
+      if (mixed_refine_tile<N>(F, Rm, Rm + NL, diag, lane, theta2, tile_la_est(prod, h.exp_sum),
+                               corr))
+        out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
+      else
+        fallback_fp64_src(src, h.b, N, M, LDS, hold, lane, h.b, logabs, phase, parity, status);
     }
-    __syncwarp();
-    const CFF prod = {h.xh, h.xl, h.yh, h.yl, h.prod_e};
-    float2 corr;
-    if (mixed_refine_tile<N>(F, Rm, Eb, diag, lane, theta2, tile_la_est(prod, h.exp_sum), corr))
-      out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
-    else
-      defer_fp64_always(pslot, h.b, lane, false, logabs);
   }
   out.flush(lane, logabs, phase, parity, status);
+  // 3. past a full list: chunks of 32 matrices, claimed
+  for (;;) {
+    if (chunks == 0) break;
+    unsigned long long j = chunks;
+    if (lane == 0) j = atomicAdd(&g_work[slot][0], 1ull);
+    j = __shfl_sync(kFull, j, 0);
+    if (j >= chunks) break;
+    const long long b0 = (long long)j * 32;
+    long long bits = 0;
+    if (b0 + lane < batch) bits = __double_as_longlong(logabs[b0 + lane]);
+    const unsigned int routed = __ballot_sync(kFull, bits == kOverRoutedBits);
+    unsigned int mask = __ballot_sync(kFull, bits == kOverFallbackBits) | routed;
+    while (mask) {
+      const int q = __ffs(mask) - 1;
+      mask &= mask - 1u;
+      const long long b = b0 + q;
+      fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                        (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+    }
+  }
+  // one release per CTA: the last CTA out empties the list and the counter
+  if (lane == 0 && atomicAdd(&cta_done, 1u) == (unsigned int)warps - 1u) {
+    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
+      atomicExch(&g_work[slot][0], 0ull);
+      atomicExch(&g_work[slot][1], 0ull);
+      atomicExch(&g_pend_count[pslot], 0u);
+      atomicExch(&g_pend_over[pslot], 0u);
+    }
+  }
 }
 
 // The FP64 pass: one CTA per SM; its warps refactorise the pending list's
@@ -535,7 +597,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
   const int pslot = N >= kDeferMinN && !inplace ? next_pend_slot() : -1;
-  // the refinement pass's buffer (n >= 24, device batches)
+  // the saved matrices for the refinement after the FP32 pass (n >= 24)
   unsigned char *refine = nullptr;
   long long refine_cap = 0;
   if (pslot >= 0 && g_mixed_refine) {
@@ -559,16 +621,18 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
                                            pslot, spill, refine, refine_cap, logabs, phase, parity,
                                            status);
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
-  if (!rc && refine) {
+  // the refinements and the FP64 refactorisations, side by side in one kernel
+  if (!rc && pslot >= 0) {
     if constexpr (N >= kDeferMinN) {
-      auto rk = lup_mixed_refine_kernel<N>;
-      rc = check_cuda(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      auto fk = lup_mixed_finish_kernel<N, Src>;
+      rc = check_cuda(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
-                      "cudaFuncSetAttribute(mixed refine)");
+                      "cudaFuncSetAttribute(mixed finish)");
       if (!rc) {
-        rk<<<grid, warps * 32, smem, stream>>>(refine, refine_cap, theta2, pslot, logabs, phase,
-                                               parity, status);
-        rc = check_cuda(cudaGetLastError(), "lup_mixed_refine_kernel launch");
+        fk<<<grid, warps * 32, smem, stream>>>(src, batch, refine, refine_cap, theta2,
+                                               next_work_slot(), pslot, logabs, phase, parity,
+                                               status);
+        rc = check_cuda(cudaGetLastError(), "lup_mixed_finish_kernel launch");
       }
     }
   }
@@ -580,8 +644,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     const int r2 = check_cuda(cudaFreeAsync(spill, stream), "cudaFreeAsync(mixed spill)");
     if (!rc) rc = r2;
   }
-  if (rc || pslot < 0) return rc;
-  return launch_fallback(src, N, batch, pslot, logabs, phase, parity, status, stream);
+  return rc;
 }
 
 }  // namespace

@@ -1166,7 +1166,7 @@ __device__ int mixed_factor_tile_ex(float4 *HL, float2 *F, int *er, int *ec, int
 
 // Tile path for kernels that keep their FP64 refactorisations in place: a
 // TILE_REFINE matrix has its back substitution refined right here (refine
-// true), so the outcome is the batched call's (FP32 pass, refinement pass).
+// true), so the outcome is the batched call's (FP32 pass, then refinement).
 template <int N>
 __device__ __forceinline__ bool mixed_factor_tile(float4 *HL, float2 *F, int *er, int *ec, int lane,
                                                   float theta2, CFF &prod, int &exp_sum,

@@ -22,9 +22,9 @@ def test_bytes_and_launch_accounting():
     # 32 MiB chunks of 24 x 24 complex128 matrices: 3640 per chunk
     assert bench.host_chunks(24, 24, 32768) == 10
     assert bench.host_chunks(8, 8, 1) == 1
-    assert [bench.mixed_launches_per_call(n) for n in (8, 16, 24, 32, 48)] == [1, 1, 3, 3, 1]
+    assert [bench.mixed_launches_per_call(n) for n in (8, 16, 24, 32, 48)] == [1, 1, 2, 2, 1]
     assert bench.host_launches_per_call(24, 24, 32768, 2, True) == 1
-    assert bench.host_launches_per_call(24, 24, 32768, 2, False) == 30
+    assert bench.host_launches_per_call(24, 24, 32768, 2, False) == 20
     assert bench.host_launches_per_call(24, 24, 32768, 1, True) == 10
     # the FP32 lane operations of the mixed method grow like n^3 and are dominated by the residual
     ops24 = bench.mixed_fp32_ops_per_matrix(24)
