@@ -794,21 +794,25 @@ __device__ __forceinline__ void tile_fwd_solve(const float2 *F,
 }
 
 // 4b. E = U^-1 Y in place: row t is scaled by 1/u_tt, then removed from the
-// rows above.
+// rows above. The reciprocals of the diagonal are taken first, one per lane,
+// into `rdiag` (N float2 of scratch).
 template <int N>
 __device__ __forceinline__ void tile_bwd_solve(const float2 *F,
                                                float2 (&Y)[TileRegs<N>::SA][TileRegs<N>::SB],
-                                               int lane) {
+                                               float2 *rdiag, int lane) {
   constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
   const int r = lane >> 3, c = lane & 7;
   const float2 zero = make_float2(0.f, 0.f);
+  __syncwarp();
+  if (lane < N) rdiag[lane] = crcpf(F[lane * LDS + lane]);
+  __syncwarp();
 #pragma unroll
   for (int s = SA - 1; s >= 0; --s) {
 #pragma unroll 1
     for (int u = 3; u >= 0; --u) {
       const int t = 4 * s + u;
       if (t >= N) continue;
-      const float2 dinv = crcpf(F[t * LDS + t]);
+      const float2 dinv = rdiag[t];
       float2 et[SB];
 #pragma unroll
       for (int b = 0; b < SB; ++b) {
@@ -978,7 +982,7 @@ __device__ int mixed_finish_tile(const float2 *F, float2 *Rm, float2 *diag, int 
   tile_load<N>(Rm, Y, lane);
   tile_fwd_solve<N>(F, Y, lane);
   if constexpr (REFINE) tile_store<N>(Rm, Y, lane);  // own entries only
-  tile_bwd_solve<N>(F, Y, lane);
+  tile_bwd_solve<N>(F, Y, diag, lane);
   prod = tile_diag_product<N>(F, lane);
   const float f = tile_frob2<N>(Y);
   const float la_est = tile_la_est(prod, exp_sum);
@@ -1002,7 +1006,7 @@ __device__ bool mixed_refine_tile(const float2 *F, float2 *Rm, float2 *Eb, float
   constexpr int LDS = N + 1, SA = TileRegs<N>::SA, SB = TileRegs<N>::SB;
   float2 Y[SA][SB];
   tile_load<N>(Rm, Y, lane);
-  tile_bwd_solve<N>(F, Y, lane);
+  tile_bwd_solve<N>(F, Y, diag, lane);
   tile_store<N>(Eb, Y, lane);
   __syncwarp();
   if constexpr (SA % 2 == 0) {
@@ -1013,7 +1017,7 @@ __device__ bool mixed_refine_tile(const float2 *F, float2 *Rm, float2 *Eb, float
     refine_rows<N, SA - SA / 2>(Rm, F, Eb, lane, SA / 2);
   }
   tile_load<N>(Rm, Y, lane);  // G, own entries
-  tile_bwd_solve<N>(F, Y, lane);
+  tile_bwd_solve<N>(F, Y, diag, lane);
   const int r = lane >> 3, c = lane & 7;
 #pragma unroll
   for (int a = 0; a < SA; ++a)
