@@ -108,6 +108,16 @@ __device__ __forceinline__ float2 crcpf(float2 u) {
   float rd = __frcp_rn(__fmaf_rn(u.x, u.x, u.y * u.y));
   return make_float2(u.x * rd, -u.y * rd);
 }
+// 1/u from the hardware's approximate reciprocal (about an ulp, subnormal
+// |u|^2 flushed to zero, which gives a non-finite multiplier and so a
+// rejection): for the FP32 LUP of the tile path, whose multipliers need not be
+// correctly rounded because the float-float residual is exact for whatever L
+// and U come out. The solves and the elimination of I + E keep crcpf.
+__device__ __forceinline__ float2 crcpf_approx(float2 u) {
+  float rd;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rd) : "f"(__fmaf_rn(u.x, u.x, u.y * u.y)));
+  return make_float2(u.x * rd, -u.y * rd);
+}
 
 // Unbiased exponent field of the larger of |re|, |im| (-2000 for zero/subnormal).
 __device__ __forceinline__ int cexp_field(double2 v) {
@@ -1118,7 +1128,7 @@ __device__ int mixed_factor_tile_ex(float4 *HL, float2 *F, int *er, int *ec, int
         par ^= 1;
       }
       __syncwarp();
-      const float2 rp = crcpf(F[t * LDS + t]);
+      const float2 rp = crcpf_approx(F[t * LDS + t]);
       if (lane > t && lane < N) F[lane * LDS + t] = cmulf(F[lane * LDS + t], rp);
       __syncwarp();
       if (t + 1 < N) {
