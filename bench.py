@@ -593,6 +593,22 @@ def run_ours(args):
     ms_e2e = max_over_ranks(world, e2.elapsed_time(e3) / args.steps)
     launches += args.steps * host_launches_per_call(n, n, batch, mode, A_host.is_pinned())
 
+    # the host link this box gives a plain copy of the same pinned batch (the
+    # e2e ceiling; it differs from box to box)
+    link_buf = torch.empty_like(A)
+    link_ms = []
+    for _ in range(3):
+        l0 = torch.cuda.Event(enable_timing=True)
+        l1 = torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        with torch.cuda.stream(stream):
+            link_buf.copy_(A_host, non_blocking=True)
+        l1.record(stream)
+        torch.cuda.synchronize()
+        link_ms.append(l0.elapsed_time(l1))
+    link_gbs = h2d / (min(link_ms) * 1e-3) * 1e-9
+    del link_buf
+
     # ---- e2e from particle coordinates (LLL workloads) ---------------------
     # what a Monte Carlo driver holds is z, not the matrices: H2D of the
     # coordinates, lufqhe_lll_det (matrices built inside the kernels), D2H of
@@ -699,7 +715,9 @@ def run_ours(args):
                     "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "call": "lufqhe_batch_lup_det_host on page-locked host buffers (mixed mode: "
-                            "the kernels read the matrices over the host link, no staging copies)"},
+                            "the kernels read the matrices over the host link, no staging copies)",
+                    "host_link_copy_gbs": link_gbs,
+                    "fraction_of_link": (h2d / (ms_e2e * 1e-3) * 1e-9) / link_gbs},
             "e2e_from_coordinates": e2e_coords,
             "gpu_launches": launches,
             "roofline": roof,
