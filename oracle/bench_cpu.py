@@ -1,6 +1,6 @@
 """CPU baseline legs of bench.py: the reference's CPU Crout path (its FP64
 restatement in liblufqhe_oracle.so, literal arithmetic) timed on the host
-cores with OpenMP over matrices, as SURVEY-style baseline only.
+cores with OpenMP over matrices, reported beside the GPU figures as a baseline only.
 
 TEST/BASELINE INFRASTRUCTURE: imported by bench.py's cpu_baseline leg and its
 `--impl reference` arm, nowhere else in the product.
