@@ -39,14 +39,12 @@
 // and FP32 pipes work side by side. If the list is full, the n >= 24 FP32
 // kernels (which hold no FP64 factorisation code) mark the matrix in logabs
 // and the second kernel scans for the marks; the others refactorise it in
-// place. For n < 24 the FP64
-// refactorisations are cheap and rare enough that the second launch costs
-// more than it saves; there the FP32 pass refines and refactorises in place,
-// and so does the n >= 24 variant that reads its batch over the host link
-// (INPLACE). The
-// kernels take their matrices from a source: dense matrices in the reference
-// layout, or lowest-Landau-level orbital matrices built from particle
-// coordinates.
+// place. For n < 24 the FP64 refactorisations are cheap and rare enough that
+// the second launch costs more than it saves; there the FP32 pass refines and
+// refactorises in place, and so does the n >= 24 variant that reads its batch
+// over the host link (INPLACE). The kernels take their matrices from a source:
+// dense matrices in the reference layout, or lowest-Landau-level orbital
+// matrices built from particle coordinates.
 
 #include <algorithm>
 #include <atomic>
@@ -168,7 +166,7 @@ __device__ __forceinline__ void release_slot(int slot, int lane) {
 // Matrices the FP32 pass leaves for a refinement of the back substitution
 // (TILE_REFINE): per matrix a header and the warp's L\U and Y = L^-1 R as they
 // lie in shared memory (row stride N + 1), in a call-local device buffer that
-// starts with three counters {saved, claimed, spare}.
+// starts with two 64-bit counters {saved, claimed}.
 struct RefineHead {
   long long b;
   int exp_sum, par, prod_e, pad;
