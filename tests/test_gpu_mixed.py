@@ -241,3 +241,13 @@ def test_refinement_pass(cuda, lufqhe_mod, oracle, n):
     fb_off = int(((off["status"] & lufqhe_mod.ST_FALLBACK) != 0).sum())
     fb_on = int(((on["status"] & lufqhe_mod.ST_FALLBACK) != 0).sum())
     assert fb_on < 0.7 * fb_off, (fb_on, fb_off)
+
+
+@pytest.mark.parametrize("n,batch,seed", [(24, 32768, 2), (32, 16384, 3), (16, 32768, 4)])
+def test_full_size_lll_against_double_double(cuda, lufqhe_mod, oracle, n, batch, seed):
+    """The full config-3 batch (and full-size n = 16, 32 LLL batches): every
+    matrix the mixed path accepts, refined ones included, is within 1e-10
+    (relative to max(1, |log|det||)) of the double-double oracle in log|det|
+    and phase; the FP64 ones carry the fused FP64 kernel's bits."""
+    A, _ = lufqhe_mod.gen_lll(batch, n, seed=seed)
+    check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.2)
