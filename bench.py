@@ -762,7 +762,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lll24", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-sample", type=int, default=8192)
+    # the reference arm factorises the whole batch every step (about 15 ms on
+    # 16 cores at n = 24): short steps let OpenMP start-up and box noise skew it
+    ap.add_argument("--ref-sample", type=int, default=32768)
     ap.add_argument("--serve-requests", type=int, default=4000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
