@@ -309,7 +309,11 @@ double lufqhe_get_option(int option);
 int lufqhe_probe_fma_peak(int kind, double *tflops, void *stream);
 
 /* ---- misc ---- */
-/* Bytes of device workspace a call needs (0 for the batched entry points). */
+/* Bytes of device memory a lufqhe_batch_lup_det call of this n, batch and mode
+ * takes, stream-ordered, from the library's own memory pool while it runs
+ * (mixed mode at n = 24 and 32: the matrices saved for the refinement of the
+ * back substitution, room for a quarter of the batch; 0 otherwise). The pool
+ * keeps freed blocks for the next call. */
 size_t lufqhe_workspace_bytes(int n, long long batch, int mode);
 /* Text for the last error on the calling host thread. */
 const char *lufqhe_last_error(void);

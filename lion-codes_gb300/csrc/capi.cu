@@ -226,7 +226,7 @@ extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, 
   // them in the matrices themselves (element (0,0)), which is also the output here.
   void *tmp = nullptr;
   size_t bytes = (size_t)n_mat * (2 * sizeof(double) + sizeof(int32_t));
-  int rc = check_cuda(cudaMallocAsync(&tmp, bytes, s), "cudaMallocAsync");
+  int rc = lib_malloc_async(&tmp, bytes, s);
   if (rc) return rc;
   double *la = static_cast<double *>(tmp);
   double *ph = la + n_mat;
@@ -234,7 +234,7 @@ extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, 
   double2 *A = reinterpret_cast<double2 *>(d_matrices);
   rc = launch_plain(A, A, mat_side, load_size, n_mat, ARITH_REF, la, ph, nullptr, st, s);
   if (!rc) rc = launch_write_det(A, mat_side, load_size, n_mat, la, ph, st, pair_product, s);
-  int rc2 = check_cuda(cudaFreeAsync(tmp, s), "cudaFreeAsync");
+  int rc2 = lib_free_async(tmp, s);
   return rc ? rc : rc2;
 }
 
@@ -301,10 +301,8 @@ extern "C" double lufqhe_get_option(int option) {
 }
 
 extern "C" size_t lufqhe_workspace_bytes(int n, long long batch, int mode) {
-  (void)n;
-  (void)batch;
-  (void)mode;
-  return 0;
+  if (n < 1 || batch < 0) return 0;
+  return mode == LUFQHE_MODE_MIXED ? mixed_workspace_bytes(n, batch) : 0;
 }
 
 extern "C" const char *lufqhe_last_error(void) { return g_err; }

@@ -23,8 +23,8 @@
 // engine while a chunk is factorised, and one chunk's kernels fill the tail of
 // another's, so the link (about 210 GB/s host-to-device on GB300) stays busy. The
 // caller's stream is forked into the two streams at entry and joined at exit;
-// staging memory comes from cudaMallocAsync on the caller's stream and is
-// freed there after the join.
+// staging memory comes from the library's stream-ordered pool on the caller's
+// stream and is freed there after the join.
 
 #include <mutex>
 
@@ -93,10 +93,8 @@ int det_over_link(const double2 *dA, int n, int lda, long long batch, double *h_
   // pageable outputs: device results, then copies
   const size_t nb = (size_t)batch;
   unsigned char *buf = nullptr;
-  int rc = check_cuda(cudaMallocAsync((void **)&buf, nb * (2 * sizeof(double) + sizeof(int32_t) +
-                                                          sizeof(int8_t)),
-                                      s),
-                      "cudaMallocAsync(results)");
+  int rc = lib_malloc_async((void **)&buf,
+                            nb * (2 * sizeof(double) + sizeof(int32_t) + sizeof(int8_t)), s);
   if (rc) return rc;
   double *dla = reinterpret_cast<double *>(buf);
   double *dph = dla + nb;
@@ -116,7 +114,7 @@ int det_over_link(const double2 *dA, int n, int lda, long long batch, double *h_
   if (!rc && h_parity)
     rc = check_cuda(cudaMemcpyAsync(h_parity, dpa, nb * sizeof(int8_t), cudaMemcpyDeviceToHost, s),
                     "D2H parity");
-  const int r2 = check_cuda(cudaFreeAsync(buf, s), "cudaFreeAsync(results)");
+  const int r2 = lib_free_async(buf, s);
   return rc ? rc : r2;
 }
 
@@ -167,7 +165,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   const size_t out_bytes = (size_t)per_chunk * (2 * sizeof(double) + sizeof(int8_t) + sizeof(int32_t));
   const size_t buf_bytes = ((in_bytes + 255) & ~(size_t)255) + ((out_bytes + 255) & ~(size_t)255);
   unsigned char *stage = nullptr;
-  rc = check_cuda(cudaMallocAsync((void **)&stage, buf_bytes * nbuf, user), "cudaMallocAsync(stage)");
+  rc = lib_malloc_async((void **)&stage, buf_bytes * nbuf, user);
   if (rc) return rc;
 
   cudaEvent_t fork = nullptr, done[kPipe] = {};
@@ -220,7 +218,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
     if (!r2) r2 = check_cuda(cudaStreamWaitEvent(user, done[i], 0), "join wait");
     if (!rc) rc = r2;
   }
-  int r3 = check_cuda(cudaFreeAsync(stage, user), "cudaFreeAsync(stage)");
+  int r3 = lib_free_async(stage, user);
   if (!rc) rc = r3;
   if (fork) cudaEventDestroy(fork);
   for (int i = 0; i < kPipe; ++i)

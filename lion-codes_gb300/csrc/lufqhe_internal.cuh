@@ -24,6 +24,8 @@ const void *device_address(const void *p);
 // Stream-ordered device memory from the library's own pool.
 int lib_malloc_async(void **p, size_t bytes, cudaStream_t s);
 int lib_free_async(void *p, cudaStream_t s);
+// Bytes a batched mixed call of this n and batch takes from that pool.
+size_t mixed_workspace_bytes(int n, long long batch);
 
 // ---- IEEE helpers ----------------------------------------------------------
 __device__ __forceinline__ bool finite_d(double v) {

@@ -610,9 +610,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   double2 *spill = nullptr;
   if (!refine) refine_cap = g_mixed_refine;  // in-place kernels: the refinement on or off
   if (inplace) {
-    rc = check_cuda(cudaMallocAsync((void **)&spill, (size_t)grid * warps * N * N * sizeof(double2),
-                                    stream),
-                    "cudaMallocAsync(mixed spill)");
+    rc = lib_malloc_async((void **)&spill, (size_t)grid * warps * N * N * sizeof(double2), stream);
     if (rc) return rc;
   }
   kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), next_work_slot(),
@@ -639,7 +637,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     if (!rc) rc = r2;
   }
   if (spill) {
-    const int r2 = check_cuda(cudaFreeAsync(spill, stream), "cudaFreeAsync(mixed spill)");
+    const int r2 = lib_free_async(spill, stream);
     if (!rc) rc = r2;
   }
   return rc;
@@ -655,6 +653,17 @@ size_t mixed_smem_per_warp(int n) {
 
 float g_mixed_theta = 0.1f;
 int g_mixed_refine = 1;
+
+// Device memory a batched mixed call takes from the library's pool while it
+// runs: the states saved for the refinement (n = 24 and 32, device batches).
+size_t mixed_workspace_bytes(int n, long long batch) {
+  if (!g_mixed_refine || fp64_share_64k(n) >= 65536u || batch == 0) return 0;
+  long long cap = std::max<long long>(256, (long long)(kRefineShare * (double)batch));
+  cap = std::min<long long>(cap, batch);
+  if (n == 24) return kRefineHeadBytes + (size_t)cap * refine_entry_bytes<24>();
+  if (n == 32) return kRefineHeadBytes + (size_t)cap * refine_entry_bytes<32>();
+  return 0;
+}
 
 namespace {
 

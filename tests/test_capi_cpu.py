@@ -129,3 +129,17 @@ def test_read_reference_file_format(lufqhe_mod, tmp_path):
     B = lufqhe_mod.read_matrices_f32(p, 16, first=5, count=10, lda=32)   # short tail
     assert B.shape == (2, 16, 32) and (B[:, :, :16] == M[5:].astype(np.complex128)).all()
     assert (B[:, :, 16:] == 0).all()
+
+
+def test_workspace_bytes(lufqhe_mod):
+    """Mixed mode at n = 24 and 32 takes room for a quarter of the batch of
+    saved matrices (header 40 B + L\\U and Y at row stride n + 1, 16-byte
+    aligned) plus 256 B of counters; other sizes and modes take nothing."""
+    lib = lufqhe_mod.lib()
+    entry24 = (40 + 2 * 24 * 25 * 8 + 15) // 16 * 16
+    assert lib.lufqhe_workspace_bytes(24, 32768, 2) == 256 + 8192 * entry24
+    entry32 = (40 + 2 * 32 * 33 * 8 + 15) // 16 * 16
+    assert lib.lufqhe_workspace_bytes(32, 1000, 2) == 256 + 256 * entry32
+    assert lib.lufqhe_workspace_bytes(16, 32768, 2) == 0
+    assert lib.lufqhe_workspace_bytes(24, 32768, 1) == 0
+    assert lib.lufqhe_workspace_bytes(24, 0, 2) == 0
