@@ -2,7 +2,7 @@
 restatement in liblufqhe_oracle.so, literal arithmetic) timed on the host
 cores with OpenMP over matrices, reported beside the GPU figures as a baseline only.
 
-TEST/BASELINE INFRASTRUCTURE: imported by bench.py's cpu_baseline leg and its
+TEST INFRASTRUCTURE (the CPU-side checker and timing arm): imported by bench.py's cpu_baseline leg and its
 `--impl reference` arm, nowhere else in the product.
 """
 from __future__ import annotations
