@@ -315,6 +315,12 @@ int lufqhe_probe_fma_peak(int kind, double *tflops, void *stream);
  * back substitution, room for a quarter of the batch; 0 otherwise). The pool
  * keeps freed blocks for the next call. */
 size_t lufqhe_workspace_bytes(int n, long long batch, int mode);
+/* Return the library pool's unused device memory to the driver, on every
+ * device the library has used. Blocks still held by work in flight stay
+ * until it completes: synchronise the streams the library ran on first to
+ * give everything back. Later calls allocate again as needed. No counterpart
+ * in the reference, whose calls take no workspace. */
+int lufqhe_release_workspace(void);
 /* Text for the last error on the calling host thread. */
 const char *lufqhe_last_error(void);
 /* Library version as "major.minor.patch". */

@@ -83,14 +83,19 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
 
 namespace lufqhe {
 
-// The batched kernels for one mode (arguments already checked).
 // The library's own stream-ordered memory pool, per device: blocks freed on
 // a stream stay in the pool for the next call instead of going back to the
 // driver at the next synchronisation (the default pool's release threshold
 // is 0, which made every first call after a synchronise map its memory again).
+// lufqhe_release_workspace trims them.
+namespace {
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+}  // namespace
+
 int lib_malloc_async(void **p, size_t bytes, cudaStream_t s) {
-  static std::mutex mu;
-  static cudaMemPool_t pools[64] = {};
+  std::mutex &mu = g_pool_mu;
+  cudaMemPool_t *pools = g_pools;
   int dev = 0;
   int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (rc) return rc;
@@ -298,6 +303,16 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_HOST_CHUNK_MB) return (double)g_host_chunk_mb;
   if (option == LUFQHE_OPT_MIXED_REFINE) return (double)g_mixed_refine;
   return NAN;
+}
+
+extern "C" int lufqhe_release_workspace(void) {
+  std::lock_guard<std::mutex> lock(lufqhe::g_pool_mu);
+  for (cudaMemPool_t pool : lufqhe::g_pools) {
+    if (!pool) continue;
+    const int rc = check_cuda(cudaMemPoolTrimTo(pool, 0), "cudaMemPoolTrimTo");
+    if (rc) return rc;
+  }
+  return LUFQHE_SUCCESS;
 }
 
 extern "C" size_t lufqhe_workspace_bytes(int n, long long batch, int mode) {

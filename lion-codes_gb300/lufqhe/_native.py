@@ -49,6 +49,7 @@ SIGNATURES = {
     "lufqhe_get_option": (F64, [I32]),
     "lufqhe_probe_fma_peak": (I32, [I32, P, P]),
     "lufqhe_workspace_bytes": (_c.c_size_t, [I32, I64, I32]),
+    "lufqhe_release_workspace": (I32, []),
     "lufqhe_last_error": (_c.c_char_p, []),
     "lufqhe_version": (_c.c_char_p, []),
 }

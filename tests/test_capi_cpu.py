@@ -143,3 +143,9 @@ def test_workspace_bytes(lufqhe_mod):
     assert lib.lufqhe_workspace_bytes(16, 32768, 2) == 0
     assert lib.lufqhe_workspace_bytes(24, 32768, 1) == 0
     assert lib.lufqhe_workspace_bytes(24, 0, 2) == 0
+
+
+def test_release_workspace_without_pool(lufqhe_mod):
+    """Before any call has made the library's memory pool there is nothing to
+    trim: the call succeeds without touching a device."""
+    assert lufqhe_mod.lib().lufqhe_release_workspace() == 0

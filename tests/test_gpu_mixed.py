@@ -251,3 +251,22 @@ def test_full_size_lll_against_double_double(cuda, lufqhe_mod, oracle, n, batch,
     and phase; the FP64 ones carry the fused FP64 kernel's bits."""
     A, _ = lufqhe_mod.gen_lll(batch, n, seed=seed)
     check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.2)
+
+
+def test_release_workspace(cuda, lufqhe_mod):
+    """The pool keeps an n = 24 call's refinement buffer after the stream is
+    synchronised; lufqhe_release_workspace hands it back to the driver, and
+    the next call allocates again and gives the same bits."""
+    lib = lufqhe_mod.lib()
+    A, _ = lufqhe_mod.gen_lll(16384, 24, seed=41)
+    ws = lib.lufqhe_workspace_bytes(24, 16384, lufqhe_mod.MODE_MIXED)
+    assert ws > 30 << 20
+    first = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    cuda.cuda.synchronize()
+    free_before = cuda.cuda.mem_get_info()[0]
+    assert lib.lufqhe_release_workspace() == 0
+    free_after = cuda.cuda.mem_get_info()[0]
+    assert free_after - free_before >= 0.9 * ws, (free_after - free_before, ws)
+    again = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    assert np.array_equal(first["logabs"], again["logabs"], equal_nan=True)
+    assert (first["status"] == again["status"]).all()
