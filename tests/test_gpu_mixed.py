@@ -270,3 +270,40 @@ def test_release_workspace(cuda, lufqhe_mod):
     again = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
     assert np.array_equal(first["logabs"], again["logabs"], equal_nan=True)
     assert (first["status"] == again["status"]).all()
+
+
+@pytest.mark.parametrize("n,lda", [(12, 16), (24, 32), (32, 33), (48, 64)])
+def test_padded_lda(cuda, lufqhe_mod, n, lda):
+    """A batch with row stride lda > n (the reference's padded loadSize) gives
+    the bits of the same matrices packed at lda = n, through the device entry
+    point and the host one (page-locked: read over the host link; pageable:
+    staged). n = 48 takes the FP64 route."""
+    A, _ = lufqhe_mod.gen_lll(1500, n, seed=70 + n)
+    want = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED))
+    buf = cuda.zeros((1500, n, lda), dtype=cuda.complex128, device="cuda")
+    buf[:, :, :n] = A
+    got = host(lufqhe_mod.batch_lup_det(buf, mode=lufqhe_mod.MODE_MIXED))
+    hb = buf.cpu()
+    outs = [got]
+    for Ah in (hb.pin_memory(), hb):
+        o = lufqhe_mod.batch_lup_det_host(Ah, mode=lufqhe_mod.MODE_MIXED)
+        cuda.cuda.synchronize()
+        outs.append({k: getattr(o, k).numpy() for k in ("logabs", "phase", "parity", "status")})
+    for o in outs:
+        assert np.array_equal(o["logabs"], want["logabs"], equal_nan=True)
+        assert np.array_equal(o["phase"], want["phase"], equal_nan=True)
+        assert (o["status"] == want["status"]).all() and (o["parity"] == want["parity"]).all()
+
+
+@pytest.mark.parametrize("n", [8, 24, 48])
+def test_empty_batches(cuda, lufqhe_mod, n):
+    """An empty mixed-mode batch is a successful call with empty results
+    through every entry point (device, host, coordinates)."""
+    A = cuda.zeros(0, n, n, dtype=cuda.complex128, device="cuda")
+    assert lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_MIXED).logabs.numel() == 0
+    out = lufqhe_mod.batch_lup_det_host(A.cpu(), mode=lufqhe_mod.MODE_MIXED)
+    cuda.cuda.synchronize()
+    assert out.logabs.numel() == 0
+    z = cuda.zeros(0, n, dtype=cuda.complex128, device="cuda")
+    assert lufqhe_mod.lll_det(z, mode=lufqhe_mod.MODE_MIXED).logabs.numel() == 0
+    cuda.cuda.synchronize()
