@@ -87,20 +87,26 @@ using namespace mixed;
 constexpr int tile_max_warps(int n) { return n == 24 ? 3 : 4; }
 constexpr int tile_min_ctas(int n) { return n == 24 ? 5 : n == 32 ? 1 : 4; }
 
-// Work counters of the batched mixed kernels, {next matrix, warps done} per
-// slot. Static device memory starts at zero; each launch takes the next slot
-// in turn and its last warp sets the slot back to zero, so a slot is free
-// again unless 4096 later launches were issued while it still ran.
+// Work counters of the batched mixed kernels, {claims after the first, CTAs
+// done} per slot. Static device memory starts at zero; each launch takes the
+// next slot in turn and its last CTA sets the slot back to zero, so a slot is
+// free again unless 4096 later launches were issued while it still ran.
 constexpr int kWorkSlots = 4096;
 __device__ unsigned long long g_work[kWorkSlots][2];
 std::atomic<unsigned int> g_work_seq{0};
 
 int next_work_slot() { return (int)(g_work_seq.fetch_add(1u) % kWorkSlots); }
 
-__device__ __forceinline__ long long claim_matrix(int slot, int lane) {
+// A warp's first matrix is its own index in the grid; later ones come from
+// the slot's counter, after the grid's warps. Small batches, where most warps
+// take one matrix, then make no same-address atomics at the start (n=8, 4096
+// matrices: 31.0 -> 28.9 us).
+__device__ __forceinline__ long long claim_matrix(int slot, int lane, bool first) {
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  if (first) return (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   unsigned long long b = 0;
   if (lane == 0) b = atomicAdd(&g_work[slot][0], 1ull);
-  return (long long)__shfl_sync(kFull, b, 0);
+  return (long long)__shfl_sync(kFull, b, 0) + warps;
 }
 
 // Pending lists of the FP64 pass, taken in turn by the calls: 256 lists of
@@ -152,10 +158,12 @@ __device__ __forceinline__ void defer_fp64_always(int pslot, long long b, int la
   }
 }
 
+// Once per CTA, after all its warps have left their loops (every warp of the
+// kernels that call this reaches it: their loops end only by break).
 __device__ __forceinline__ void release_slot(int slot, int lane) {
-  if (lane == 0) {
-    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    if (atomicAdd(&g_work[slot][1], 1ull) == warps - 1) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
       // every warp has made its last claim: reset for the slot's next launch
       atomicExch(&g_work[slot][0], 0ull);
       atomicExch(&g_work[slot][1], 0ull);
@@ -237,8 +245,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
   S.ec = S.er + n;
 
   DeferredOut out;
-  for (;;) {
-    const long long b = claim_matrix(slot, lane);
+  for (bool first = true;; first = false) {
+    const long long b = claim_matrix(slot, lane, first);
     if (b >= batch) break;
     __syncwarp();
     double2 *M = reinterpret_cast<double2 *>(S.SC);
@@ -298,8 +306,8 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   double2 *own = INPLACE ? spill + ((size_t)blockIdx.x * warps + warp) * N * N : nullptr;
 
   DeferredOut out;
-  for (;;) {
-    const long long b = claim_matrix(slot, lane);
+  for (bool first = true;; first = false) {
+    const long long b = claim_matrix(slot, lane, first);
     if (b >= batch) break;
     __syncwarp();
     double2 *M = reinterpret_cast<double2 *>(HL);
