@@ -195,28 +195,43 @@ def max_over_ranks(world, value: float) -> float:
     return float(t.item())
 
 
-def accuracy_vs_fp64(np, mixed, plain) -> dict:
-    """Relative log|det| error of the mixed result against the plain FP64
-    kernel, |d log|det|| / max(1, |log|det||), and the phase error."""
-    ok = (plain["status"] == 0) & ((mixed["status"] & ~8) == 0)
-    rel = np.abs(mixed["logabs"][ok] - plain["logabs"][ok]) / np.maximum(
-        1.0, np.abs(plain["logabs"][ok]))
-    dph = np.abs(np.angle(np.exp(1j * (mixed["phase"][ok] - plain["phase"][ok]))))
-    accepted = ok & (mixed["status"] == 0)
-    rel_acc = np.abs(mixed["logabs"][accepted] - plain["logabs"][accepted]) / np.maximum(
-        1.0, np.abs(plain["logabs"][accepted]))
-    return {
-        "vs": "plain FP64 kernel (reference pivot rule and arithmetic), whole batch",
-        "max_rel_logabs_err": float(rel.max(initial=0.0)),
-        "median_rel_logabs_err": float(np.median(rel)) if rel.size else 0.0,
-        "p99_rel_logabs_err": float(np.quantile(rel, 0.99)) if rel.size else 0.0,
-        "max_rel_logabs_err_mixed_accepted": float(rel_acc.max(initial=0.0)),
-        "count_above_1e-10": int((rel > 1e-10).sum()),
-        "max_phase_err_rad": float(dph.max(initial=0.0)),
-        "compared": int(ok.sum()),
-        "note": "FP64 LU itself carries up to ~1e-10 rel error on these matrices; the "
-                "double-double oracle comparison lives in tests/test_gpu_mixed.py",
-    }
+ST_FALLBACK = 8
+ST_FP64 = 16
+
+
+def dd_accuracy(np, oracle, A_np, la, ph, st) -> tuple[dict, "object"]:
+    """Error of EVERY result against the double-double oracle (complex LU in
+    ~32 digits): max(|d log|det||, |d phase|) / max(1, |log|det||), overall and
+    by route (accepted by the FP32 path, refactorised in FP64, routed to FP64)."""
+    la_dd, ph_dd, _ = oracle.logdet_dd(A_np)
+    scale = np.maximum(1.0, np.abs(la_dd))
+    fin = np.isfinite(la_dd) & np.isfinite(la)
+    e = np.zeros(len(la))
+    dph = np.abs(np.angle(np.exp(1j * (ph[fin] - ph_dd[fin]))))
+    e[fin] = np.maximum(np.abs(la[fin] - la_dd[fin]), dph) / scale[fin]
+    # a non-finite result must match a non-finite truth (singular / NaN input)
+    mismatch = int((np.isfinite(la_dd) != np.isfinite(la)).sum())
+    routes = {"accepted": st == 0, "fp64_fallback": (st & ST_FALLBACK) != 0,
+              "fp64_routed": (st & ST_FP64) != 0}
+    out = {"vs": "double-double oracle, every result of the batch",
+           "compared": int(fin.sum()), "nonfinite_mismatch": mismatch,
+           "max_rel_err": float(e.max(initial=0.0)),
+           "median_rel_err": float(np.median(e[fin])) if fin.any() else 0.0,
+           "count_above_1e-10": int((e > 1e-10).sum()),
+           "by_route": {k: {"count": int(m.sum()), "max_rel_err": float(e[m].max(initial=0.0)),
+                            "count_above_1e-10": int((e[m] > 1e-10).sum())}
+                        for k, m in routes.items()}}
+    return out, (la_dd, ph_dd)
+
+
+def rel_err_vs(np, la, ph, truth) -> "object":
+    la_dd, ph_dd = truth
+    scale = np.maximum(1.0, np.abs(la_dd))
+    fin = np.isfinite(la_dd) & np.isfinite(la)
+    e = np.zeros(len(la))
+    e[fin] = np.maximum(np.abs(la[fin] - la_dd[fin]),
+                        np.abs(np.angle(np.exp(1j * (ph[fin] - ph_dd[fin]))))) / scale[fin]
+    return e
 
 
 def ncu_traffic(kernel: str, workload: str):
@@ -247,6 +262,30 @@ def measure_pipe_peaks(torch, lufqhe) -> dict:
     return out
 
 
+def kernel_times(torch, lufqhe, fn, steps: int) -> dict:
+    """Per-kernel device time of `steps` calls of fn, from the CUDA events the
+    library records around each launch on the launching stream
+    (LUFQHE_OPT_KERNEL_TIMING): {name: {"launches", "ms", "ms_per_launch"}}."""
+    import ctypes
+    lib = lufqhe.lib()
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.lufqhe_kernel_times(buf, len(buf))  # drop anything recorded before
+    lib.lufqhe_set_option(6, 1.0)
+    try:
+        for _ in range(steps):
+            fn()
+        torch.cuda.synchronize()
+        rc = lib.lufqhe_kernel_times(buf, len(buf))
+    finally:
+        lib.lufqhe_set_option(6, 0.0)
+    if rc != 0:
+        return {}
+    t = json.loads(buf.value.decode())
+    for v in t.values():
+        v["ms_per_launch"] = v["ms"] / max(1, v["launches"])
+    return t
+
+
 def make_inputs(torch, lufqhe, wl, want_z=False):
     kind, n, batch, seed = WORKLOADS[wl]
     z = None
@@ -273,300 +312,157 @@ def time_device(torch, lufqhe, A, mode, out, steps, warmup, stream):
     return e0.elapsed_time(e1) / steps
 
 
-def run_mixedn(args, world, rank, local):
-    """Mixed-size batch: groups of LLL matrices, one persistent launch replayed
-    from a CUDA graph, tile sizes and warps per CTA from the autotuner."""
+def hbm_peak_gbs():
+    p = load_peaks().get("hbm_gbs")
+    return (p, "MEASURED_PEAKS.json hbm_gbs (of measured)") if p else \
+        (6800.0, "fallback 6.8 TB/s (of fallback)")
+
+
+def run_batched(args, world, rank, local, workload, full=True):
+    """One batched workload (configs 1-3): mixed determinants/s with the batch
+    resident, the plain FP64 kernels on the same batch, every result against
+    the double-double oracle, the dominant kernel's roofline from CUDA events
+    around its own launches; with `full`, also e2e through the host-buffer
+    C-ABI call, e2e from particle coordinates and the CPU baseline."""
     import numpy as np
     import torch
 
     import lufqhe
+    import lufqhe_oracle
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
-    _, _, total, seed = WORKLOADS["mixedn"]
-    counts = np.random.default_rng(seed).multinomial(total, [1.0 / len(MIXED_SIZES)] * len(MIXED_SIZES))
-    groups, off = [], 0
     with torch.cuda.stream(stream):
-        for n, c in zip(MIXED_SIZES, counts):
-            A, _ = lufqhe.gen_lll(int(c), n, seed=seed * 100 + n, sigma=math.sqrt(n))
-            groups.append((A, off))
-            off += int(c)
-    torch.cuda.synchronize()
-
-    def alloc():
-        return lufqhe.DetResult(torch.empty(total, dtype=torch.float64, device=dev),
-                                torch.empty(total, dtype=torch.float64, device=dev),
-                                torch.empty(total, dtype=torch.int8, device=dev),
-                                torch.empty(total, dtype=torch.int32, device=dev))
-
-    out = alloc()
-    plan = lufqhe.Plan(groups, out, mode=lufqhe.MODE_MIXED, autotune=True, stream=stream)
-    tune = plan.describe()
-
-    def timed(fn, steps):
-        for _ in range(args.warmup):
-            fn()
-        torch.cuda.synchronize()
-        barrier(world)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(steps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / steps
-
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    ms = timed(lambda: plan.execute(stream=stream), args.steps)
-    time.sleep(0.2)
-    clocks = sampler.stop()
-    ms_max = max_over_ranks(world, ms)
-    mixed_st = out.status.cpu().numpy()
-    mixed_la = out.logabs.cpu().numpy()
-
-    # the same batch as one plain FP64 (fused) persistent launch
-    out_p = alloc()
-    plan_p = lufqhe.Plan(groups, out_p, mode=lufqhe.MODE_PLAIN_FP64_FUSED, autotune=True,
-                         stream=stream)
-    ms_plain = timed(lambda: plan_p.execute(stream=stream), max(2, args.steps // 2))
-    plain_la = out_p.logabs.cpu().numpy()
-    # per-size throughput: each group as its own batched call
-    per_n = {}
-    for (A, o), n in zip(groups, MIXED_SIZES):
-        r = lufqhe.DetResult(out.logabs[o:o + A.shape[0]], out.phase[o:o + A.shape[0]],
-                             out.parity[o:o + A.shape[0]], out.status[o:o + A.shape[0]])
-        t = timed(lambda: lufqhe.batch_lup_det(A, mode=lufqhe.MODE_MIXED, stream=stream, out=r),
-                  max(2, args.steps // 4))
-        per_n[str(n)] = {"count": int(A.shape[0]), "dets_per_s": A.shape[0] / (t * 1e-3),
-                         "fallbacks": int(((mixed_st[o:o + A.shape[0]] & 8) != 0).sum())}
-    launches = args.steps + max(2, args.steps // 2) + len(groups) * max(2, args.steps // 4)
-
-    # e2e: the same batch in page-locked host memory, results to page-locked
-    # host memory: a plan on the host buffers, whose kernels read the matrices
-    # and write the results over the host link (no copies), graph replay
-    hosts = [torch.empty(A.shape, dtype=A.dtype, pin_memory=True) for A, _ in groups]
-    for h, (A, _) in zip(hosts, groups):
-        h.copy_(A)
-    out_host = lufqhe.DetResult(*(torch.empty(total, dtype=getattr(out, k).dtype, pin_memory=True)
-                                  for k in ("logabs", "phase", "parity", "status")))
-    plan_h = lufqhe.Plan([(h, o) for h, (_, o) in zip(hosts, groups)], out_host,
-                         mode=lufqhe.MODE_MIXED, autotune=True, stream=stream)
-    torch.cuda.synchronize()
-
-    def e2e():
-        plan_h.execute(stream=stream)
-
-    ms_e2e = max_over_ranks(world, timed(e2e, args.steps))
-    launches += args.steps
-    h2d = sum(h.numel() * h.element_size() for h in hosts)
-    d2h = sum(getattr(out_host, k).numel() * getattr(out_host, k).element_size()
-              for k in ("logabs", "phase", "parity", "status"))
-    F = sum(flops_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
-    B = sum(bytes_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
-    pipes = measure_pipe_peaks(torch, lufqhe)
-    hbm_peak = load_peaks().get("hbm_gbs") or 6800.0
-    big = str(MIXED_SIZES[-1])
-    big_ms = ((tune or {}).get("tiles") or {}).get(big, {}).get("ms_alone")
-    big_tflops = (flops_per_matrix(MIXED_SIZES[-1]) * int(counts[-1]) / (big_ms * 1e-3) * 1e-12
-                  if big_ms else None)
-    ok = (plain_la == plain_la) & (mixed_st == 0)
-    rel = np.abs(mixed_la[ok] - plain_la[ok]) / np.maximum(1.0, np.abs(plain_la[ok]))
-    if rank == 0:
-        line = {
-            "metric": "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)",
-            "value": world * total / (ms_max * 1e-3), "unit": "dets/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128 in / fp32+float-float compute / f64 out",
-            "data": "synthetic (seeded, generated on device)",
-            "config": {"workload": f"mixedn: {total} LLL matrices, n uniform over "
-                                   f"{list(MIXED_SIZES)}, one persistent launch in a CUDA graph",
-                       "counts": {str(n): int(c) for n, c in zip(MIXED_SIZES, counts)},
-                       "l2": "inputs larger than L2 (no flush)"},
-            "plain_fp64_fused_persistent_dets_per_s": total / (ms_plain * 1e-3),
-            "mixed_over_plain_fused": ms_plain / ms,
-            "per_n": per_n,
-            "autotune": tune,
-            "accuracy_vs_plain_fp64": {"max_rel_logabs_err_accepted": float(rel.max(initial=0)),
-                                       "count_above_1e-10": int((rel > 1e-10).sum())},
-            "fallbacks": {"count": int(((mixed_st & 8) != 0).sum()), "of": total},
-            "e2e": {"value": world * total / (ms_e2e * 1e-3), "unit": "dets/s",
-                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "call": "lufqhe_plan_execute on a plan over page-locked host buffers (the "
-                            "kernels read the matrices and write the results over the host link)"},
-            "gpu_launches": launches,
-            # the n=48 group (FP64 route, warp-group pass) takes most of the step:
-            # its F.dets/s alone against the FP64 FMA peak; "step" is the whole
-            # plan's F.dets/s (one FP64-accurate determinant per unit) against it
-            "roofline": {"kernel": "grouped_group_kernel (n=48 group, alone)", "bound": "fp64",
-                         "achieved": big_tflops, "peak": pipes.get("fp64_tflops"),
-                         "unit": "TFLOP/s",
-                         "frac": (big_tflops / pipes["fp64_tflops"])
-                         if big_tflops and pipes.get("fp64_tflops") else None,
-                         "traffic": None,
-                         "step": {"achieved": F / (ms * 1e-3) * 1e-12,
-                                  "frac": (F / (ms * 1e-3) * 1e-12 / pipes["fp64_tflops"])
-                                  if pipes.get("fp64_tflops") else None},
-                         "hbm": {"achieved": B / (ms * 1e-3) * 1e-9, "peak": hbm_peak,
-                                 "unit": "GB/s", "frac": B / (ms * 1e-3) * 1e-9 / hbm_peak}},
-            "clocks": clocks,
-        }
-        import bench_cpu
-        A0 = groups[MIXED_SIZES.index(24)][0][:4096].cpu().numpy()
-        line["cpu_baseline"] = bench_cpu.cpu_baseline(np, A0, 24, seconds=args.cpu_seconds)
-        print(json.dumps(line), flush=True)
-    plan.close()
-    plan_p.close()
-    plan_h.close()
-
-
-def run_serving(args, world, rank, local):
-    """Serving: offline capacity per size class, then the walker stream at 70%
-    of it and at the configured 20k requests/s; p50/p99 latency (arrival to
-    result on the host) and throughput, mixed and FP64."""
-    import numpy as np
-    import torch
-
-    import lufqhe
-
-    torch.cuda.set_device(local)
-    seed = WORKLOADS["serving"][3]
-    rng = np.random.default_rng(seed)
-    ks = np.maximum(1, np.minimum(4096, np.floor(np.exp(rng.uniform(0, np.log(4097), 200000)))))
-    mean_k = float(ks.mean())
-
-    def offline_rate(n, mode):
-        count = max(512, min(32768, int(2e8 // (16 * n * n))))
-        A, _ = lufqhe.gen_lll(count, n, seed=seed * 100 + n)
-        out = lufqhe.batch_lup_det(A, mode=mode)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(3):
-            lufqhe.batch_lup_det(A, mode=mode, out=out)
-        e1.record()
-        torch.cuda.synchronize()
-        return count / (e0.elapsed_time(e1) / 3 * 1e-3)
-
-    result = {}
-    launches = 0
-    for label, mode in (("mixed", lufqhe.MODE_MIXED), ("fp64", lufqhe.MODE_PLAIN_FP64_FUSED)):
-        rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
-        launches += 4 * len(SERVE_SIZES)
-        sec_per_matrix = float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
-        offline_mps = 1.0 / sec_per_matrix                  # matrices/s of the mix
-        cap_req = offline_mps / mean_k                      # requests/s at full load
-        inv = np.array([1.0 / rates[n] for n in SERVE_SIZES])
-        sms = np.maximum(2, np.round(152 * inv / inv.sum())).astype(int)
-        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
-        srv = lufqhe.Server(64 << 30, mode=mode, classes=SERVE_SIZES, class_sms=list(map(int, sms)),
-                            max_k=4096, tile=8)
-        runs = {}
-        for tag, rate, nreq in (("at_70pct_offline", 0.7 * cap_req, args.serve_requests),
-                                ("at_20k_req_s", 20000.0, max(200, args.serve_requests // 4))):
-            lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nreq, moves=100, k_min=1,
-                                               k_max=4096, seed=seed)
-            per = {}
-            for n in SERVE_SIZES:
-                m = ns == n
-                if m.any():
-                    per[str(n)] = {"p50_ms": float(np.percentile(lat[m], 50) / 1e3),
-                                   "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
-                                   "requests": int(m.sum())}
-            runs[tag] = {"rate_req_s": rate, "requests": int(len(lat)),
-                         "p50_ms": float(np.percentile(lat, 50) / 1e3),
-                         "p99_ms": float(np.percentile(lat, 99) / 1e3),
-                         "throughput_dets_s": mats / el,
-                         "fraction_of_offline": (mats / el) / offline_mps,
-                         "per_n": per}
-        srv.close()
-        result[label] = {"offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
-                         "offline_mix_dets_per_s": offline_mps,
-                         "offline_capacity_req_s": cap_req, "class_sms": list(map(int, sms)),
-                         "runs": runs}
-    if rank == 0:
-        r70 = result["mixed"]["runs"]["at_70pct_offline"]
-        line = {
-            "metric": "serving: determinants/s at 70% of offline load, with p50/p99 latency",
-            "value": r70["throughput_dets_s"], "unit": "dets/s", "n_gpus": world,
-            "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128 in / fp32+float-float compute / f64 out",
-            "data": "synthetic (seeded Poisson walker stream)",
-            "config": {"workload": "serving: Poisson move requests, k log-uniform 1..4096, "
-                                   "n in (8,16,32,64), 100 moves per walker, walkers resident in "
-                                   "HBM (64 GiB budget)", "mean_k": mean_k},
-            "p50_ms": r70["p50_ms"], "p99_ms": r70["p99_ms"],
-            "serving": result, "gpu_launches": launches,
-        }
-        print(json.dumps(line), flush=True)
-
-
-def run_ours(args):
-    import numpy as np
-    import torch
-
-    import lufqhe
-
-    world, rank, local = dist_setup(args)
-    if args.workload == "mixedn":
-        return run_mixedn(args, world, rank, local)
-    if args.workload == "serving":
-        return run_serving(args, world, rank, local)
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.Stream(device=dev)
-    with torch.cuda.stream(stream):
-        A, n, batch, z_dev = make_inputs(torch, lufqhe, args.workload, want_z=True)
+        A, n, batch, z_dev = make_inputs(torch, lufqhe, workload, want_z=True)
     torch.cuda.synchronize()
     res = lufqhe.DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
                            torch.empty(batch, dtype=torch.float64, device=dev),
                            torch.empty(batch, dtype=torch.int8, device=dev),
                            torch.empty(batch, dtype=torch.int32, device=dev))
+    steps = args.steps if full else max(5, args.steps // 2)
+    mode = lufqhe.MODE_MIXED
 
     # ---- headline: mixed, device-resident --------------------------------
-    mode = lufqhe.MODE_MIXED
     for _ in range(args.warmup):
         lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=res)
     torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
+    sampler = ClockSampler(local) if full else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=res)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms_mixed = e0.elapsed_time(e1) / args.steps
-    time.sleep(0.2)
-    clocks = sampler.stop()
+    ms_mixed = e0.elapsed_time(e1) / steps
+    clocks = None
+    if sampler:
+        time.sleep(0.2)
+        clocks = sampler.stop()
     barrier(world)
     ms_mixed_max = max_over_ranks(world, ms_mixed)
-    value = world * batch / (ms_mixed_max * 1e-3)
-    launches = args.steps * mixed_launches_per_call(n)
-
+    launches = steps * mixed_launches_per_call(n)
     mixed_out = {k: getattr(res, k).cpu().numpy() for k in ("logabs", "phase", "status")}
+
+    # ---- the dominant kernel alone: CUDA events around its own launches ----
+    kt = kernel_times(torch, lufqhe,
+                      lambda: lufqhe.batch_lup_det(A, mode=mode, stream=stream, out=res), steps)
+    dom = f"lup_mixed_tile_kernel<{n}>"
 
     # ---- plain FP64 kernels (same batch) ---------------------------------
     ms_plain_ref = time_device(torch, lufqhe, A, lufqhe.MODE_PLAIN_FP64, res,
-                               max(2, args.steps // 2), 2, stream)
-    plain_ref = {k: getattr(res, k).cpu().numpy() for k in ("logabs", "phase", "status")}
+                               max(2, steps // 2), 2, stream)
     ms_plain_fused = time_device(torch, lufqhe, A, lufqhe.MODE_PLAIN_FP64_FUSED, res,
-                                 max(2, args.steps // 2), 2, stream)
-    launches += 2 * max(2, args.steps // 2)
+                                 max(2, steps // 2), 2, stream)
+    fused_out = {k: getattr(res, k).cpu().numpy() for k in ("logabs", "phase", "status")}
+    kt_plain = kernel_times(torch, lufqhe, lambda: lufqhe.batch_lup_det(
+        A, mode=lufqhe.MODE_PLAIN_FP64_FUSED, stream=stream, out=res), max(2, steps // 2))
+
+    dets_mixed = batch / (ms_mixed * 1e-3)
+    dets_ref = batch / (ms_plain_ref * 1e-3)
+    dets_fused = batch / (ms_plain_fused * 1e-3)
+    F = flops_per_matrix(n)
+    B = bytes_per_matrix(n)
+    hbm_peak, hbm_src = hbm_peak_gbs()
+    pipes = measure_pipe_peaks(torch, lufqhe)
+
+    out = None
+    if rank == 0:
+        A_np = A.cpu().numpy()
+        acc, truth = dd_accuracy(np, lufqhe_oracle, A_np, mixed_out["logabs"],
+                                 mixed_out["phase"], mixed_out["status"])
+        e_fp64 = rel_err_vs(np, fused_out["logabs"], fused_out["phase"], truth)
+        acc["plain_fp64_fused_vs_dd"] = {"max_rel_err": float(e_fp64.max(initial=0.0)),
+                                         "count_above_1e-10": int((e_fp64 > 1e-10).sum())}
+        t_dom = kt.get(dom, {}).get("ms_per_launch")
+        fp32_peak = pipes.get("fp32_tflops")
+        fp64_peak = pipes.get("fp64_tflops")
+        roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak,
+                "peak_source": hbm_src,
+                "algorithmic_bytes_per_launch": batch * B,
+                "bytes_per_matrix": B,
+                "traffic": ncu_traffic("lup_mixed_tile_kernel", workload)}
+        if t_dom:
+            ach = batch * B / (t_dom * 1e-3) * 1e-9
+            roof.update({
+                "achieved": ach, "frac": ach / hbm_peak,
+                "kernel_ms_per_launch": t_dom, "launches_timed": kt[dom]["launches"],
+                "share_of_step": t_dom / ms_mixed,
+                "fp32": {"achieved_tflops": batch * F / (t_dom * 1e-3) * 1e-12,
+                         "peak": fp32_peak,
+                         "frac": (batch * F / (t_dom * 1e-3) * 1e-12 / fp32_peak)
+                         if fp32_peak else None,
+                         "peak_source": "library FMA probe kernel, this run (no FP32 figure in "
+                                        "MEASURED_PEAKS.json)",
+                         "flops_per_matrix": F},
+                "method_fp32_lane_ops": {
+                    "ops_per_matrix": mixed_fp32_ops_per_matrix(n),
+                    "frac_of_half_fp32_peak": (mixed_fp32_ops_per_matrix(n) * batch /
+                                               (t_dom * 1e-3) * 1e-12 / (fp32_peak / 2.0))
+                    if fp32_peak else None},
+            })
+        t_pl = kt_plain.get(f"lup_plain_kernel<{n}>", kt_plain.get(
+            f"lup_plain_group_kernel<{n}>", {})).get("ms_per_launch")
+        roof["plain_fp64"] = {
+            "kernel": f"lup_plain_kernel<{n}> (fused)", "bound": "fp64", "unit": "TFLOP/s",
+            "peak": fp64_peak, "peak_source": "library FMA probe kernel, this run (no FP64 figure "
+                                              "in MEASURED_PEAKS.json)",
+            "kernel_ms_per_launch": t_pl,
+            "achieved": batch * F / (t_pl * 1e-3) * 1e-12 if t_pl else None,
+            "frac": (batch * F / (t_pl * 1e-3) * 1e-12 / fp64_peak) if t_pl and fp64_peak
+            else None,
+            "traffic": ncu_traffic("lup_plain_kernel", workload)}
+        out = {
+            "value": world * batch / (ms_mixed_max * 1e-3), "unit": "dets/s",
+            "ms_per_step": ms_mixed_max, "steps": steps,
+            "config": workload_config(workload, world),
+            "plain_fp64": {"dets_per_s_reference_arith": dets_ref,
+                           "dets_per_s_fused": dets_fused,
+                           "mixed_over_plain_fused": dets_mixed / dets_fused,
+                           "mixed_over_plain_reference_arith": dets_mixed / dets_ref},
+            "accuracy": acc,
+            "fallbacks": {"count": int(((mixed_out["status"] & ST_FALLBACK) != 0).sum()),
+                          "of": batch},
+            "hbm_gbs": B * dets_mixed * 1e-9,
+            "kernel_times_ms": kt,
+            "roofline": roof,
+            "gpu_launches": launches,
+        }
+        if clocks is not None:
+            out["clocks"] = clocks
+    if not full:
+        barrier(world)
+        return out
 
     # ---- e2e through the C-ABI with host buffers ---------------------------
     # lufqhe_batch_lup_det_host: the batch and the results in page-locked host
-    # memory; the library pipelines H2D copy, factorisation and D2H copy
+    # memory (mixed mode: the kernels read the matrices over the host link)
     A_host = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
     A_host.copy_(A)
     out_host = lufqhe.DetResult(*(torch.empty(getattr(res, k).shape, dtype=getattr(res, k).dtype,
@@ -591,10 +487,8 @@ def run_ours(args):
     e3.record(stream)
     torch.cuda.synchronize()
     ms_e2e = max_over_ranks(world, e2.elapsed_time(e3) / args.steps)
-    launches += args.steps * host_launches_per_call(n, n, batch, mode, A_host.is_pinned())
 
-    # the host link this box gives a plain copy of the same pinned batch (the
-    # e2e ceiling; it differs from box to box)
+    # the host link this box gives a plain copy of the same pinned batch
     link_buf = torch.empty_like(A)
     link_ms = []
     for _ in range(3):
@@ -610,13 +504,8 @@ def run_ours(args):
     del link_buf
 
     # ---- e2e from particle coordinates (LLL workloads) ---------------------
-    # what a Monte Carlo driver holds is z, not the matrices: H2D of the
-    # coordinates, lufqhe_lll_det (matrices built inside the kernels), D2H of
-    # the results, every step
     e2e_coords = None
     if z_dev is not None:
-        # coordinates and results in page-locked host memory, read and written
-        # by the kernels over the host link
         z_host = z_dev.contiguous().cpu().pin_memory()
 
         def coords_step():
@@ -634,106 +523,334 @@ def run_ours(args):
         e5.record(stream)
         torch.cuda.synchronize()
         ms_c = max_over_ranks(world, e4.elapsed_time(e5) / args.steps)
-        launches += args.steps * mixed_launches_per_call(n)
         e2e_coords = {"value": world * batch / (ms_c * 1e-3), "unit": "dets/s", "ms_per_step": ms_c,
                       "h2d_bytes_per_step": z_host.numel() * z_host.element_size(),
                       "d2h_bytes_per_step": d2h,
                       "call": "lufqhe_lll_det (orbital matrices built in the kernels from z)"}
-
-    # ---- kernel-only timing of the dominant kernel (roofline) --------------
-    peaks_file = load_peaks()
-    pipes = measure_pipe_peaks(torch, lufqhe)
-    F = flops_per_matrix(n)
-    B = bytes_per_matrix(n)
-    hbm_peak = peaks_file.get("hbm_gbs")
-    hbm_src = "MEASURED_PEAKS.json" if hbm_peak else "fallback 6800 GB/s"
-    hbm_peak = hbm_peak or 6800.0
-
-    out = None
     if rank == 0:
-        acc = accuracy_vs_fp64(np, mixed_out, plain_ref)
-        # cpu_baseline leg: the reference's CPU Crout path (FP64 restatement)
         import bench_cpu
-        cpu = bench_cpu.cpu_baseline(np, A.cpu().numpy(), n, seconds=args.cpu_seconds)
-        dets_mixed = batch / (ms_mixed * 1e-3)
-        dets_ref = batch / (ms_plain_ref * 1e-3)
-        dets_fused = batch / (ms_plain_fused * 1e-3)
-        fallback = int(((mixed_out["status"] & lufqhe.ST_FALLBACK) != 0).sum())
-        fp32_peak = pipes.get("fp32_tflops")
-        fp64_peak = pipes.get("fp64_tflops")
-        # FP32 pipe roofline in lane operations: the measured FMA peak (flops/s)
-        # halved gives FP32 lane operations/s (one FMA = one lane operation)
-        ops = mixed_fp32_ops_per_matrix(n)
-        achieved_tops = ops * dets_mixed * 1e-12
-        ops_peak = fp32_peak / 2.0 if fp32_peak else None
-        roof = {
-            "kernel": f"lup_mixed_tile_kernel<{n}>",
-            "bound": "fp32",
-            "achieved": achieved_tops,
-            "peak": ops_peak,
-            "unit": "T FP32 lane-ops/s",
-            "frac": (achieved_tops / ops_peak) if ops_peak else None,
-            "peak_source": "measured FP32 FMA peak (library probe kernel, this run) / 2",
-            "fp32_ops_per_matrix": ops,
-            "lup_flops_per_matrix": F,
-            "traffic": ncu_traffic("lup_mixed_tile_kernel", args.workload),
-            "hbm": {"achieved": B * dets_mixed * 1e-9, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": B * dets_mixed * 1e-9 / hbm_peak, "peak_source": hbm_src,
-                    "bytes_per_matrix": B},
-            "plain_fp64": {"kernel": "lup_plain_kernel<ARITH_FUSED>", "bound": "fp64",
-                           "achieved": F * dets_fused * 1e-12, "peak": fp64_peak,
-                           "unit": "TFLOP/s",
-                           "frac": (F * dets_fused * 1e-12 / fp64_peak) if fp64_peak else None,
-                           "traffic": ncu_traffic("lup_plain_kernel", args.workload)},
-        }
-        out = {
-            "metric": "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)",
-            "value": value,
-            "unit": "dets/s",
-            "n_gpus": world,
-            "steps": args.steps,
-            "warmup": args.warmup,
-            "ms_per_step": ms_mixed_max,
-            "higher_is_better": True,
-            "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "c128 in / fp32+float-float compute / f64 out",
-            "data": "synthetic (seeded, generated on device)",
-            "config": {"workload": f"{args.workload}: {batch} x n={n} "
-                                   f"{'LLL orbital' if WORKLOADS[args.workload][0] == 'lll' else 'complex Gaussian'} "
-                                   f"complex128, seed {WORKLOADS[args.workload][3]}",
-                       "batch": batch, "n": n,
-                       "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}"},
-            "plain_fp64": {"dets_per_s_reference_arith": dets_ref,
-                           "dets_per_s_fused": dets_fused,
-                           "mixed_over_plain_fused": dets_mixed / dets_fused,
-                           "mixed_over_plain_reference_arith": dets_mixed / dets_ref},
-            "accuracy": acc,
-            "fallbacks": {"count": fallback, "of": batch},
-            "e2e": {"value": world * batch / (ms_e2e * 1e-3), "unit": "dets/s",
-                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
-                    "call": "lufqhe_batch_lup_det_host on page-locked host buffers (mixed mode: "
-                            "the kernels read the matrices over the host link, no staging copies)",
-                    "host_link_copy_gbs": link_gbs,
-                    "fraction_of_link": (h2d / (ms_e2e * 1e-3) * 1e-9) / link_gbs},
-            "e2e_from_coordinates": e2e_coords,
-            "gpu_launches": launches,
-            "roofline": roof,
-            "cpu_baseline": cpu,
-            "clocks": clocks,
-        }
+        out["e2e"] = {"value": world * batch / (ms_e2e * 1e-3), "unit": "dets/s",
+                      "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h,
+                      "call": "lufqhe_batch_lup_det_host on page-locked host buffers (mixed mode: "
+                              "the kernels read the matrices over the host link, no staging "
+                              "copies)",
+                      "host_link_copy_gbs": link_gbs,
+                      "fraction_of_link": (h2d / (ms_e2e * 1e-3) * 1e-9) / link_gbs}
+        out["e2e_from_coordinates"] = e2e_coords
+        # cpu_baseline leg: the reference's CPU Crout path (FP64 restatement)
+        out["cpu_baseline"] = bench_cpu.cpu_baseline(np, A.cpu().numpy(), n,
+                                                     seconds=args.cpu_seconds)
     barrier(world)
-    if out is not None:
-        print(json.dumps(out), flush=True)
+    return out
+
+
+def run_plan(args, world, rank, local, full=True):
+    """Config 4: a mixed-size batch of LLL matrices as one plan (work list and
+    CUDA graph, tiles, FP64 shares and CTA size from the autotuner), against the
+    same plan in plain fused FP64; every result against the double-double
+    oracle; per-n rates from batched calls; with `full`, e2e from page-locked
+    host buffers."""
+    import numpy as np
+    import torch
+
+    import lufqhe
+    import lufqhe_oracle
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    _, _, total, seed = WORKLOADS["mixedn"]
+    counts = np.random.default_rng(seed).multinomial(total, [1.0 / len(MIXED_SIZES)] * len(MIXED_SIZES))
+    groups, off = [], 0
+    with torch.cuda.stream(stream):
+        for n, c in zip(MIXED_SIZES, counts):
+            A, _ = lufqhe.gen_lll(int(c), n, seed=seed * 100 + n, sigma=math.sqrt(n))
+            groups.append((A, off))
+            off += int(c)
+    torch.cuda.synchronize()
+    steps = args.steps if full else max(5, args.steps // 2)
+
+    def alloc():
+        return lufqhe.DetResult(torch.empty(total, dtype=torch.float64, device=dev),
+                                torch.empty(total, dtype=torch.float64, device=dev),
+                                torch.empty(total, dtype=torch.int8, device=dev),
+                                torch.empty(total, dtype=torch.int32, device=dev))
+
+    out = alloc()
+    plan = lufqhe.Plan(groups, out, mode=lufqhe.MODE_MIXED, autotune=True, stream=stream)
+    tune = plan.describe()
+
+    def timed(fn, nsteps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(nsteps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / nsteps
+
+    sampler = ClockSampler(local) if full else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    ms = timed(lambda: plan.execute(stream=stream), steps)
+    clocks = None
+    if sampler:
+        time.sleep(0.2)
+        clocks = sampler.stop()
+    ms_max = max_over_ranks(world, ms)
+    launches = steps * plan.kernels()
+    mixed_st = out.status.cpu().numpy()
+    mixed_la = out.logabs.cpu().numpy()
+    mixed_ph = out.phase.cpu().numpy()
+    kt = kernel_times(torch, lufqhe, lambda: plan.execute(stream=stream, graph=False), steps)
+
+    # the same batch as one plain FP64 (fused) plan
+    out_p = alloc()
+    plan_p = lufqhe.Plan(groups, out_p, mode=lufqhe.MODE_PLAIN_FP64_FUSED, autotune=True,
+                         stream=stream)
+    ms_plain = timed(lambda: plan_p.execute(stream=stream), max(2, steps // 2))
+    plain_la = out_p.logabs.cpu().numpy()
+    plain_ph = out_p.phase.cpu().numpy()
+    # per-size throughput: each group as its own batched call
+    per_n = {}
+    for (A, o), n in zip(groups, MIXED_SIZES):
+        r = lufqhe.DetResult(out.logabs[o:o + A.shape[0]], out.phase[o:o + A.shape[0]],
+                             out.parity[o:o + A.shape[0]], out.status[o:o + A.shape[0]])
+        t = timed(lambda: lufqhe.batch_lup_det(A, mode=lufqhe.MODE_MIXED, stream=stream, out=r),
+                  max(2, steps // 4))
+        per_n[str(n)] = {"count": int(A.shape[0]), "dets_per_s": A.shape[0] / (t * 1e-3),
+                         "fallbacks": int(((mixed_st[o:o + A.shape[0]] & ST_FALLBACK) != 0).sum())}
+    F = sum(flops_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
+    B = sum(bytes_per_matrix(n) * int(c) for n, c in zip(MIXED_SIZES, counts))
+    pipes = measure_pipe_peaks(torch, lufqhe)
+    hbm_peak, hbm_src = hbm_peak_gbs()
+
+    res = None
+    if rank == 0:
+        # every result of every group against the double-double oracle
+        accs, e_all, e_fp64 = {}, [], []
+        for (A, o), n in zip(groups, MIXED_SIZES):
+            c = A.shape[0]
+            a, truth = dd_accuracy(np, lufqhe_oracle, A.cpu().numpy(), mixed_la[o:o + c],
+                                   mixed_ph[o:o + c], mixed_st[o:o + c])
+            accs[str(n)] = a
+            e_all.append(rel_err_vs(np, mixed_la[o:o + c], mixed_ph[o:o + c], truth))
+            e_fp64.append(rel_err_vs(np, plain_la[o:o + c], plain_ph[o:o + c], truth))
+        e_all = np.concatenate(e_all)
+        e_fp64 = np.concatenate(e_fp64)
+        acc = {"vs": "double-double oracle, every result of the 200000",
+               "max_rel_err": float(e_all.max()), "count_above_1e-10": int((e_all > 1e-10).sum()),
+               "plain_fp64_fused_vs_dd": {"max_rel_err": float(e_fp64.max()),
+                                          "count_above_1e-10": int((e_fp64 > 1e-10).sum())},
+               "per_n": accs}
+        top = max(kt.items(), key=lambda kv: kv[1]["ms"]) if kt else None
+        roof = None
+        if top:
+            name, v = top
+            nn = int(name.split("<")[1].rstrip(">")) if "<" in name else MIXED_SIZES[-1]
+            cnt = int(counts[MIXED_SIZES.index(nn)]) if nn in MIXED_SIZES else 0
+            t_k = v["ms_per_launch"]
+            fl = flops_per_matrix(nn) * cnt
+            roof = {"kernel": name, "bound": "fp64", "unit": "TFLOP/s",
+                    "kernel_ms_per_launch": t_k, "share_of_step": t_k / ms,
+                    "achieved": fl / (t_k * 1e-3) * 1e-12,
+                    "peak": pipes.get("fp64_tflops"),
+                    "frac": (fl / (t_k * 1e-3) * 1e-12 / pipes["fp64_tflops"])
+                    if pipes.get("fp64_tflops") else None,
+                    "peak_source": "library FMA probe kernel, this run",
+                    "traffic": None,
+                    "hbm": {"achieved": B / (ms * 1e-3) * 1e-9, "peak": hbm_peak,
+                            "unit": "GB/s", "frac": B / (ms * 1e-3) * 1e-9 / hbm_peak,
+                            "peak_source": hbm_src}}
+        res = {"value": world * total / (ms_max * 1e-3), "unit": "dets/s", "ms_per_step": ms_max,
+               "steps": steps, "config": workload_config("mixedn", world)
+               | {"counts": {str(n): int(c) for n, c in zip(MIXED_SIZES, counts)}},
+               "plain_fp64_fused_plan_dets_per_s": total / (ms_plain * 1e-3),
+               "mixed_over_plain_fused": ms_plain / ms, "per_n": per_n, "autotune": tune,
+               "accuracy": acc,
+               "fallbacks": {"count": int(((mixed_st & ST_FALLBACK) != 0).sum()), "of": total},
+               "kernel_times_ms": kt, "roofline": roof, "gpu_launches": launches,
+               "step_fp64_tflops": F / (ms * 1e-3) * 1e-12}
+        if clocks is not None:
+            res["clocks"] = clocks
+    if full:
+        # e2e: the same batch in page-locked host memory, results to page-locked
+        # host memory: a plan on the host buffers (kernels read and write over
+        # the host link), graph replay
+        hosts = [torch.empty(A.shape, dtype=A.dtype, pin_memory=True) for A, _ in groups]
+        for h, (A, _) in zip(hosts, groups):
+            h.copy_(A)
+        out_host = lufqhe.DetResult(*(torch.empty(total, dtype=getattr(out, k).dtype,
+                                                  pin_memory=True)
+                                      for k in ("logabs", "phase", "parity", "status")))
+        plan_h = lufqhe.Plan([(h, o) for h, (_, o) in zip(hosts, groups)], out_host,
+                             mode=lufqhe.MODE_MIXED, autotune=True, stream=stream)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks(world, timed(lambda: plan_h.execute(stream=stream), steps))
+        h2d = sum(h.numel() * h.element_size() for h in hosts)
+        d2h = sum(getattr(out_host, k).numel() * getattr(out_host, k).element_size()
+                  for k in ("logabs", "phase", "parity", "status"))
+        if res is not None:
+            res["e2e"] = {"value": world * total / (ms_e2e * 1e-3), "unit": "dets/s",
+                          "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+                          "d2h_bytes_per_step": d2h,
+                          "call": "lufqhe_plan_execute on a plan over page-locked host buffers "
+                                  "(the kernels read the matrices and write the results over the "
+                                  "host link)"}
+            import bench_cpu
+            A0 = groups[MIXED_SIZES.index(24)][0][:4096].cpu().numpy()
+            res["cpu_baseline"] = bench_cpu.cpu_baseline(np, A0, 24, seconds=args.cpu_seconds)
+        plan_h.close()
+    plan.close()
+    plan_p.close()
+    return res
+
+
+def run_serve(args, world, rank, local, full=True):
+    """Config 5: offline capacity per size class, then the Poisson walker
+    stream at 70% of it and at the configured 20k requests/s; p50/p99 latency
+    (arrival to result on the host) and throughput; mixed and (with `full`)
+    FP64 servers."""
+    import numpy as np
+    import torch
+
+    import lufqhe
+
+    torch.cuda.set_device(local)
+    seed = WORKLOADS["serving"][3]
+    rng = np.random.default_rng(seed)
+    ks = np.maximum(1, np.minimum(4096, np.floor(np.exp(rng.uniform(0, np.log(4097), 200000)))))
+    mean_k = float(ks.mean())
+    nreq = args.serve_requests if full else max(500, args.serve_requests // 2)
+
+    def offline_rate(n, mode):
+        count = max(512, min(32768, int(2e8 // (16 * n * n))))
+        A, _ = lufqhe.gen_lll(count, n, seed=seed * 100 + n)
+        out = lufqhe.batch_lup_det(A, mode=mode)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            lufqhe.batch_lup_det(A, mode=mode, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        return count / (e0.elapsed_time(e1) / 3 * 1e-3)
+
+    result = {}
+    modes = (("mixed", lufqhe.MODE_MIXED), ("fp64", lufqhe.MODE_PLAIN_FP64_FUSED))
+    for label, mode in (modes if full else modes[:1]):
+        rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
+        sec_per_matrix = float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
+        offline_mps = 1.0 / sec_per_matrix                  # matrices/s of the mix
+        cap_req = offline_mps / mean_k                      # requests/s at full load
+        inv = np.array([1.0 / rates[n] for n in SERVE_SIZES])
+        sms = np.maximum(2, np.round(152 * inv / inv.sum())).astype(int)
+        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
+        srv = lufqhe.Server(64 << 30, mode=mode, classes=SERVE_SIZES, class_sms=list(map(int, sms)),
+                            max_k=4096, tile=8)
+        runs = {}
+        for tag, rate, nr in (("at_70pct_offline", 0.7 * cap_req, nreq),
+                              ("at_20k_req_s", 20000.0, max(200, nreq // 4))):
+            lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100, k_min=1,
+                                               k_max=4096, seed=seed)
+            per = {}
+            for n in SERVE_SIZES:
+                m = ns == n
+                if m.any():
+                    per[str(n)] = {"p50_ms": float(np.percentile(lat[m], 50) / 1e3),
+                                   "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
+                                   "requests": int(m.sum())}
+            runs[tag] = {"rate_req_s": rate, "requests": int(len(lat)),
+                         "p50_ms": float(np.percentile(lat, 50) / 1e3),
+                         "p99_ms": float(np.percentile(lat, 99) / 1e3),
+                         "throughput_dets_s": mats / el,
+                         "fraction_of_offline": (mats / el) / offline_mps,
+                         "per_n": per}
+        srv.close()
+        result[label] = {"offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
+                         "offline_mix_dets_per_s": offline_mps,
+                         "offline_capacity_req_s": cap_req, "class_sms": list(map(int, sms)),
+                         "runs": runs}
+    if rank != 0:
+        return None
+    r70 = result["mixed"]["runs"]["at_70pct_offline"]
+    return {"value": r70["throughput_dets_s"], "unit": "dets/s",
+            "p50_ms": r70["p50_ms"], "p99_ms": r70["p99_ms"],
+            "fraction_of_offline": r70["fraction_of_offline"],
+            "config": workload_config("serving", world) | {"mean_k": mean_k},
+            "serving": result}
+
+
+METRIC = "determinants/s (mixed FP32+FP64-corrected, <=1e-10 rel log|det| err)"
+
+
+def base_line(args, world) -> dict:
+    return {"metric": METRIC, "n_gpus": world, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 in / fp32+float-float compute / f64 out",
+            "data": "synthetic (seeded, generated on device)"}
+
+
+def run_ours(args):
+    world, rank, local = dist_setup(args)
+    if args.workload == "mixedn":
+        r = run_plan(args, world, rank, local, full=True)
+    elif args.workload == "serving":
+        r = run_serve(args, world, rank, local, full=True)
+        if r is not None:
+            r |= {"steps": 1, "ms_per_step": None, "gpu_launches": None,
+                  "metric": "serving: determinants/s at 70% of offline load, with p50/p99 latency",
+                  "data": "synthetic (seeded Poisson walker stream)"}
+    else:
+        r = run_batched(args, world, rank, local, args.workload, full=True)
+        if args.workload == "lll24" and not args.no_subconfigs:
+            # compact results of the other configurations, in the same line
+            subs = {
+                "config1_gauss8": run_batched(args, world, rank, local, "gauss8", full=False),
+                "config2_gauss16": run_batched(args, world, rank, local, "gauss16", full=False),
+                "config4_mixedn": run_plan(args, world, rank, local, full=False),
+                "config5_serving": run_serve(args, world, rank, local, full=False),
+            }
+            if r is not None:
+                r["configs"] = subs
+    if rank == 0 and r is not None:
+        line = base_line(args, world) | r
+        print(json.dumps(line), flush=True)
+
+
+def workload_config(workload: str, world: int) -> dict:
+    """The `config` object of the JSON line, identical in both arms."""
+    kind, n, batch, seed = WORKLOADS[workload]
+    if kind in ("lll", "gauss"):
+        what = "LLL orbital" if kind == "lll" else "complex Gaussian"
+        return {"workload": f"{workload}: {batch} x n={n} {what} complex128, seed {seed}",
+                "batch": batch, "n": n, "l2": "inputs larger than L2 (no flush)",
+                "parallelism": f"replicas x{world}"}
+    if kind == "mixed":
+        return {"workload": f"mixedn: {batch} LLL matrices, n uniform over {list(MIXED_SIZES)}, "
+                            "one persistent launch in a CUDA graph",
+                "batch": batch, "l2": "inputs larger than L2 (no flush)",
+                "parallelism": f"replicas x{world}"}
+    return {"workload": "serving: Poisson move requests, k log-uniform 1..4096, n in "
+                        f"{SERVE_SIZES}, 100 moves per walker, walkers resident in HBM",
+            "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args):
-    """The reference's CPU Crout path (FP64 restatement, OpenMP over host cores)."""
+    """The reference's CPU Crout path (FP64 restatement, OpenMP over host cores).
+    Inputs come from the oracle's own generators (the same seeded draws as the
+    library's), so this arm loads nothing of the product."""
     import numpy as np
 
-    import lufqhe
+    import lufqhe_oracle
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -743,13 +860,14 @@ def run_reference(args):
 
     def make_inputs(kind, n, count, seed):
         if kind == "lll":
-            return lufqhe.gen_lll_host(count, n, seed=seed)[0]
-        return lufqhe.gen_gaussian_host(count, n, seed=seed)
+            return lufqhe_oracle.gen_lll(count, n, seed=seed)[0]
+        return lufqhe_oracle.gen_gaussian(count, n, seed=seed)
 
     kind, n, batch, seed = WORKLOADS[args.workload]
     if kind in ("mixed", "serve"):  # the reference factorises one size at a time; n=24
         kind, n, batch = "lll", 24, 32768
-    line = bench_cpu.reference_arm(np, args, kind, n, batch, seed, make_inputs)
+    line = bench_cpu.reference_arm(np, args, kind, n, batch, seed, make_inputs,
+                                   workload_config(args.workload, world))
     line["n_gpus"] = world
     print(json.dumps(line), flush=True)
 
@@ -766,6 +884,8 @@ def main():
     # 16 cores at n = 24): short steps let OpenMP start-up and box noise skew it
     ap.add_argument("--ref-sample", type=int, default=32768)
     ap.add_argument("--serve-requests", type=int, default=4000)
+    ap.add_argument("--no-subconfigs", action="store_true",
+                    help="default workload only: leave out the compact config 1/2/4/5 results")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sys.path.insert(0, str(ROOT / "oracle"))

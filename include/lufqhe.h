@@ -80,6 +80,9 @@ extern "C" {
  * (LU-fqhe/inc/LUCoreGPU.h:47, LU-fqhe/src/LUCoreGPU.cu:38-106): device batch
  * pointer, n and batch count in; per-matrix determinant out. The input is not
  * modified. Asynchronous on `stream`; no host synchronisation.
+ * dtype LUFQHE_C64 takes the reference's own float2 buffers (8-byte aligned)
+ * as they are: each entry is widened to FP64 as it is loaded (exact), so the
+ * results equal those of the batch's complex128 copy bit for bit, in every mode.
  */
 int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int dtype, int mode,
                          double *d_logabs, double *d_phase, int8_t *d_parity, int32_t *d_status,
@@ -113,6 +116,7 @@ int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode, double *d_
  * factorisation of another; pageable memory works but serialises the copies.
  * Device memory comes from the stream-ordered allocator and is released on
  * `stream`. Results are bit-identical to lufqhe_batch_lup_det's either way.
+ * dtype LUFQHE_C64 takes complex64 host matrices (half the bytes to move).
  * Asynchronous on `stream`: the results are in host memory once `stream` has
  * completed, and the batch must stay unchanged until then.
  * d_parity / d_status may be NULL as in lufqhe_batch_lup_det.
@@ -144,18 +148,35 @@ int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, int load_si
                           int pair_product, void *stream);
 
 /*
+ * The same reference-shaped call on the reference's own element type: float2
+ * matrices, exactly what LUCoreGPU::CALL(float2 **d_Matrices, ...) receives
+ * (LU-fqhe/inc/LUCoreGPU.h:47) and what its Monte Carlo loop copies to the
+ * device (LU-fqhe/src/MonteCarloLoop.cu:316-325), so that caller links
+ * unchanged. The factorisation runs in FP64 on the widened entries (plain FP64
+ * reference arithmetic); element (0,0) of every matrix receives its complex64
+ * determinant (or, with pair_product, matrix 2i the pair's product), rounded
+ * to nearest, +-inf / 0 outside the float range as the reference's float
+ * product would be; the rest of each matrix is left as L\U factors rounded to
+ * float.
+ */
+int lufqhe_lucoregpu_call_c64(void *d_matrices, int n_mat, int mat_side, int load_size,
+                              int pair_product, void *stream);
+
+/*
  * Same call as lufqhe_lucoregpu_call, for callers that cannot allocate device
- * memory once they run (a fixed device-memory budget sized at start-up, an HBM
- * admission figure, buffers owned by the caller's pool). No counterpart in the
- * reference: the reference allocates nothing inside LUCoreGPU::CALL because it
- * writes each determinant into its matrix, while this library keeps per-matrix
- * log|det|, phase and status as temporaries. Here they live in a fixed
- * 5 MiB file-scope device array held by every device that loads the library
- * until exit; nMat above LUFQHE_NOALLOC_MAX_MATRICES is rejected with
- * LUFQHE_ERR_INVALID_ARG. All calls share that array: calls whose kernels
- * overlap on the GPU race, so order them (one stream). The array's address is
- * looked up on the first call on each device; make that call before any
- * stream capture.
+ * memory once they run: a Monte Carlo driver that fixes its whole device
+ * budget at start-up, a server that admits work against a fixed HBM figure,
+ * or a host whose buffers all belong to a memory pool it owns. The per-matrix
+ * temporaries (log|det|, phase, status: 20 bytes per matrix) live in one
+ * fixed 5 MiB file-scope device array, held by every device that loads the
+ * library until the process exits, instead of stream-ordered allocations.
+ * n_mat above LUFQHE_NOALLOC_MAX_MATRICES is rejected with
+ * LUFQHE_ERR_INVALID_ARG. All calls on a device share that array and it keeps
+ * the last call's contents: calls whose kernels overlap on the GPU race, so
+ * order them (one stream). The array's device address is looked up once per
+ * device, on the first call made with that device current; make that first
+ * call before any stream capture, and do not use the library across a
+ * cudaDeviceReset (the looked-up address would be stale).
  */
 #define LUFQHE_NOALLOC_MAX_MATRICES 262144
 int lufqhe_lucoregpu_call_noalloc(void *d_matrices, int n_mat, int mat_side, int load_size,
@@ -299,6 +320,10 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
  * ||E||_F is within the threshold, in a pass of its own, before sending the
  * rest to FP64; 0 sends them all to FP64. */
 #define LUFQHE_OPT_MIXED_REFINE 5
+/* 1: the batched entry points record a CUDA event pair around every kernel
+ * they launch, on the launching stream, for lufqhe_kernel_times (not while
+ * the stream is being captured); 0 (default): no events. */
+#define LUFQHE_OPT_KERNEL_TIMING 6
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 
@@ -307,6 +332,14 @@ double lufqhe_get_option(int option);
  * kind 0 = FP64, kind 1 = FP32. Synchronises `stream`. No counterpart in the
  * reference; it supplies the roofline denominators of the benchmark. */
 int lufqhe_probe_fma_peak(int kind, double *tflops, void *stream);
+
+/* Per-kernel device times recorded while LUFQHE_OPT_KERNEL_TIMING was on:
+ * waits for the recorded events, writes a JSON object
+ * {"<kernel><n>": {"launches": L, "ms": total}, ...} into json (len bytes) and
+ * clears the record. No counterpart in the reference; it lets a benchmark
+ * time the dominant kernel of a multi-kernel call with CUDA events on the
+ * launching stream. */
+int lufqhe_kernel_times(char *json, size_t len);
 
 /* ---- misc ---- */
 /* Bytes of device memory a lufqhe_batch_lup_det call of this n, batch and mode

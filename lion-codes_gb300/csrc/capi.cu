@@ -4,7 +4,10 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
+#include <vector>
 
 #include "lufqhe_internal.cuh"
 
@@ -48,6 +51,50 @@ int check_cuda(cudaError_t e, const char *what) {
   return LUFQHE_ERR_CUDA;
 }
 
+// ---- per-kernel timing (measurement) ----------------------------------------
+int g_kernel_timing = 0;
+
+namespace {
+struct TimedLaunch {
+  std::string name;
+  cudaEvent_t e0, e1;
+};
+std::mutex g_timing_mu;
+std::vector<TimedLaunch> g_timed;
+}  // namespace
+
+KernelTimer::KernelTimer(const char *name, int n, cudaStream_t stream)
+    : name_(name), n_(n), stream_(stream) {
+  if (!g_kernel_timing) return;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return;
+  }
+  if (cudaEventCreate(&e0_) != cudaSuccess || cudaEventRecord(e0_, stream) != cudaSuccess) {
+    if (e0_) cudaEventDestroy(e0_);
+    e0_ = nullptr;
+    cudaGetLastError();
+  }
+}
+
+void KernelTimer::stop() {
+  if (!e0_) return;
+  cudaEvent_t e1 = nullptr;
+  if (cudaEventCreate(&e1) != cudaSuccess || cudaEventRecord(e1, stream_) != cudaSuccess) {
+    cudaEventDestroy(e0_);
+    if (e1) cudaEventDestroy(e1);
+    e0_ = nullptr;
+    cudaGetLastError();
+    return;
+  }
+  char label[96];
+  snprintf(label, sizeof(label), "%s<%d>", name_, n_);
+  std::lock_guard<std::mutex> lock(g_timing_mu);
+  g_timed.push_back({label, e0_, e1});
+  e0_ = nullptr;
+}
+
 int device_sm_count() {
   int s = props().sms;
   return s > 0 ? s : 1;
@@ -62,7 +109,7 @@ using namespace lufqhe;
 namespace {
 
 int check_common(const void *A, int n, int lda, long long batch, const double *logabs,
-                 const char *fn) {
+                 const char *fn, size_t align = 16) {
   if ((batch > 0 && (!A || !logabs)) || n < 1 || lda < n || batch < 0) {
     set_error("%s: invalid argument (A=%p logabs=%p n=%d lda=%d batch=%lld)", fn, A,
               (const void *)logabs, n, lda, batch);
@@ -72,8 +119,8 @@ int check_common(const void *A, int n, int lda, long long batch, const double *l
     set_error("%s: n=%d exceeds the supported maximum %d", fn, n, LUFQHE_MAX_N);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
-  if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) {  // complex128 alignment
-    set_error("%s: A must be 16-byte aligned", fn);
+  if ((reinterpret_cast<uintptr_t>(A) & (align - 1)) != 0) {  // element alignment
+    set_error("%s: A must be %zu-byte aligned", fn, align);
     return LUFQHE_ERR_INVALID_ARG;
   }
   return LUFQHE_SUCCESS;
@@ -94,6 +141,12 @@ cudaMemPool_t g_pools[64] = {};
 }  // namespace
 
 int lib_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+  // under stream capture the allocation becomes a graph memory node (graph-
+  // owned memory, its own for every instantiated graph)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) cudaGetLastError();
+  if (cap == cudaStreamCaptureStatusActive)
+    return check_cuda(cudaMallocAsync(p, bytes, s), "cudaMallocAsync (captured)");
   std::mutex &mu = g_pool_mu;
   cudaMemPool_t *pools = g_pools;
   int dev = 0;
@@ -140,9 +193,26 @@ const void *device_address(const void *p) {
   return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : p;
 }
 
-int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
-                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s,
-                     bool host_link) {
+int batch_det_device(const void *Av, int dtype, int n, int lda, long long batch, int mode,
+                     double *logabs, double *phase, int8_t *parity, int32_t *status,
+                     cudaStream_t s, bool host_link) {
+  if (dtype == LUFQHE_C64) {
+    const float2 *A = static_cast<const float2 *>(Av);
+    switch (mode) {
+      case LUFQHE_MODE_PLAIN_FP64:
+        return launch_plain32(A, nullptr, n, lda, batch, ARITH_REF, logabs, phase, parity, status,
+                              s);
+      case LUFQHE_MODE_PLAIN_FP64_FUSED:
+        return launch_plain32(A, nullptr, n, lda, batch, ARITH_FUSED, logabs, phase, parity,
+                              status, s);
+      case LUFQHE_MODE_MIXED:
+        return launch_mixed32(A, n, lda, batch, logabs, phase, parity, status, s);
+      default:
+        set_error("lufqhe_batch_lup_det: unknown mode %d", mode);
+        return LUFQHE_ERR_UNSUPPORTED_MODE;
+    }
+  }
+  const double2 *A = static_cast<const double2 *>(Av);
   switch (mode) {
     case LUFQHE_MODE_PLAIN_FP64:
       return launch_plain(A, nullptr, n, lda, batch, ARITH_REF, logabs, phase, parity, status, s);
@@ -162,14 +232,14 @@ int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode
 extern "C" int lufqhe_batch_lup_det(const void *d_A, int n, int lda, long long batch, int dtype,
                                     int mode, double *d_logabs, double *d_phase,
                                     int8_t *d_parity, int32_t *d_status, void *stream) {
-  int rc = check_common(d_A, n, lda, batch, d_logabs, "lufqhe_batch_lup_det");
-  if (rc) return rc;
-  if (dtype != LUFQHE_C128) {
-    set_error("lufqhe_batch_lup_det: dtype %d not supported (complex128 only)", dtype);
+  if (!dtype_bytes(dtype)) {
+    set_error("lufqhe_batch_lup_det: unknown dtype %d", dtype);
     return LUFQHE_ERR_UNSUPPORTED_MODE;
   }
-  return batch_det_device(reinterpret_cast<const double2 *>(d_A), n, lda, batch, mode, d_logabs,
-                          d_phase, d_parity, d_status, (cudaStream_t)stream, false);
+  int rc = check_common(d_A, n, lda, batch, d_logabs, "lufqhe_batch_lup_det", dtype_bytes(dtype));
+  if (rc) return rc;
+  return batch_det_device(d_A, dtype, n, lda, batch, mode, d_logabs, d_phase, d_parity, d_status,
+                          (cudaStream_t)stream, false);
 }
 
 extern "C" int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode,
@@ -243,8 +313,36 @@ extern "C" int lufqhe_lucoregpu_call(void *d_matrices, int n_mat, int mat_side, 
   return rc ? rc : rc2;
 }
 
+extern "C" int lufqhe_lucoregpu_call_c64(void *d_matrices, int n_mat, int mat_side,
+                                         int load_size, int pair_product, void *stream) {
+  if (!d_matrices || n_mat < 0 || mat_side < 1 || load_size < mat_side ||
+      (reinterpret_cast<uintptr_t>(d_matrices) & 7) != 0) {
+    set_error("lufqhe_lucoregpu_call_c64: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  if (mat_side > LUFQHE_MAX_N) {
+    set_error("lufqhe_lucoregpu_call_c64: matSide=%d exceeds %d", mat_side, LUFQHE_MAX_N);
+    return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+  if (n_mat == 0) return LUFQHE_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  void *tmp = nullptr;
+  size_t bytes = (size_t)n_mat * (2 * sizeof(double) + sizeof(int32_t));
+  int rc = lib_malloc_async(&tmp, bytes, s);
+  if (rc) return rc;
+  double *la = static_cast<double *>(tmp);
+  double *ph = la + n_mat;
+  int32_t *st = reinterpret_cast<int32_t *>(ph + n_mat);
+  float2 *A = reinterpret_cast<float2 *>(d_matrices);
+  rc = launch_plain32(A, A, mat_side, load_size, n_mat, ARITH_REF, la, ph, nullptr, st, s);
+  if (!rc) rc = launch_write_det32(A, mat_side, load_size, n_mat, la, ph, st, pair_product, s);
+  int rc2 = lib_free_async(tmp, s);
+  return rc ? rc : rc2;
+}
+
 namespace lufqhe {
 extern float g_mixed_theta;
+extern int g_kernel_timing;
 extern int g_tile_warps;
 extern float g_fp64_share;
 extern int g_host_chunk_mb;
@@ -292,6 +390,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_mixed_refine = (int)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_KERNEL_TIMING) {
+    if (!(value == 0.0 || value == 1.0)) {
+      set_error("lufqhe_set_option: kernel timing must be 0 or 1");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_kernel_timing = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   set_error("lufqhe_set_option: unknown option %d", option);
   return LUFQHE_ERR_INVALID_ARG;
 }
@@ -302,6 +408,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_FP64_SHARE) return (double)g_fp64_share;
   if (option == LUFQHE_OPT_HOST_CHUNK_MB) return (double)g_host_chunk_mb;
   if (option == LUFQHE_OPT_MIXED_REFINE) return (double)g_mixed_refine;
+  if (option == LUFQHE_OPT_KERNEL_TIMING) return (double)g_kernel_timing;
   return NAN;
 }
 
@@ -312,6 +419,48 @@ extern "C" int lufqhe_release_workspace(void) {
     const int rc = check_cuda(cudaMemPoolTrimTo(pool, 0), "cudaMemPoolTrimTo");
     if (rc) return rc;
   }
+  return LUFQHE_SUCCESS;
+}
+
+extern "C" int lufqhe_kernel_times(char *json, size_t len) {
+  if (!json || len == 0) {
+    set_error("lufqhe_kernel_times: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  std::vector<TimedLaunch> recs;
+  {
+    std::lock_guard<std::mutex> lock(lufqhe::g_timing_mu);
+    recs.swap(lufqhe::g_timed);
+  }
+  std::map<std::string, std::pair<long long, double>> agg;
+  int rc = LUFQHE_SUCCESS;
+  for (const TimedLaunch &r : recs) {
+    float ms = 0.0f;
+    if (!rc) rc = check_cuda(cudaEventSynchronize(r.e1), "cudaEventSynchronize(kernel timing)");
+    if (!rc) rc = check_cuda(cudaEventElapsedTime(&ms, r.e0, r.e1), "cudaEventElapsedTime");
+    cudaEventDestroy(r.e0);
+    cudaEventDestroy(r.e1);
+    if (!rc) {
+      auto &a = agg[r.name];
+      a.first += 1;
+      a.second += ms;
+    }
+  }
+  if (rc) return rc;
+  std::string out = "{";
+  for (const auto &kv : agg) {
+    char item[192];
+    snprintf(item, sizeof(item), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}",
+             out.size() > 1 ? ", " : "", kv.first.c_str(), kv.second.first, kv.second.second);
+    out += item;
+  }
+  out += "}";
+  if (out.size() + 1 > len) {
+    set_error("lufqhe_kernel_times: buffer of %zu bytes holds less than %zu", len,
+              out.size() + 1);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  memcpy(json, out.c_str(), out.size() + 1);
   return LUFQHE_SUCCESS;
 }
 

@@ -440,10 +440,13 @@ int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
     // a warp-group CTA takes one item at a time
     const long long want = pass == 2 ? L.nitems : (L.nitems + L.warps - 1) / L.warps;
     const int grid = (int)std::min<long long>(L.ctas, want);
+    static const char *names[3] = {"grouped_kernel", "grouped_kernel_fp64", "grouped_group_kernel"};
+    KernelTimer timer(names[pass], L.nf, s);
     k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
                                                        p->refine,
                                                        p->logabs, p->phase, p->parity, p->status);
+    timer.stop();
     rc = check_cuda(cudaGetLastError(), "grouped_kernel launch");
   }
   return rc;
@@ -675,7 +678,15 @@ extern "C" int lufqhe_plan_describe(const lufqhe_plan_t *plan, char *buf, size_t
     set_error("lufqhe_plan_describe: invalid argument");
     return LUFQHE_ERR_INVALID_ARG;
   }
-  snprintf(buf, len, "%s", plan->report.c_str());
+  // the report is one JSON object: add the kernels one execution launches
+  int kernels = 0;
+  for (const Launch &L : plan->launch) kernels += (L.nitems > 0 && L.ctas > 0) ? 1 : 0;
+  std::string r = plan->report;
+  const size_t close = r.rfind('}');
+  if (close != std::string::npos)
+    r.insert(close, std::string(r.size() > 2 ? ", " : "") + "\"kernels\": " +
+                        std::to_string(kernels));
+  snprintf(buf, len, "%s", r.c_str());
   return LUFQHE_SUCCESS;
 }
 

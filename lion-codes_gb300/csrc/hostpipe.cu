@@ -64,10 +64,6 @@ int pipe_streams(PipeStreams *out) {
 
 int g_host_chunk_mb = 32;  // input bytes per chunk, MiB
 
-int batch_det_device(const double2 *A, int n, int lda, long long batch, int mode, double *logabs,
-                     double *phase, int8_t *parity, int32_t *status, cudaStream_t s,
-                     bool host_link);
-
 namespace {
 
 // Device view of page-locked host memory, or null (pageable, device or null p).
@@ -82,14 +78,14 @@ void *mapped_view(const void *p) {
 }
 
 // Mixed mode on a pinned batch: one launch reading over the host link.
-int det_over_link(const double2 *dA, int n, int lda, long long batch, double *h_logabs,
+int det_over_link(const void *dA, int dtype, int n, int lda, long long batch, double *h_logabs,
                   double *h_phase, int8_t *h_parity, int32_t *h_status, cudaStream_t s) {
   double *la = static_cast<double *>(mapped_view(h_logabs));
   double *ph = static_cast<double *>(mapped_view(h_phase));
   int8_t *pa = static_cast<int8_t *>(mapped_view(h_parity));
   int32_t *st = static_cast<int32_t *>(mapped_view(h_status));
   if (la && (!h_phase || ph) && (!h_parity || pa) && (!h_status || st))
-    return batch_det_device(dA, n, lda, batch, LUFQHE_MODE_MIXED, la, ph, pa, st, s, true);
+    return batch_det_device(dA, dtype, n, lda, batch, LUFQHE_MODE_MIXED, la, ph, pa, st, s, true);
   // pageable outputs: device results, then copies
   const size_t nb = (size_t)batch;
   unsigned char *buf = nullptr;
@@ -100,7 +96,7 @@ int det_over_link(const double2 *dA, int n, int lda, long long batch, double *h_
   double *dph = dla + nb;
   int32_t *dst = reinterpret_cast<int32_t *>(dph + nb);
   int8_t *dpa = reinterpret_cast<int8_t *>(dst + nb);
-  rc = batch_det_device(dA, n, lda, batch, LUFQHE_MODE_MIXED, dla, h_phase ? dph : nullptr,
+  rc = batch_det_device(dA, dtype, n, lda, batch, LUFQHE_MODE_MIXED, dla, h_phase ? dph : nullptr,
                         h_parity ? dpa : nullptr, h_status ? dst : nullptr, s, true);
   if (!rc)
     rc = check_cuda(cudaMemcpyAsync(h_logabs, dla, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
@@ -136,8 +132,8 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
               LUFQHE_MAX_N);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
-  if (dtype != LUFQHE_C128) {
-    set_error("lufqhe_batch_lup_det_host: dtype %d not supported (complex128 only)", dtype);
+  if (!dtype_bytes(dtype)) {
+    set_error("lufqhe_batch_lup_det_host: unknown dtype %d", dtype);
     return LUFQHE_ERR_UNSUPPORTED_MODE;
   }
   if (mode != LUFQHE_MODE_PLAIN_FP64 && mode != LUFQHE_MODE_PLAIN_FP64_FUSED &&
@@ -149,13 +145,12 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
   cudaStream_t user = (cudaStream_t)stream;
   if (mode == LUFQHE_MODE_MIXED)
     if (const void *dA = mapped_view(h_A))
-      return det_over_link(static_cast<const double2 *>(dA), n, lda, batch, h_logabs, h_phase,
-                           h_parity, h_status, user);
+      return det_over_link(dA, dtype, n, lda, batch, h_logabs, h_phase, h_parity, h_status, user);
   PipeStreams ps;
   int rc = pipe_streams(&ps);
   if (rc) return rc;
 
-  const size_t mat_bytes = (size_t)n * lda * sizeof(double2);
+  const size_t mat_bytes = (size_t)n * lda * dtype_bytes(dtype);
   long long per_chunk = (long long)(((size_t)g_host_chunk_mb << 20) / mat_bytes);
   if (per_chunk < 1) per_chunk = 1;
   const long long chunks = (batch + per_chunk - 1) / per_chunk;
@@ -183,7 +178,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
     const long long lo = c * per_chunk;
     const long long cnt = (lo + per_chunk <= batch) ? per_chunk : batch - lo;
     unsigned char *buf = stage + (size_t)k * buf_bytes;
-    double2 *dA = reinterpret_cast<double2 *>(buf);
+    void *dA = buf;
     double *dla = reinterpret_cast<double *>(buf + ((in_bytes + 255) & ~(size_t)255));
     double *dph = dla + per_chunk;
     int32_t *dst = reinterpret_cast<int32_t *>(dph + per_chunk);
@@ -192,7 +187,7 @@ extern "C" int lufqhe_batch_lup_det_host(const void *h_A, int n, int lda, long l
                                     cudaMemcpyHostToDevice, s),
                     "H2D chunk");
     if (!rc)
-      rc = batch_det_device(dA, n, lda, cnt, mode, dla, h_phase ? dph : nullptr,
+      rc = batch_det_device(dA, dtype, n, lda, cnt, mode, dla, h_phase ? dph : nullptr,
                             h_parity ? dpa : nullptr, h_status ? dst : nullptr, s, false);
     if (!rc)
       rc = check_cuda(cudaMemcpyAsync(h_logabs + lo, dla, (size_t)cnt * sizeof(double),

@@ -27,6 +27,24 @@ int lib_free_async(void *p, cudaStream_t s);
 // Bytes a batched mixed call of this n and batch takes from that pool.
 size_t mixed_workspace_bytes(int n, long long batch);
 
+// Per-kernel timing for measurement (option LUFQHE_OPT_KERNEL_TIMING): while
+// it is on, a KernelTimer records a CUDA event on the launching stream before
+// and after the launch it brackets, and files the pair under the kernel's
+// name (with n) for lufqhe_kernel_times. Off (the default), or while the
+// stream is being captured, it does nothing.
+class KernelTimer {
+ public:
+  KernelTimer(const char *name, int n, cudaStream_t stream);
+  void stop();
+  ~KernelTimer() { stop(); }
+
+ private:
+  const char *name_;
+  int n_;
+  cudaStream_t stream_;
+  cudaEvent_t e0_ = nullptr;
+};
+
 // ---- IEEE helpers ----------------------------------------------------------
 __device__ __forceinline__ bool finite_d(double v) {
   return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000;
@@ -206,5 +224,22 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,
                      const double *phase, const int32_t *status, int pair_product,
                      cudaStream_t stream);
+// complex64 batches (the reference's float2 buffers): widened to FP64 on load
+int launch_plain32(const float2 *A, float2 *Aout, int n, int lda, long long batch, int arith,
+                   double *logabs, double *phase, int8_t *parity, int32_t *status,
+                   cudaStream_t stream, int status_or = 0);
+int launch_mixed32(const float2 *A, int n, int lda, long long batch, double *logabs,
+                   double *phase, int8_t *parity, int32_t *status, cudaStream_t stream);
+int launch_write_det32(float2 *A, int n, int lda, long long batch, const double *logabs,
+                       const double *phase, const int32_t *status, int pair_product,
+                       cudaStream_t stream);
+// Batched call on device (or mapped) memory of either element type.
+int batch_det_device(const void *A, int dtype, int n, int lda, long long batch, int mode,
+                     double *logabs, double *phase, int8_t *parity, int32_t *status,
+                     cudaStream_t s, bool host_link);
+// Bytes of one matrix element of dtype (LUFQHE_C128 / LUFQHE_C64), 0 if unknown.
+inline size_t dtype_bytes(int dtype) {
+  return dtype == LUFQHE_C128 ? 16 : dtype == LUFQHE_C64 ? 8 : 0;
+}
 
 }  // namespace lufqhe

@@ -131,6 +131,57 @@ struct DenseSource {
   }
 };
 
+// complex64 matrices in the reference layout: the reference's own buffer type
+// (LUCoreGPU::CALL takes float2 matrices, LU-fqhe/inc/LUCoreGPU.h:47). Each
+// entry is widened to FP64 as it is loaded, which is exact, so a complex64
+// batch gives the results of its complex128 copy bit for bit.
+struct Dense32Source {
+  const float2 *A;
+  int lda;
+  __device__ __forceinline__ static double2 widen(float2 v) {
+    return make_double2((double)v.x, (double)v.y);
+  }
+  template <bool COHERENT = false>
+  __device__ __forceinline__ bool load(long long b, int n, double2 *M, int lds, int lane) const {
+    const float2 *src = A + (size_t)b * n * lda;
+    bool bad = false;
+    BlockWalk w(lane, n);
+    for (int e = lane; e < n * n; e += 32) {
+      const float2 *p = src + (size_t)w.i * lda + w.k;
+      const double2 v = widen(COHERENT ? __ldcg(p) : __ldg(p));
+      bad |= !finite_c(v);
+      M[w.i * lds + w.k] = v;
+      w.next(n);
+    }
+    bad = __any_sync(kFull, bad);
+    __syncwarp();
+    return bad;
+  }
+  __device__ __forceinline__ double2 first(long long b, int n) const {
+    return widen(__ldg(A + (size_t)b * n * lda));
+  }
+  __device__ __forceinline__ bool load_group(long long b, int n, double2 *M, int lds, int tid,
+                                             int nthr) const {
+    const float2 *src = A + (size_t)b * n * lda;
+    bool bad = false;
+    StrideWalk w(tid, nthr, n);
+    for (int e = tid; e < n * n; e += nthr) {
+      const double2 v = widen(__ldg(src + (size_t)w.i * lda + w.k));
+      bad |= !finite_c(v);
+      M[w.i * lds + w.k] = v;
+      w.next(n);
+    }
+    return __syncthreads_or(bad);
+  }
+};
+
+// Store of an FP64 entry into a caller's matrix of either element type (the
+// in-place factors of the reference-shaped call; complex64 rounds to nearest).
+__device__ __forceinline__ void store_entry(double2 *p, double2 v) { *p = v; }
+__device__ __forceinline__ void store_entry(float2 *p, double2 v) {
+  *p = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+}
+
 struct LllSource {
   const double2 *Z;
   template <bool COHERENT = false>

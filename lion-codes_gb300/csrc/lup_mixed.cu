@@ -1,57 +1,8 @@
-// Mixed-precision batched complex LUP determinant.
-//
-// Per matrix (one warp, shared memory), with FP64 used only where accuracy
-// needs it and almost all arithmetic on the FP32 and integer pipes, which on
-// GB300 run far faster than FP64:
-//  1. power-of-two column-then-row equilibration A^ = D_r^-1 A D_c^-1, chosen
-//     from the exponent fields (exact; log|det D| is added back in FP64);
-//  2. split of every scaled FP64 entry into float hi + lo by integer
-//     operations (48 significant bits kept);
-//  3. FP32 complex LUP of hi with partial pivoting on |Re|+|Im|; alongside,
-//     the residual R = P A^ - L U is accumulated exactly in float-float
-//     (Ogita-Rump-Oishi Dot2: TwoProd + TwoSum per real product, the real
-//     and imaginary parts as packed FP32 pairs), starting from hi + lo, so R
-//     carries FP64-level accuracy although every operation is an FP32 one;
-//  4. E = U^-1 L^-1 R by FP32 triangular solves;
-//  5. log det(I + E) by an unpivoted FP32 LU that keeps the identity implicit
-//     (only the small offsets are stored), log1p/atan2 of each pivot, or, for
-//     the register-tiled sizes when ||E|| is small enough that the dropped
-//     terms stay below 1e-12 max(1, |log|det||), by tr E - tr(E^2)/2;
-//  6. log|det| = log|prod u_jj| (complex float-float product, one FP64 log
-//     and atan2 per matrix, deferred and done for 32 matrices at once by the
-//     32 lanes) + equilibration + Re log det(I+E); phase likewise.
-// A matrix whose ||E||_F exceeds the threshold, or whose FP32 factorisation
-// meets a zero or non-finite pivot, is refactorised by the FP64 warp routine
-// (reference pivot rule, fused arithmetic) and flagged LUFQHE_ST_FALLBACK.
-// The permutation parity reported is that of the pivoting actually used.
-//
-// Warps take matrices from a work counter rather than a fixed grid stride: a
-// matrix refactorised in FP64 costs many times an accepted one, and a fixed
-// share of the batch per warp would leave the kernel waiting on the warps
-// that drew the most of them. For n >= 24 the refinements and FP64
-// refactorisations run after the FP32 pass, in a second kernel on the same
-// stream that has the whole GPU: the FP32 pass saves a matrix whose
-// correction is within theta but beyond what FP32 solves carry (its L\U and
-// Y = L^-1 R) for one refinement step of the back substitution, and appends
-// the index of a rejected matrix to a pending list in static device memory;
-// the second kernel deals the list's entries out to its warps at a fixed
-// stride for FP64 while the other warps refine the saved matrices, so the FP64
-// and FP32 pipes work side by side. If the list is full, the n >= 24 FP32
-// kernels (which hold no FP64 factorisation code) mark the matrix in logabs
-// and the second kernel scans for the marks; the others refactorise it in
-// place. For n < 24 the FP64 refactorisations are cheap and rare enough that
-// the second launch costs more than it saves; there the FP32 pass refines and
-// refactorises in place, and so does the n >= 24 variant that reads its batch
-// over the host link (INPLACE). The kernels take their matrices from a source:
-// dense matrices in the reference layout, or lowest-Landau-level orbital
-// matrices built from particle coordinates.
+// Mixed-precision batched complex LUP determinant: complex128 and
+// lowest-Landau-level entry points, the precision policy and the options.
+// The method and its kernels are described in mixed_kernels.cuh.
 
-#include <algorithm>
-#include <atomic>
-#include <cmath>
-#include <type_traits>
-
-#include "mixed_core.cuh"
+#include "mixed_kernels.cuh"
 
 namespace lufqhe {
 
@@ -74,585 +25,6 @@ unsigned int fp64_share_64k(int n) {
   return (unsigned int)(s * 65536.0f);
 }
 
-namespace {
-
-using namespace mixed;
-
-// Warps per CTA and CTAs per SM the register-tiled kernels are compiled for:
-// the register budget this leaves (65536 / (32 warps blocks)) is what lets the
-// SM hold that many warps, whichever of registers or shared memory binds.
-// n = 24: 3-warp CTAs, 5 per SM (15 KB of shared memory per warp); n <= 16:
-// 4-warp CTAs, 4 per SM; n = 32: shared memory allows 8 warps whatever the
-// registers.
-constexpr int tile_max_warps(int n) { return n == 24 ? 3 : 4; }
-constexpr int tile_min_ctas(int n) { return n == 24 ? 5 : n == 32 ? 1 : 4; }
-
-// Work counters of the batched mixed kernels, {claims after the first, CTAs
-// done} per slot. Static device memory starts at zero; each launch takes the
-// next slot in turn and its last CTA sets the slot back to zero, so a slot is
-// free again unless 4096 later launches were issued while it still ran.
-constexpr int kWorkSlots = 4096;
-__device__ unsigned long long g_work[kWorkSlots][2];
-std::atomic<unsigned int> g_work_seq{0};
-
-int next_work_slot() { return (int)(g_work_seq.fetch_add(1u) % kWorkSlots); }
-
-// A warp's first matrix is its own index in the grid; later ones come from
-// the slot's counter, after the grid's warps. Small batches, where most warps
-// take one matrix, then make no same-address atomics at the start (n=8, 4096
-// matrices: 31.0 -> 28.9 us).
-__device__ __forceinline__ long long claim_matrix(int slot, int lane, bool first) {
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  if (first) return (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  unsigned long long b = 0;
-  if (lane == 0) b = atomicAdd(&g_work[slot][0], 1ull);
-  return (long long)__shfl_sync(kFull, b, 0) + warps;
-}
-
-// Pending lists of the FP64 pass, taken in turn by the calls: 256 lists of
-// 16384 entries (16 MiB). A list is busy only from a call's FP32 pass to the
-// end of its FP64 pass, so 256 calls would have to be in flight at once for
-// two to share one; a call with more rejections than a list holds marks the
-// rest in logabs for the FP64 pass's scan.
-constexpr int kPendSlots = 256;
-constexpr unsigned int kPendCap = 1u << 14;
-__device__ unsigned int g_pend[kPendSlots][kPendCap];
-__device__ unsigned int g_pend_count[kPendSlots];
-__device__ unsigned int g_pend_over[kPendSlots];  // some matrix found the list full
-
-// List entries: the matrix index, with this bit set for the FP64 route (status
-// flag LUFQHE_ST_FP64) rather than a rejection (LUFQHE_ST_FALLBACK).
-constexpr unsigned int kPendRouted = 0x80000000u;
-// logabs bits of a matrix that found the list full: the FP64 pass then scans
-// logabs for them (a quiet NaN payload no log-determinant takes)
-constexpr long long kOverFallbackBits = 0x7ff8c0ffee5eed01ll;
-constexpr long long kOverRoutedBits = 0x7ff8c0ffee5eed02ll;
-std::atomic<unsigned int> g_pend_seq{0};
-
-int next_pend_slot() { return (int)(g_pend_seq.fetch_add(1u) % kPendSlots); }
-
-constexpr int kDeferMinN = 24;
-// Warps of the FP64 pass's CTA (one CTA per SM).
-constexpr int kFallbackMaxWarps = 20;
-
-// Hand matrix b to the FP64 pass; false (warp-uniform) if there is none
-// (pslot < 0) or its list is full.
-__device__ __forceinline__ bool defer_fp64(int pslot, long long b, int lane, bool routed) {
-  if (pslot < 0 || b >= (long long)kPendRouted) return false;
-  unsigned int pos = 0;
-  if (lane == 0) pos = atomicAdd(&g_pend_count[pslot], 1u);
-  pos = __shfl_sync(kFull, pos, 0);
-  if (pos >= kPendCap) return false;
-  if (lane == 0) g_pend[pslot][pos] = (unsigned int)b | (routed ? kPendRouted : 0u);
-  return true;
-}
-
-// Same, for a kernel that holds no FP64 factorisation of its own: a matrix
-// that finds the list full is marked in logabs for the FP64 pass's scan.
-__device__ __forceinline__ void defer_fp64_always(int pslot, long long b, int lane, bool routed,
-                                                  double *logabs) {
-  if (defer_fp64(pslot, b, lane, routed)) return;
-  if (lane == 0) {
-    logabs[b] = __longlong_as_double(routed ? kOverRoutedBits : kOverFallbackBits);
-    atomicOr(&g_pend_over[pslot], 1u);
-  }
-}
-
-// Once per CTA, after all its warps have left their loops (every warp of the
-// kernels that call this reaches it: their loops end only by break).
-__device__ __forceinline__ void release_slot(int slot, int lane) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
-      // every warp has made its last claim: reset for the slot's next launch
-      atomicExch(&g_work[slot][0], 0ull);
-      atomicExch(&g_work[slot][1], 0ull);
-    }
-  }
-}
-
-// Matrices the FP32 pass leaves for a refinement of the back substitution
-// (TILE_REFINE): per matrix a header and the warp's L\U and Y = L^-1 R as they
-// lie in shared memory (row stride N + 1), in a call-local device buffer that
-// starts with two 64-bit counters {saved, claimed}.
-struct RefineHead {
-  long long b;
-  int exp_sum, par, prod_e, pad;
-  float xh, xl, yh, yl;
-};
-constexpr size_t kRefineHeadBytes = 256;  // the counters, before entry 0
-template <int N>
-constexpr size_t refine_entry_bytes() {
-  return (sizeof(RefineHead) + 2 * (size_t)N * (N + 1) * sizeof(float2) + 15) & ~(size_t)15;
-}
-// Share of a batch the refinement buffer has room for (the rest go straight
-// to the FP64 pass): on lowest-Landau-level n = 24 matrices about 9% qualify.
-constexpr double kRefineShare = 0.25;
-
-// Save a TILE_REFINE matrix; false (warp-uniform) if the buffer is full.
-template <int N>
-__device__ bool save_refine(unsigned char *buf, long long cap, long long b, const float2 *F,
-                            const float2 *Rm, const CFF &prod, int exp_sum, int par, int lane) {
-  constexpr int NL = N * (N + 1);
-  unsigned long long k = 0;
-  if (lane == 0) k = atomicAdd(reinterpret_cast<unsigned long long *>(buf), 1ull);
-  k = __shfl_sync(kFull, k, 0);
-  if (k >= (unsigned long long)cap) return false;
-  unsigned char *e = buf + kRefineHeadBytes + k * refine_entry_bytes<N>();
-  float2 *dF = reinterpret_cast<float2 *>(e + sizeof(RefineHead));
-  float2 *dY = dF + NL;
-  for (int q = lane; q < NL; q += 32) {
-    dF[q] = F[q];
-    dY[q] = Rm[q];
-  }
-  if (lane == 0) {
-    RefineHead h;
-    h.b = b;
-    h.exp_sum = exp_sum;
-    h.par = par;
-    h.prod_e = prod.e;
-    h.pad = 0;
-    h.xh = prod.xh;
-    h.xl = prod.xl;
-    h.yh = prod.yh;
-    h.yl = prod.yl;
-    *reinterpret_cast<RefineHead *>(e) = h;
-  }
-  return true;
-}
-
-template <class Src>
-__global__ void __launch_bounds__(kMaxWarpsMixed * 32)
-    lup_mixed_kernel(Src src, int n, long long batch,
-                     float theta2, unsigned int share64k, int slot, int pslot,
-                     double *__restrict__ logabs, double *__restrict__ phase,
-                     int8_t *__restrict__ parity, int32_t *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int lds = n + 1;
-  const size_t nl = (size_t)n * lds;
-  MixedSmem S;
-  unsigned char *base = smem_raw;
-  S.SC = reinterpret_cast<float4 *>(base) + warp * nl;
-  base += warps * nl * sizeof(float4);
-  S.Af = reinterpret_cast<float2 *>(base) + warp * nl;
-  base += warps * nl * sizeof(float2);
-  S.hold = reinterpret_cast<double *>(base) + warp * 2 * n;
-  base += warps * 2 * (size_t)n * sizeof(double);
-  S.er = reinterpret_cast<int *>(base) + warp * 2 * n;
-  S.ec = S.er + n;
-
-  DeferredOut out;
-  for (bool first = true;; first = false) {
-    const long long b = claim_matrix(slot, lane, first);
-    if (b >= batch) break;
-    __syncwarp();
-    double2 *M = reinterpret_cast<double2 *>(S.SC);
-    if (share64k && route_fp64_entry(src.first(b, n), share64k)) {
-      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status,
-                        LUFQHE_ST_FP64);
-      continue;
-    }
-    if (src.load(b, n, M, lds, lane)) {
-      emit_nonfinite(lane, b, logabs, phase, parity, status);
-      continue;
-    }
-    CFF prod;
-    int exp_sum, par;
-    float2 corr;
-    if (mixed_factor(S, n, lane, theta2, prod, exp_sum, corr, par))
-      out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-    else if (!defer_fp64(pslot, b, lane, false))
-      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status);
-  }
-  out.flush(lane, logabs, phase, parity, status);
-  release_slot(slot, lane);
-}
-
-
-template <int N, class Src, bool INPLACE = false>
-__global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
-    lup_mixed_tile_kernel(Src src, long long batch, float theta2,
-                          unsigned int share64k, int slot, int pslot, double2 *spill,
-                          unsigned char *refine, long long refine_cap,
-                          double *__restrict__ logabs,
-                          double *__restrict__ phase, int8_t *__restrict__ parity,
-                          int32_t *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  // n >= 24: every FP64 factorisation goes to the FP64 pass, so this kernel
-  // carries no FP64 factorisation code (a smaller instruction footprint).
-  // INPLACE keeps them in this kernel: for a batch read over the host link,
-  // where the FP32 pass waits on the link and has compute to spare.
-  constexpr bool DEFER = !INPLACE && N >= kDeferMinN;
-  constexpr int LDS = N + 1;
-  constexpr size_t NL = (size_t)N * LDS;
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  unsigned char *base = smem_raw;
-  float4 *HL = reinterpret_cast<float4 *>(base) + warp * NL;
-  base += warps * NL * sizeof(float4);
-  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
-  base += warps * NL * sizeof(float2);
-  double *hold = reinterpret_cast<double *>(base) + warp * 2 * N;
-  base += warps * 2 * (size_t)N * sizeof(double);
-  int *er = reinterpret_cast<int *>(base) + warp * 2 * N;
-  int *ec = er + N;
-  // INPLACE: this warp's copy of its current matrix in global memory (a few
-  // KB per warp, so the copies stay in L2); an FP64 refactorisation reloads
-  // it from there instead of reading the matrix over the host link again
-  double2 *own = INPLACE ? spill + ((size_t)blockIdx.x * warps + warp) * N * N : nullptr;
-
-  DeferredOut out;
-  for (bool first = true;; first = false) {
-    const long long b = claim_matrix(slot, lane, first);
-    if (b >= batch) break;
-    __syncwarp();
-    double2 *M = reinterpret_cast<double2 *>(HL);
-    if (share64k && route_fp64_entry(src.first(b, N), share64k)) {
-      if constexpr (DEFER)
-        defer_fp64_always(pslot, b, lane, true, logabs);
-      else
-        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                          LUFQHE_ST_FP64);
-      continue;
-    }
-    if (src.load(b, N, M, LDS, lane)) {
-      emit_nonfinite(lane, b, logabs, phase, parity, status);
-      continue;
-    }
-    if constexpr (INPLACE) {
-      BlockWalk w(lane, N);
-      for (int e = lane; e < N * N; e += 32) {
-        own[e] = M[w.i * LDS + w.k];
-        w.next(N);
-      }
-    }
-    CFF prod;
-    int exp_sum, par;
-    float2 corr;
-    if constexpr (DEFER) {
-      const int code =
-          mixed_factor_tile_ex<N, true>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
-      if (code == TILE_ACCEPT)
-        out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-      // a matrix within theta but above the FP32 solves' cap gets its back
-      // substitution refined in the next pass, if the buffer has room
-      else if (!(code == TILE_REFINE && refine &&
-                 save_refine<N>(refine, refine_cap, b, F, reinterpret_cast<const float2 *>(HL),
-                                prod, exp_sum, par, lane)))
-        defer_fp64_always(pslot, b, lane, false, logabs);
-    } else {
-      // in place: the refinement (refine_cap != 0), then FP64 (n < 24, where
-      // both are rare, and the host-link variant, which has compute to spare)
-      if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par,
-                               refine_cap != 0))
-        out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-      else if constexpr (INPLACE)
-        fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
-                                             logabs, phase, parity, status);
-      else
-        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
-    }
-  }
-  out.flush(lane, logabs, phase, parity, status);
-  release_slot(slot, lane);
-}
-
-// The passes after the FP32 pass, as one kernel in the FP32 pass's
-// shared-memory layout (n >= 24): the FP64 refactorisations of the matrices
-// the FP32 pass rejected, dealt out at a fixed stride over the grid's warps
-// first, while the warps without one refine the saved matrices (claimed one at
-// a time; a refinement that fails is refactorised in FP64 on the spot). The
-// FP64 pipe and the FP32 pipes then work side by side instead of one pass
-// after the other. Matrices past a full pending list are found in chunks of
-// 32 whose logabs the FP32 pass marked. The last CTA out empties the list.
-template <int N, class Src>
-__global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
-    lup_mixed_finish_kernel(Src src, long long batch, const unsigned char *refine,
-                            long long refine_cap, float theta2, int slot, int pslot,
-                            double *__restrict__ logabs, double *__restrict__ phase,
-                            int8_t *__restrict__ parity, int32_t *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int LDS = N + 1;
-  constexpr size_t NL = (size_t)N * LDS;
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  unsigned char *base = smem_raw;
-  float4 *HL = reinterpret_cast<float4 *>(base) + warp * NL;
-  double2 *M = reinterpret_cast<double2 *>(HL);
-  float2 *Rm = reinterpret_cast<float2 *>(HL);
-  base += warps * NL * sizeof(float4);
-  float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
-  base += warps * NL * sizeof(float2);
-  double *hold = reinterpret_cast<double *>(base) + warp * 2 * N;
-  base += warps * 2 * (size_t)N * sizeof(double);
-  float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
-  __shared__ unsigned int cta_done;
-  if (threadIdx.x == 0) cta_done = 0u;
-  __syncthreads();
-  // 1. the FP32 pass's rejections, dealt out
-  const unsigned long long listed =
-      min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
-  const unsigned long long chunks =
-      *(volatile unsigned int *)&g_pend_over[pslot] ? (unsigned long long)(batch + 31) / 32 : 0ull;
-  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
-  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
-       j += stride) {
-    const unsigned int e = g_pend[pslot][j];
-    const long long b = e & ~kPendRouted;
-    fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
-  }
-  // 2. the saved matrices, claimed; a failed refinement is refactorised here
-  DeferredOut out;
-  if (refine) {
-    unsigned long long *ctr =
-        reinterpret_cast<unsigned long long *>(const_cast<unsigned char *>(refine));
-    const unsigned long long saved =
-        min(*(volatile unsigned long long *)ctr, (unsigned long long)refine_cap);
-    for (;;) {
-      unsigned long long k = saved;
-      if (lane == 0 && *(volatile unsigned long long *)(ctr + 1) < saved)
-        k = atomicAdd(ctr + 1, 1ull);
-      k = __shfl_sync(kFull, k, 0);
-      if (k >= saved) break;
-      const unsigned char *e = refine + kRefineHeadBytes + k * refine_entry_bytes<N>();
-      const RefineHead h = *reinterpret_cast<const RefineHead *>(e);
-      const float2 *sF = reinterpret_cast<const float2 *>(e + sizeof(RefineHead));
-      const float2 *sY = sF + NL;
-      __syncwarp();
-      for (int q = lane; q < (int)NL; q += 32) {
-        F[q] = __ldcg(sF + q);
-        Rm[q] = __ldcg(sY + q);
-      }
-      __syncwarp();
-      const CFF prod = {h.xh, h.xl, h.yh, h.yl, h.prod_e};
-      float2 corr;
-      if (mixed_refine_tile<N>(F, Rm, Rm + NL, diag, lane, theta2, tile_la_est(prod, h.exp_sum),
-                               corr))
-        out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
-      else
-        fallback_fp64_src(src, h.b, N, M, LDS, hold, lane, h.b, logabs, phase, parity, status);
-    }
-  }
-  out.flush(lane, logabs, phase, parity, status);
-  // 3. past a full list: chunks of 32 matrices, claimed
-  for (;;) {
-    if (chunks == 0) break;
-    unsigned long long j = chunks;
-    if (lane == 0) j = atomicAdd(&g_work[slot][0], 1ull);
-    j = __shfl_sync(kFull, j, 0);
-    if (j >= chunks) break;
-    const long long b0 = (long long)j * 32;
-    long long bits = 0;
-    if (b0 + lane < batch) bits = __double_as_longlong(logabs[b0 + lane]);
-    const unsigned int routed = __ballot_sync(kFull, bits == kOverRoutedBits);
-    unsigned int mask = __ballot_sync(kFull, bits == kOverFallbackBits) | routed;
-    while (mask) {
-      const int q = __ffs(mask) - 1;
-      mask &= mask - 1u;
-      const long long b = b0 + q;
-      fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                        (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
-    }
-  }
-  // one release per CTA: the last CTA out empties the list and the counter
-  if (lane == 0 && atomicAdd(&cta_done, 1u) == (unsigned int)warps - 1u) {
-    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
-      atomicExch(&g_work[slot][0], 0ull);
-      atomicExch(&g_work[slot][1], 0ull);
-      atomicExch(&g_pend_count[pslot], 0u);
-      atomicExch(&g_pend_over[pslot], 0u);
-    }
-  }
-}
-
-// The FP64 pass: one CTA per SM; its warps refactorise the pending list's
-// matrices (reference pivot rule, fused arithmetic, status flag
-// LUFQHE_ST_FALLBACK, or LUFQHE_ST_FP64 for the routed share). Every
-// factorisation of one n costs the same, so the entries are dealt out at a
-// fixed stride: entry j goes to warp j / G of CTA j % G (G CTAs), so the first
-// G entries land on warp 0 of every SM, the next G on warp 1 (the next SM
-// sub-partition), and no sub-partition's FP64 pipe holds more than
-// ceil(count / (4 G)) of them when the list is short. (First-come claims
-// piled up to five matrices on some sub-partitions while others idled.) If
-// the list overflowed, the matrices past it are found in chunks of 32 whose
-// logabs the FP32 pass marked, claimed from a counter. The last CTA out
-// empties the list for its next user.
-template <class Src>
-__global__ void __launch_bounds__(kFallbackMaxWarps * 32)
-    lup_mixed_fallback_kernel(Src src, int n, long long batch,
-                              int slot, int pslot, double *__restrict__ logabs,
-                              double *__restrict__ phase, int8_t *__restrict__ parity,
-                              int32_t *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int lds = n + 1;
-  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
-  double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
-                                            (size_t)warps * n * lds) +
-                 warp * 2 * n;
-  __shared__ unsigned int cta_done;
-  if (threadIdx.x == 0) cta_done = 0u;
-  __syncthreads();
-  const unsigned long long listed =
-      min(*(volatile unsigned int *)&g_pend_count[pslot], kPendCap);
-  const unsigned long long chunks =
-      *(volatile unsigned int *)&g_pend_over[pslot] ? (unsigned long long)(batch + 31) / 32 : 0ull;
-  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
-  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
-       j += stride) {
-    const unsigned int e = g_pend[pslot][j];
-    const long long b = e & ~kPendRouted;
-    fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
-                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
-  }
-  for (;;) {
-    if (chunks == 0) break;
-    unsigned long long j = chunks;
-    if (lane == 0) j = atomicAdd(&g_work[slot][0], 1ull);
-    j = __shfl_sync(kFull, j, 0);
-    if (j >= chunks) break;
-    const long long b0 = (long long)j * 32;
-    long long bits = 0;
-    if (b0 + lane < batch) bits = __double_as_longlong(logabs[b0 + lane]);
-    const unsigned int routed = __ballot_sync(kFull, bits == kOverRoutedBits);
-    unsigned int mask = __ballot_sync(kFull, bits == kOverFallbackBits) | routed;
-    while (mask) {
-      const int q = __ffs(mask) - 1;
-      mask &= mask - 1u;
-      const long long b = b0 + q;
-      fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
-                        (routed >> q) & 1u ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
-    }
-  }
-  // one release per CTA: the last CTA out empties the list and the counter
-  if (lane == 0 && atomicAdd(&cta_done, 1u) == (unsigned int)warps - 1u) {
-    if (atomicAdd(&g_work[slot][1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
-      atomicExch(&g_work[slot][0], 0ull);
-      atomicExch(&g_work[slot][1], 0ull);
-      atomicExch(&g_pend_count[pslot], 0u);
-      atomicExch(&g_pend_over[pslot], 0u);
-    }
-  }
-}
-
-template <class Src>
-int launch_fallback(Src src, int n, long long batch, int pslot, double *logabs, double *phase,
-                    int8_t *parity, int32_t *status, cudaStream_t stream) {
-  const size_t per_warp = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
-  int warps = (int)(device_smem_optin() / per_warp);
-  if (warps > kFallbackMaxWarps) warps = kFallbackMaxWarps;
-  if (warps < 1) warps = 1;
-  const size_t smem = per_warp * warps;
-  auto kern = lup_mixed_fallback_kernel<Src>;
-  int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem),
-                      "cudaFuncSetAttribute(mixed fallback)");
-  if (rc) return rc;
-  int per_sm = 0;
-  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
-                  "occupancy(mixed fallback)");
-  if (rc) return rc;
-  if (per_sm < 1) {
-    set_error("mixed fallback: n=%d does not fit on an SM", n);
-    return LUFQHE_ERR_UNSUPPORTED_N;
-  }
-  // one CTA per SM (the list's length is known only on the device)
-  long long want = (batch + warps - 1) / warps;
-  long long cap = (long long)device_sm_count();
-  int grid = (int)(want < cap ? want : cap);
-  kern<<<grid, warps * 32, smem, stream>>>(src, n, batch, next_work_slot(), pslot, logabs, phase,
-                                           parity, status);
-  return check_cuda(cudaGetLastError(), "lup_mixed_fallback_kernel launch");
-}
-
-template <int N, class Src>
-int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, double *phase,
-                      int8_t *parity, int32_t *status, cudaStream_t stream, bool inplace) {
-  // only dense batches of the deferring sizes have an in-place variant
-  constexpr bool kHasInplace = N >= kDeferMinN && std::is_same<Src, DenseSource>::value;
-  if (!kHasInplace) inplace = false;
-  const size_t per_warp = tile_smem_per_warp<N>();
-  // small CTAs: the register-heavy residual tile limits residency, and
-  // smaller CTAs let the scheduler fill an SM with several of them
-  int warps = (int)(device_smem_optin() / per_warp);
-  int wcap = tile_max_warps(N);
-  if (g_tile_warps > 0 && g_tile_warps < wcap) wcap = g_tile_warps;
-  if (warps > wcap) warps = wcap;
-  const size_t smem = per_warp * warps;
-  auto kern = lup_mixed_tile_kernel<N, Src, false>;
-  if constexpr (kHasInplace)
-    if (inplace) kern = lup_mixed_tile_kernel<N, Src, true>;
-  int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem),
-                      "cudaFuncSetAttribute(mixed tile)");
-  if (rc) return rc;
-  int per_sm = 0;
-  rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
-                  "occupancy(mixed tile)");
-  if (rc) return rc;
-  if (per_sm < 1) per_sm = 1;
-  long long want = (batch + warps - 1) / warps;
-  long long cap = (long long)device_sm_count() * per_sm;
-  int grid = (int)(want < cap ? want : cap);
-  const int pslot = N >= kDeferMinN && !inplace ? next_pend_slot() : -1;
-  // the saved matrices for the refinement after the FP32 pass (n >= 24)
-  unsigned char *refine = nullptr;
-  long long refine_cap = 0;
-  if (pslot >= 0 && g_mixed_refine) {
-    refine_cap = std::max<long long>(256, (long long)(kRefineShare * (double)batch));
-    refine_cap = std::min<long long>(refine_cap, batch);
-    rc = lib_malloc_async((void **)&refine, kRefineHeadBytes + (size_t)refine_cap * refine_entry_bytes<N>(),
-                          stream);
-    if (!rc)
-      rc = check_cuda(cudaMemsetAsync(refine, 0, kRefineHeadBytes, stream), "memset(refine)");
-    if (rc) return rc;
-  }
-  double2 *spill = nullptr;
-  if (!refine) refine_cap = g_mixed_refine;  // in-place kernels: the refinement on or off
-  if (inplace) {
-    rc = lib_malloc_async((void **)&spill, (size_t)grid * warps * N * N * sizeof(double2), stream);
-    if (rc) return rc;
-  }
-  kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), next_work_slot(),
-                                           pslot, spill, refine, refine_cap, logabs, phase, parity,
-                                           status);
-  rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
-  // the refinements and the FP64 refactorisations, side by side in one kernel
-  if (!rc && pslot >= 0) {
-    if constexpr (N >= kDeferMinN) {
-      auto fk = lup_mixed_finish_kernel<N, Src>;
-      rc = check_cuda(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem),
-                      "cudaFuncSetAttribute(mixed finish)");
-      if (!rc) {
-        fk<<<grid, warps * 32, smem, stream>>>(src, batch, refine, refine_cap, theta2,
-                                               next_work_slot(), pslot, logabs, phase, parity,
-                                               status);
-        rc = check_cuda(cudaGetLastError(), "lup_mixed_finish_kernel launch");
-      }
-    }
-  }
-  if (refine) {
-    const int r2 = lib_free_async(refine, stream);
-    if (!rc) rc = r2;
-  }
-  if (spill) {
-    const int r2 = lib_free_async(spill, stream);
-    if (!rc) rc = r2;
-  }
-  return rc;
-}
-
-}  // namespace
-
 size_t mixed_smem_per_warp(int n) {
   const int lds = n + 1;
   return (size_t)n * lds * (sizeof(float2) + sizeof(float4)) + 2 * (size_t)n * sizeof(double) +
@@ -663,72 +35,20 @@ float g_mixed_theta = 0.1f;
 int g_mixed_refine = 1;
 
 // Device memory a batched mixed call takes from the library's pool while it
-// runs: the states saved for the refinement (n = 24 and 32, device batches).
+// runs, its state block (CallState): the head, for n >= 24 the pending list
+// (one entry per matrix) and, for n = 24 and 32, the saved matrices.
 size_t mixed_workspace_bytes(int n, long long batch) {
-  if (!g_mixed_refine || fp64_share_64k(n) >= 65536u || batch == 0) return 0;
-  long long cap = std::max<long long>(256, (long long)(kRefineShare * (double)batch));
-  cap = std::min<long long>(cap, batch);
-  if (n == 24) return kRefineHeadBytes + (size_t)cap * refine_entry_bytes<24>();
-  if (n == 32) return kRefineHeadBytes + (size_t)cap * refine_entry_bytes<32>();
-  return 0;
-}
-
-namespace {
-
-// plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
-template <class Src, class PlainFn>
-int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *phase,
-                     int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64,
-                     bool inplace = false) {
-  if (batch == 0) return LUFQHE_SUCCESS;
-  // every matrix on the FP64 route: the plain fused kernel, whose shared
-  // memory layout holds more warps per SM than the mixed kernels'
-  if (fp64_share_64k(n) >= 65536u)
-    return plain_fp64();
-  const float th2 = g_mixed_theta * g_mixed_theta;
-  switch (n) {
-    case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    default: break;
+  if (fp64_share_64k(n) >= 65536u || batch == 0) return 0;
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  if (n < kDeferMinN) return kHeadBytes;  // at most the work counter
+  size_t bytes = kHeadBytes + up((size_t)batch * sizeof(unsigned int));
+  if (g_mixed_refine && (n == 24 || n == 32)) {
+    long long cap = std::max<long long>(256, (long long)(kRefineShare * (double)batch));
+    cap = std::min<long long>(cap, batch);
+    bytes += up((size_t)cap * (n == 24 ? refine_entry_bytes<24>() : refine_entry_bytes<32>()));
   }
-  const size_t per_warp = mixed_smem_per_warp(n);
-  const size_t optin = device_smem_optin();
-  int warps = (int)(optin / per_warp);
-  if (warps > 4) warps = 4;
-  if (warps < 1) {
-    set_error("n=%d needs %zu bytes of shared memory per matrix; the device offers %zu", n,
-              per_warp, optin);
-    return LUFQHE_ERR_UNSUPPORTED_N;
-  }
-  const size_t smem = per_warp * warps;
-  auto kern = lup_mixed_kernel<Src>;
-  int rc = check_cuda(cudaFuncSetAttribute(kern,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "cudaFuncSetAttribute(mixed)");
-  if (rc) return rc;
-  int per_sm = 0;
-  rc = check_cuda(
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem),
-      "occupancy(mixed)");
-  if (rc) return rc;
-  if (per_sm < 1) per_sm = 1;
-  long long want = (batch + warps - 1) / warps;
-  long long cap = (long long)device_sm_count() * per_sm;
-  int grid = (int)(want < cap ? want : cap);
-  const float theta2 = g_mixed_theta * g_mixed_theta;
-  const int pslot = n >= kDeferMinN ? next_pend_slot() : -1;
-  kern<<<grid, warps * 32, smem, stream>>>(src, n, batch, theta2, fp64_share_64k(n),
-                                           next_work_slot(), pslot, logabs, phase, parity, status);
-  rc = check_cuda(cudaGetLastError(), "lup_mixed_kernel launch");
-  if (rc || pslot < 0) return rc;
-  return launch_fallback(src, n, batch, pslot, logabs, phase, parity, status, stream);
+  return bytes;
 }
-
-}  // namespace
 
 int launch_mixed(const double2 *A, int n, int lda, long long batch, double *logabs,
                  double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,

@@ -20,9 +20,11 @@ namespace {
 
 constexpr int kMaxWarpsPlain = 8;
 
-template <int ARITH, class Src>
+// Out: element type of the in-place factors (double2, or float2 for the
+// reference's complex64 buffers)
+template <int ARITH, class Src, class Out = double2>
 __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
-    lup_plain_kernel(Src src, double2 *__restrict__ Aout, int n, int lda,
+    lup_plain_kernel(Src src, Out *__restrict__ Aout, int n, int lda,
                      long long batch, double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status,
                      int status_or) {
@@ -57,10 +59,10 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
     }
 
     if (Aout && (st == 0 || st == LUFQHE_ST_SINGULAR)) {
-      double2 *dst = Aout + (size_t)b * n * lda;
+      Out *dst = Aout + (size_t)b * n * lda;
       BlockWalk w(lane, n);
       for (int e = lane; e < nn; e += 32) {
-        dst[(size_t)w.i * lda + w.k] = M[w.i * lds + w.k];
+        store_entry(dst + (size_t)w.i * lda + w.k, M[w.i * lds + w.k]);
         w.next(n);
       }
     }
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
 // Writes exp(logabs + i*phase) into element (0,0); with pair_product the even
 // matrix of each pair gets the product of the pair's determinants
 // (LU-fqhe/src/LUCoreGPU.cu:403-435).
-__global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
+template <class T>
+__global__ void write_det_kernel(T *A, int n, int lda, long long batch,
                                  const double *logabs, const double *phase,
                                  const int32_t *status, int pair_product) {
   long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -95,7 +98,7 @@ __global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
     sincos(ph, &s, &c);
     v = make_double2(m * c, m * s);
   }
-  A[(size_t)b * n * lda] = v;
+  store_entry(A + (size_t)b * n * lda, v);
 }
 
 }  // namespace
@@ -106,9 +109,9 @@ __global__ void write_det_kernel(double2 *A, int n, int lda, long long batch,
 constexpr int kGroupWarps = kFp64GroupWarps;
 constexpr int kGroupMinN = kFp64GroupMinN;
 
-template <int ARITH, class Src>
+template <int ARITH, class Src, class Out = double2>
 __global__ void __launch_bounds__(kGroupWarps * 32)
-    lup_plain_group_kernel(Src src, double2 *__restrict__ Aout, int n, int lda, long long batch,
+    lup_plain_group_kernel(Src src, Out *__restrict__ Aout, int n, int lda, long long batch,
                            double *__restrict__ logabs, double *__restrict__ phase,
                            int8_t *__restrict__ parity, int32_t *__restrict__ status,
                            int status_or) {
@@ -125,10 +128,10 @@ __global__ void __launch_bounds__(kGroupWarps * 32)
     if (!st) st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par);
     __syncthreads();
     if (Aout && (st == 0 || st == LUFQHE_ST_SINGULAR)) {
-      double2 *dst = Aout + (size_t)b * n * lda;
+      Out *dst = Aout + (size_t)b * n * lda;
       StrideWalk w(tid, nthr, n);
       for (int e = tid; e < n * n; e += nthr) {
-        dst[(size_t)w.i * lda + w.k] = M[w.i * lds + w.k];
+        store_entry(dst + (size_t)w.i * lda + w.k, M[w.i * lds + w.k]);
         w.next(n);
       }
     }
@@ -159,15 +162,15 @@ size_t plain_smem_per_warp(int n) {
   return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
 }
 
-template <class Src>
-int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, int arith,
+template <class Src, class Out = double2>
+int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int arith,
                      double *logabs, double *phase, int8_t *parity, int32_t *status,
                      cudaStream_t stream, int status_or) {
   if (batch == 0) return LUFQHE_SUCCESS;
   if (n >= kGroupMinN) {
     const size_t smem = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
-    auto kern = arith == ARITH_REF ? lup_plain_group_kernel<ARITH_REF, Src>
-                                   : lup_plain_group_kernel<ARITH_FUSED, Src>;
+    auto kern = arith == ARITH_REF ? lup_plain_group_kernel<ARITH_REF, Src, Out>
+                                   : lup_plain_group_kernel<ARITH_FUSED, Src, Out>;
     int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),
                         "cudaFuncSetAttribute(plain group)");
@@ -183,8 +186,11 @@ int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, in
     }
     const long long cap = (long long)device_sm_count() * per_sm;
     const int grid = (int)(batch < cap ? batch : cap);
+    KernelTimer timer(arith == ARITH_REF ? "lup_plain_group_kernel_ref" : "lup_plain_group_kernel",
+                      n, stream);
     kern<<<grid, kGroupWarps * 32, smem, stream>>>(src, Aout, n, lda, batch, logabs, phase, parity,
                                                    status, status_or);
+    timer.stop();
     return check_cuda(cudaGetLastError(), "lup_plain_group_kernel launch");
   }
   const size_t per_warp = plain_smem_per_warp(n);
@@ -197,8 +203,8 @@ int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, in
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
   const size_t smem = per_warp * warps;
-  auto kern =
-      arith == ARITH_REF ? lup_plain_kernel<ARITH_REF, Src> : lup_plain_kernel<ARITH_FUSED, Src>;
+  auto kern = arith == ARITH_REF ? lup_plain_kernel<ARITH_REF, Src, Out>
+                                 : lup_plain_kernel<ARITH_FUSED, Src, Out>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
                       "cudaFuncSetAttribute(plain)");
@@ -211,8 +217,10 @@ int launch_plain_src(Src src, double2 *Aout, int n, int lda, long long batch, in
   long long want = (batch + warps - 1) / warps;
   long long cap = (long long)device_sm_count() * per_sm;
   int grid = (int)(want < cap ? want : cap);
+  KernelTimer timer(arith == ARITH_REF ? "lup_plain_kernel_ref" : "lup_plain_kernel", n, stream);
   kern<<<grid, warps * 32, smem, stream>>>(src, Aout, n, lda, batch, logabs, phase, parity, status,
                                            status_or);
+  timer.stop();
   return check_cuda(cudaGetLastError(), "lup_plain_kernel launch");
 }
 
@@ -223,22 +231,42 @@ int launch_plain(const double2 *A, double2 *Aout, int n, int lda, long long batc
                           status, stream, status_or);
 }
 
+int launch_plain32(const float2 *A, float2 *Aout, int n, int lda, long long batch, int arith,
+                   double *logabs, double *phase, int8_t *parity, int32_t *status,
+                   cudaStream_t stream, int status_or) {
+  return launch_plain_src(Dense32Source{A, lda}, Aout, n, lda, batch, arith, logabs, phase,
+                          parity, status, stream, status_or);
+}
+
 int launch_plain_lll(const double2 *Z, int n, long long batch, int arith, double *logabs,
                      double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
                      int status_or) {
-  return launch_plain_src(LllSource{Z}, nullptr, n, n, batch, arith, logabs, phase, parity, status,
-                          stream, status_or);
+  return launch_plain_src(LllSource{Z}, static_cast<double2 *>(nullptr), n, n, batch, arith,
+                          logabs, phase, parity, status, stream, status_or);
+}
+
+template <class T>
+int launch_write_det_t(T *A, int n, int lda, long long batch, const double *logabs,
+                       const double *phase, const int32_t *status, int pair_product,
+                       cudaStream_t stream) {
+  if (batch == 0) return LUFQHE_SUCCESS;
+  int threads = 256;
+  long long blocks = (batch + threads - 1) / threads;
+  write_det_kernel<T><<<(unsigned)blocks, threads, 0, stream>>>(A, n, lda, batch, logabs, phase,
+                                                                status, pair_product);
+  return check_cuda(cudaGetLastError(), "write_det_kernel launch");
 }
 
 int launch_write_det(double2 *A, int n, int lda, long long batch, const double *logabs,
                      const double *phase, const int32_t *status, int pair_product,
                      cudaStream_t stream) {
-  if (batch == 0) return LUFQHE_SUCCESS;
-  int threads = 256;
-  long long blocks = (batch + threads - 1) / threads;
-  write_det_kernel<<<(unsigned)blocks, threads, 0, stream>>>(A, n, lda, batch, logabs, phase,
-                                                             status, pair_product);
-  return check_cuda(cudaGetLastError(), "write_det_kernel launch");
+  return launch_write_det_t(A, n, lda, batch, logabs, phase, status, pair_product, stream);
+}
+
+int launch_write_det32(float2 *A, int n, int lda, long long batch, const double *logabs,
+                       const double *phase, const int32_t *status, int pair_product,
+                       cudaStream_t stream) {
+  return launch_write_det_t(A, n, lda, batch, logabs, phase, status, pair_product, stream);
 }
 
 }  // namespace lufqhe

@@ -18,7 +18,8 @@
 //
 // Its device address is looked up once per device, with that device current,
 // on the first call made on that device; make that first call before any
-// stream capture begins.
+// stream capture begins. The address is kept for the life of the process, so
+// the library must not be used across a cudaDeviceReset.
 
 #include <mutex>
 

@@ -29,6 +29,9 @@ ST_FP64 = 16
 
 MAX_N = 64
 
+DTYPE_C128 = 0
+DTYPE_C64 = 1
+
 
 def lib():
     return _native.load()
@@ -59,19 +62,30 @@ def _shape(A, lda):
     return batch, n, lda
 
 
+def _dtype_code(A):
+    import torch
+    if A.dtype == torch.complex128:
+        return DTYPE_C128
+    if A.dtype == torch.complex64:
+        return DTYPE_C64
+    raise TypeError("A must be complex128 or complex64")
+
+
 def batch_lup_det(A, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | None = None):
-    """Determinants of a (batch, n, lda) complex128 CUDA tensor (first n columns used)."""
+    """Determinants of a (batch, n, lda) complex128 or complex64 CUDA tensor
+    (first n columns used); complex64 entries are widened exactly."""
     import torch
     batch, n, lda = _shape(A, None)
-    if A.dtype != torch.complex128 or not A.is_cuda:
-        raise TypeError("A must be a complex128 CUDA tensor")
+    dtype = _dtype_code(A)
+    if not A.is_cuda:
+        raise TypeError("A must be a CUDA tensor")
     if out is None:
         dev = A.device
         out = DetResult(torch.empty(batch, dtype=torch.float64, device=dev),
                         torch.empty(batch, dtype=torch.float64, device=dev),
                         torch.empty(batch, dtype=torch.int8, device=dev),
                         torch.empty(batch, dtype=torch.int32, device=dev))
-    rc = lib().lufqhe_batch_lup_det(A.data_ptr(), n, lda, batch, 0, mode, out.logabs.data_ptr(),
+    rc = lib().lufqhe_batch_lup_det(A.data_ptr(), n, lda, batch, dtype, mode, out.logabs.data_ptr(),
                                     out.phase.data_ptr(), out.parity.data_ptr(),
                                     out.status.data_ptr(), _stream_ptr(stream))
     _native.check(rc, "lufqhe_batch_lup_det")
@@ -107,15 +121,16 @@ def batch_lup_det_host(A, mode: int = MODE_PLAIN_FP64, stream=None,
     asynchronous on `stream`; synchronise it before reading `out`."""
     import torch
     batch, n, lda = _shape(A, None)
-    if A.dtype != torch.complex128 or A.is_cuda or not A.is_contiguous():
-        raise TypeError("A must be a contiguous complex128 host tensor")
+    dtype = _dtype_code(A)
+    if A.is_cuda or not A.is_contiguous():
+        raise TypeError("A must be a contiguous complex128 / complex64 host tensor")
     if out is None:
         pin = A.is_pinned()
         out = DetResult(torch.empty(batch, dtype=torch.float64, pin_memory=pin),
                         torch.empty(batch, dtype=torch.float64, pin_memory=pin),
                         torch.empty(batch, dtype=torch.int8, pin_memory=pin),
                         torch.empty(batch, dtype=torch.int32, pin_memory=pin))
-    rc = lib().lufqhe_batch_lup_det_host(A.data_ptr(), n, lda, batch, 0, mode,
+    rc = lib().lufqhe_batch_lup_det_host(A.data_ptr(), n, lda, batch, dtype, mode,
                                          out.logabs.data_ptr(), out.phase.data_ptr(),
                                          out.parity.data_ptr(), out.status.data_ptr(),
                                          _stream_ptr(stream))
@@ -141,10 +156,13 @@ def factor_inplace(A, mode: int = MODE_PLAIN_FP64, stream=None) -> DetResult:
 
 
 def lucoregpu_call(A, pair_product: bool = False, stream=None) -> None:
-    """Reference-shaped call: determinant written into element (0,0) of each matrix."""
+    """Reference-shaped call: determinant written into element (0,0) of each
+    matrix; complex64 tensors (the reference's float2 buffers) take the
+    complex64 form of the call."""
     batch, n, lda = _shape(A, None)
-    rc = lib().lufqhe_lucoregpu_call(A.data_ptr(), batch, n, lda, int(pair_product),
-                                     _stream_ptr(stream))
+    fn = lib().lufqhe_lucoregpu_call_c64 if _dtype_code(A) == DTYPE_C64 else \
+        lib().lufqhe_lucoregpu_call
+    rc = fn(A.data_ptr(), batch, n, lda, int(pair_product), _stream_ptr(stream))
     _native.check(rc, "lufqhe_lucoregpu_call")
 
 
@@ -234,6 +252,10 @@ class Plan:
         buf = ctypes.create_string_buffer(8192)
         _native.check(lib().lufqhe_plan_describe(self._h, buf, len(buf)), "lufqhe_plan_describe")
         return json.loads(buf.value.decode())
+
+    def kernels(self) -> int:
+        """Kernels one execution of the plan launches."""
+        return int(self.describe().get("kernels", 0))
 
     def close(self):
         if self._h:

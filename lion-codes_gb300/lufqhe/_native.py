@@ -27,6 +27,7 @@ SIGNATURES = {
     "lufqhe_batch_lup_factor_inplace": (I32, [P, I32, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_lucoregpu_call": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),
+    "lufqhe_lucoregpu_call_c64": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_pair_sum": (I32, [P, P, I64, P, P]),
     "lufqhe_plan_create": (I32, [P, P, I32, I32, P, P, P, P, I32, P]),
     "lufqhe_plan_execute": (I32, [P, P]),
@@ -48,6 +49,7 @@ SIGNATURES = {
     "lufqhe_set_option": (I32, [I32, F64]),
     "lufqhe_get_option": (F64, [I32]),
     "lufqhe_probe_fma_peak": (I32, [I32, P, P]),
+    "lufqhe_kernel_times": (I32, [P, _c.c_size_t]),
     "lufqhe_workspace_bytes": (_c.c_size_t, [I32, I64, I32]),
     "lufqhe_release_workspace": (I32, []),
     "lufqhe_last_error": (_c.c_char_p, []),

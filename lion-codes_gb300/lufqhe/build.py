@@ -21,10 +21,12 @@ LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "liblufqhe.so"
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is compiled without floating-point contraction, so the host
+# generators give the same bits on x86-64 and aarch64 (where FMA is baseline)
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
-SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu"]
+SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "lup_mixed_c64.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu"]
 
 
 def _nvcc() -> str:

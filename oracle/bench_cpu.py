@@ -45,9 +45,10 @@ def cpu_baseline(np, A_host, n: int, seconds: float = 10.0, max_mats: int = 3276
                       f"restatement of LUCoreCPU::determinant, OpenMP {nt} threads"}
 
 
-def reference_arm(np, args, kind: str, n: int, batch: int, seed: int, make_inputs) -> dict:
+def reference_arm(np, args, kind: str, n: int, batch: int, seed: int, make_inputs,
+                  config: dict) -> dict:
     """The `--impl reference` JSON line: K timed steps, each one pass over a
-    bounded sample of the workload."""
+    bounded sample of the workload. `config` is the GPU arm's config object."""
     sample = min(batch, args.ref_sample)
     A = make_inputs(kind, n, sample, seed)
     nt = _threads()
@@ -67,8 +68,8 @@ def reference_arm(np, args, kind: str, n: int, batch: int, seed: int, make_input
         "value": rate, "unit": "dets/s", "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": f"{args.workload}: {batch} x n={n}", "batch": batch, "n": n,
-                   "sample_per_step": sample},
+        "config": config,
+        "sample_per_step": sample,
         "cpu_baseline": {"value": rate, "unit": "dets/s", "cores": nt, "kind": "port",
                          "sample": desc},
         "e2e": {"value": rate, "unit": "dets/s", "h2d_bytes_per_step": 0,

@@ -39,6 +39,11 @@ def lib():
         _lib.lufqhe_oracle_lup_det_fp64.argtypes = [_P, _I, _I, _L, _I, _P, _P, _P, _P, _P, _P, _I]
         _lib.lufqhe_oracle_logdet_dd.argtypes = [_P, _I, _I, _L, _P, _P, _P, _I]
         _lib.lufqhe_oracle_pair_sum.argtypes = [_P, _I, _I, _L, _P, _P, _I]
+        _lib.lufqhe_oracle_lup_det_f32.argtypes = [_P, _I, _I, _L, _P, _P, _P, _P, _I]
+        _lib.lufqhe_oracle_gen_gaussian.argtypes = [_P, _I, _I, _L, ctypes.c_ulonglong,
+                                                    ctypes.c_double]
+        _lib.lufqhe_oracle_gen_lll.argtypes = [_P, _P, _I, _I, _L, ctypes.c_ulonglong,
+                                               ctypes.c_double]
     return _lib
 
 
@@ -51,6 +56,7 @@ def ref_lib():
     if _ref is None:
         _ref = ctypes.CDLL(str(REF_SO))
         _ref.ref_lucorecpu_det_batch.argtypes = [_P, _I, _I, _L, _P, _I]
+        _ref.ref_lucorecpu_factor_batch.argtypes = [_P, _I, _I, _L, _P, _P, _I]
     return _ref
 
 
@@ -118,3 +124,62 @@ def ref_det_f32(A32, nthreads: int = 0):
     if rc != 0:
         raise ValueError("reference harness rejected the arguments")
     return det
+
+
+def lup_det_f32(A32, nthreads: int = 0):
+    """Float32 restatement of LUCoreCPU::determinant: complex64 det (direct
+    product, as the reference returns it), factors (batch, n, n) complex64 in
+    pivoted row order, piv (batch, n) and status."""
+    A32 = np.ascontiguousarray(A32, dtype=np.complex64)
+    batch, n, cols = A32.shape
+    det = np.empty(batch, np.complex64)
+    fac = np.empty((batch, n, n), np.complex64)
+    piv = np.empty((batch, n), np.int32)
+    st = np.empty(batch, np.int32)
+    rc = lib().lufqhe_oracle_lup_det_f32(A32.ctypes.data, n, cols, batch, det.ctypes.data,
+                                         fac.ctypes.data, piv.ctypes.data, st.ctypes.data,
+                                         nthreads)
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    return {"det": det, "factors": fac, "piv": piv, "status": st}
+
+
+def ref_factor_f32(A32, nthreads: int = 0):
+    """The reference's own float32 determinant and the factors it leaves in place."""
+    A32 = np.ascontiguousarray(A32, dtype=np.complex64)
+    batch, n, cols = A32.shape
+    det = np.empty(batch, np.complex64)
+    fac = np.empty((batch, n, n), np.complex64)
+    rc = ref_lib().ref_lucorecpu_factor_batch(A32.ctypes.data, n, cols, batch, det.ctypes.data,
+                                              fac.ctypes.data, nthreads)
+    if rc != 0:
+        raise ValueError("reference harness rejected the arguments")
+    return det, fac
+
+
+def factor_digests(fac):
+    """One 64-bit digest per matrix of its factor bytes (blake2b), for compact
+    bit-for-bit comparison against committed golden values."""
+    import hashlib
+    fac = np.ascontiguousarray(fac)
+    return np.array([int.from_bytes(hashlib.blake2b(m.tobytes(), digest_size=8).digest(), "little")
+                     for m in fac], dtype=np.uint64)
+
+
+def gen_gaussian(batch: int, n: int, seed: int, sigma: float = 1.0):
+    """The library's seeded complex Gaussian matrices, generated here on the host."""
+    A = np.empty((batch, n, n), np.complex128)
+    if lib().lufqhe_oracle_gen_gaussian(A.ctypes.data, n, n, batch, seed, sigma) != 0:
+        raise ValueError("oracle rejected the arguments")
+    return A
+
+
+def gen_lll(batch: int, n: int, seed: int, sigma: float | None = None):
+    """The library's seeded lowest-Landau-level orbital matrices; returns (A, z)."""
+    import math
+    sigma = math.sqrt(n) if sigma is None else sigma
+    A = np.empty((batch, n, n), np.complex128)
+    z = np.empty((batch, n), np.complex128)
+    if lib().lufqhe_oracle_gen_lll(A.ctypes.data, z.ctypes.data, n, n, batch, seed, sigma) != 0:
+        raise ValueError("oracle rejected the arguments")
+    return A, z

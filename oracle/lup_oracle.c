@@ -229,6 +229,218 @@ int lufqhe_oracle_lup_det_fp64(const double *A, int n, int lda, long long batch,
 }
 
 /* ------------------------------------------------------------------------- */
+/* Float32 restatement: the same steps in the reference's own precision, to   */
+/* pin the restatement bit for bit against the reference's compiled code.     */
+/* Every operation follows LUCoreCPU::determinant (LU-fqhe/src/LUCoreCPU.cu:   */
+/* 112-267) in float, in the same order, with nothing fused (this file is     */
+/* built with -ffp-contract=off):                                              */
+/*   scale  big = max_j fabs(Re a_ij), compared in double with 1e-24 (:145-160) */
+/*   Crout  tmp = (l.x u.x - l.y u.y, l.y u.x + l.x u.y); sum -= tmp (:164-205) */
+/*   pivot  dum = fabs(sum.x) / holder[i] in float, `dum >= big`    (:207-212) */
+/*   swap   rows j <-> imax, d = -d, holder[imax] = holder[j]        (:215-232) */
+/*   divide den = p.x p.x + p.y p.y; ((a.x p.x + a.y p.y)/den,                 */
+/*          (a.y p.x - a.x p.y)/den)                                 (:234-251) */
+/*   det    det = det * u_jj left to right from (1, 0), then d * det (:256-265) */
+/* The factors are left in place (pivoted row order) as the reference leaves  */
+/* them. A row scale below 1e-24 (where the reference calls exit(0)) gives     */
+/* status LUFQHE_ST_SCALE_TINY and det = NaN; an exact zero pivot (where the   */
+/* reference divides by zero) is carried through the same IEEE divisions.      */
+/* ------------------------------------------------------------------------- */
+typedef struct { float x, y; } cplxf;
+
+static int factor_one_f32(cplxf *a, int n, float *holder, int *piv, cplxf *det_out) {
+  float d = 1.0f;
+  int imax = 0;
+  for (int i = 0; i < n; ++i) {
+    float big = 0.0f;
+    for (int j = 0; j < n; ++j) {
+      float t = fabsf(a[i * n + j].x);
+      if (t > big) big = t;
+    }
+    if ((double)big < 1e-24) {
+      det_out->x = NAN;
+      det_out->y = NAN;
+      return LUFQHE_ST_SCALE_TINY;
+    }
+    holder[i] = big;
+  }
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < j; ++i) {
+      cplxf s = a[i * n + j];
+      for (int k = 0; k < i; ++k) {
+        cplxf l = a[i * n + k], u = a[k * n + j];
+        float tx = l.x * u.x - l.y * u.y;
+        float ty = l.y * u.x + l.x * u.y;
+        s.x = s.x - tx;
+        s.y = s.y - ty;
+      }
+      a[i * n + j] = s;
+    }
+    float big = 0.0f;
+    for (int i = j; i < n; ++i) {
+      cplxf s = a[i * n + j];
+      for (int k = 0; k < j; ++k) {
+        cplxf l = a[i * n + k], u = a[k * n + j];
+        float tx = l.x * u.x - l.y * u.y;
+        float ty = l.y * u.x + l.x * u.y;
+        s.x = s.x - tx;
+        s.y = s.y - ty;
+      }
+      a[i * n + j] = s;
+      float dum = fabsf(s.x) / holder[i];
+      if (dum >= big) {
+        big = dum;
+        imax = i;
+      }
+    }
+    if (piv) piv[j] = imax;
+    if (j != imax) {
+      for (int k = 0; k < n; ++k) {
+        cplxf t = a[imax * n + k];
+        a[imax * n + k] = a[j * n + k];
+        a[j * n + k] = t;
+      }
+      d = -d;
+      holder[imax] = holder[j];
+    }
+    if (j != n - 1) {
+      cplxf p = a[j * n + j];
+      for (int i = j + 1; i < n; ++i) {
+        float den = p.x * p.x + p.y * p.y;
+        cplxf v = a[i * n + j], t;
+        t.x = (v.x * p.x + v.y * p.y) / den;
+        t.y = (v.y * p.x - v.x * p.y) / den;
+        a[i * n + j] = t;
+      }
+    }
+  }
+  cplxf det = {1.0f, 0.0f};
+  for (int i = 0; i < n; ++i) {
+    cplxf u = a[i * n + i], t;
+    t.x = det.x * u.x - det.y * u.y;
+    t.y = det.y * u.x + det.x * u.y;
+    det = t;
+  }
+  det_out->x = d * det.x;
+  det_out->y = d * det.y;
+  return 0;
+}
+
+/*
+ * Batched float32 restatement. A: `batch` complex64 matrices (interleaved
+ * floats), row stride lda, matrix stride n*lda. det: one complex64 per matrix
+ * (the reference's direct product). Optional: factors (batch*n*n complex64,
+ * row stride n, the in-place result), piv (batch*n), status (batch).
+ */
+int lufqhe_oracle_lup_det_f32(const float *A, int n, int lda, long long batch, float *det,
+                              float *factors, int *piv, int *status, int nthreads) {
+  if (n < 1 || lda < n || batch < 0 || !A || !det) return -1;
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    cplxf *work = (cplxf *)malloc(sizeof(cplxf) * (size_t)n * n);
+    float *holder = (float *)malloc(sizeof(float) * (size_t)n);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long long b = 0; b < batch; ++b) {
+      const float *src = A + (size_t)b * n * lda * 2;
+      for (int i = 0; i < n; ++i)
+        memcpy(work + (size_t)i * n, src + (size_t)i * lda * 2, sizeof(cplxf) * n);
+      cplxf dt;
+      int st = factor_one_f32(work, n, holder, piv ? piv + (size_t)b * n : NULL, &dt);
+      det[2 * b] = dt.x;
+      det[2 * b + 1] = dt.y;
+      if (status) status[b] = st;
+      if (factors) memcpy(factors + (size_t)b * n * n * 2, work, sizeof(cplxf) * (size_t)n * n);
+    }
+    free(work);
+    free(holder);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Seeded synthetic inputs: the same draws as the library's host generators   */
+/* (counter-based SplitMix64 uniforms, Box-Muller Gaussians, lowest-Landau-   */
+/* level rows by repeated multiplication), so that the CPU reference arm of   */
+/* the benchmark builds its workload without loading the product library.     */
+/* Bit-identical to lufqhe_gen_gaussian_host / lufqhe_gen_lll_host (a CPU     */
+/* test checks it); both are compiled without floating-point contraction.     */
+/* ------------------------------------------------------------------------- */
+static uint64_t gen_mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+static double gen_uniform01(uint64_t key, uint64_t ctr) {
+  uint64_t r = gen_mix64(key + ctr * 0xD2B74407B1CE6E93ull);
+  return ((double)(r >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+static uint64_t gen_seed_key(uint64_t seed) { return gen_mix64(seed ^ 0x5851F42D4C957F2Dull); }
+static void gen_gauss2(uint64_t key, uint64_t ctr, double *g0, double *g1) {
+  double u1 = gen_uniform01(key, 2 * ctr);
+  double u2 = gen_uniform01(key, 2 * ctr + 1);
+  double r = sqrt(-2.0 * log(u1));
+  double s = sin(2.0 * kPi * u2);
+  double c = cos(2.0 * kPi * u2);
+  *g0 = r * c;
+  *g1 = r * s;
+}
+
+/* i.i.d. complex Gaussian entries, Re and Im ~ N(0, sigma^2/2). */
+int lufqhe_oracle_gen_gaussian(double *A, int n, int lda, long long batch,
+                               unsigned long long seed, double sigma) {
+  if (!A || n < 1 || lda < n || batch < 0) return -1;
+  uint64_t key = gen_seed_key(seed);
+  double scale = sigma * sqrt(0.5);
+  for (long long b = 0; b < batch; ++b)
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < n; ++k) {
+        double g0, g1;
+        gen_gauss2(key, (uint64_t)b * n * n + (uint64_t)i * n + k, &g0, &g1);
+        double *e = A + 2 * ((size_t)b * n * lda + (size_t)i * lda + k);
+        e[0] = g0 * scale;
+        e[1] = g1 * scale;
+      }
+  return 0;
+}
+
+/* M_ik = z_i^k exp(-|z_i|^2/4), z_i complex Gaussian with E|z|^2 = sigma^2
+ * (z may be NULL). */
+int lufqhe_oracle_gen_lll(double *A, double *z, int n, int lda, long long batch,
+                          unsigned long long seed, double sigma) {
+  if (!A || n < 1 || lda < n || batch < 0) return -1;
+  uint64_t key = gen_seed_key(seed);
+  double scale = sigma * sqrt(0.5);
+  for (long long b = 0; b < batch; ++b)
+    for (int i = 0; i < n; ++i) {
+      double g0, g1;
+      gen_gauss2(key, (uint64_t)b * n + i, &g0, &g1);
+      double zx = g0 * scale, zy = g1 * scale;
+      if (z) {
+        z[2 * ((size_t)b * n + i)] = zx;
+        z[2 * ((size_t)b * n + i) + 1] = zy;
+      }
+      double w = exp(-(zx * zx + zy * zy) * 0.25);
+      double px = 1.0, py = 0.0;
+      double *row = A + 2 * ((size_t)b * n * lda + (size_t)i * lda);
+      for (int k = 0; k < n; ++k) {
+        row[2 * k] = px * w;
+        row[2 * k + 1] = py * w;
+        double nx = px * zx - py * zy;
+        double ny = px * zy + py * zx;
+        px = nx;
+        py = ny;
+      }
+    }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Double-double "truth" oracle. FP64 LU with the reference's |Re| pivot rule  */
 /* loses up to ~1e-10 relative in log|det| on ill-conditioned lowest-Landau-   */
 /* level matrices, so the error of the mixed-precision path is measured       */

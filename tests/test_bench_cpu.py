@@ -43,3 +43,25 @@ def test_reference_arm_json_line():
         assert k in line, k
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["cores"] >= 1
+
+
+def test_reference_arm_loads_no_product_code():
+    """The reference arm builds its inputs with the oracle's generators: the
+    product library must not be mapped into that process, and its config object
+    is the GPU arm's (bench.workload_config)."""
+    code = (
+        "import sys, json, io, contextlib; sys.argv = ['bench.py', '--impl', 'reference', "
+        "'--steps', '1', '--warmup', '3', '--ref-sample', '512']\n"
+        "import bench\n"
+        "buf = io.StringIO()\n"
+        "with contextlib.redirect_stdout(buf):\n"
+        "    bench.main()\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'line': json.loads(buf.getvalue().strip().splitlines()[-1]), "
+        "'loaded': 'liblufqhe.so' in maps}))\n")
+    proc = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                          timeout=600)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    res = json.loads(proc.stdout.strip().splitlines()[-1])
+    assert res["loaded"] is False
+    assert res["line"]["config"] == bench.workload_config("lll24", 1)

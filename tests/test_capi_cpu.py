@@ -49,7 +49,8 @@ FAKE_ODD = ctypes.c_void_p(0x1008)
     ((FAKE, 8, 8, -1, 0, 0, FAKE, None, None, None, None), -1),    # batch < 0
     ((FAKE, 65, 65, 4, 0, 0, FAKE, None, None, None, None), -2),   # n too large
     ((FAKE_ODD, 8, 8, 4, 0, 0, FAKE, None, None, None, None), -1),  # misaligned
-    ((FAKE, 8, 8, 4, 1, 0, FAKE, None, None, None, None), -4),     # complex64 not offered
+    ((FAKE, 8, 8, 4, 7, 0, FAKE, None, None, None, None), -4),     # unknown dtype
+    ((ctypes.c_void_p(0x1004), 8, 8, 4, 1, 0, FAKE, None, None, None, None), -1),  # c64 misaligned
     ((FAKE, 8, 8, 4, 0, 9, FAKE, None, None, None, None), -4),     # unknown mode
 ])
 def test_argument_validation(lufqhe_mod, args, code):
@@ -66,7 +67,7 @@ def test_argument_validation(lufqhe_mod, args, code):
     ((FAKE, 8, 7, 4, 0, 0, FAKE, None, None, None, None), -1),     # lda < n
     ((FAKE, 8, 8, -1, 0, 0, FAKE, None, None, None, None), -1),    # batch < 0
     ((FAKE, 65, 65, 4, 0, 0, FAKE, None, None, None, None), -2),   # n too large
-    ((FAKE, 8, 8, 4, 1, 0, FAKE, None, None, None, None), -4),     # complex64 not offered
+    ((FAKE, 8, 8, 4, 7, 0, FAKE, None, None, None, None), -4),     # unknown dtype
     ((FAKE, 8, 8, 4, 0, 9, FAKE, None, None, None, None), -4),     # unknown mode
 ])
 def test_host_entry_argument_validation(lufqhe_mod, args, code):
@@ -132,15 +133,18 @@ def test_read_reference_file_format(lufqhe_mod, tmp_path):
 
 
 def test_workspace_bytes(lufqhe_mod):
-    """Mixed mode at n = 24 and 32 takes room for a quarter of the batch of
-    saved matrices (header 40 B + L\\U and Y at row stride n + 1, 16-byte
-    aligned) plus 256 B of counters; other sizes and modes take nothing."""
+    """A mixed call's state block from the library's pool: a 256-byte head (its
+    work counter), for n >= 24 a pending list of one 4-byte entry per matrix,
+    and at n = 24 and 32 room for a quarter of the batch of saved matrices
+    (header 40 B + L\\U and Y at row stride n + 1, 16-byte aligned), each part
+    rounded up to 256 bytes. The plain modes take nothing."""
     lib = lufqhe_mod.lib()
+    up = lambda v: (v + 255) // 256 * 256  # noqa: E731
     entry24 = (40 + 2 * 24 * 25 * 8 + 15) // 16 * 16
-    assert lib.lufqhe_workspace_bytes(24, 32768, 2) == 256 + 8192 * entry24
+    assert lib.lufqhe_workspace_bytes(24, 32768, 2) == 256 + up(4 * 32768) + up(8192 * entry24)
     entry32 = (40 + 2 * 32 * 33 * 8 + 15) // 16 * 16
-    assert lib.lufqhe_workspace_bytes(32, 1000, 2) == 256 + 256 * entry32
-    assert lib.lufqhe_workspace_bytes(16, 32768, 2) == 0
+    assert lib.lufqhe_workspace_bytes(32, 1000, 2) == 256 + up(4 * 1000) + up(256 * entry32)
+    assert lib.lufqhe_workspace_bytes(16, 32768, 2) == 256
     assert lib.lufqhe_workspace_bytes(24, 32768, 1) == 0
     assert lib.lufqhe_workspace_bytes(24, 0, 2) == 0
 
@@ -149,3 +153,31 @@ def test_release_workspace_without_pool(lufqhe_mod):
     """Before any call has made the library's memory pool there is nothing to
     trim: the call succeeds without touching a device."""
     assert lufqhe_mod.lib().lufqhe_release_workspace() == 0
+
+
+def test_oracle_generators_match_library(lufqhe_mod, oracle):
+    """The oracle's seeded generators (used by the CPU reference arm, which must
+    not load the product library) draw the library's host matrices bit for bit."""
+    for n, seed in ((8, 0), (16, 1)):
+        assert np.array_equal(oracle.gen_gaussian(64, n, seed=seed),
+                              lufqhe_mod.gen_gaussian_host(64, n, seed=seed))
+    for n, seed in ((6, 3), (24, 2), (48, 4)):
+        A, z = oracle.gen_lll(64, n, seed=seed)
+        B, zb = lufqhe_mod.gen_lll_host(64, n, seed=seed)
+        assert np.array_equal(z, zb) and np.array_equal(A, B)
+
+
+@pytest.mark.parametrize("fn", ["lufqhe_lucoregpu_call", "lufqhe_lucoregpu_call_c64",
+                                "lufqhe_lucoregpu_call_noalloc"])
+def test_reference_shaped_call_validation(lufqhe_mod, fn):
+    """The reference-shaped calls reject bad geometry before any CUDA call and
+    treat an empty batch as a no-op (the complex64 form also checks alignment)."""
+    lib = lufqhe_mod.lib()
+    f = getattr(lib, fn)
+    assert f(None, 4, 8, 8, 0, None) == -1
+    assert f(FAKE, -1, 8, 8, 0, None) == -1
+    assert f(FAKE, 4, 8, 7, 0, None) == -1
+    assert f(FAKE, 4, 65, 65, 0, None) == -2
+    assert f(FAKE, 0, 8, 8, 0, None) == 0
+    if fn.endswith("_c64"):
+        assert f(ctypes.c_void_p(0x1004), 4, 8, 8, 0, None) == -1

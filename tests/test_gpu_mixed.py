@@ -177,10 +177,10 @@ def test_mixed_deterministic_across_batch_positions(cuda, lufqhe_mod):
 
 
 @pytest.mark.parametrize("share", [0.0, 0.5])
-def test_fp64_pass_list_overflow(cuda, lufqhe_mod, threshold, fp64_share, share):
-    """n = 24 hands every FP64 factorisation to the second pass through a list
-    of 16384 entries per call; with every matrix rejected (threshold 0) a batch
-    just past that size overflows it, and the marked rest must be found too."""
+def test_fp64_pass_every_matrix_listed(cuda, lufqhe_mod, threshold, fp64_share, share):
+    """n = 24 hands every FP64 factorisation to the second pass through the
+    call's pending list, which has room for the whole batch: with every matrix
+    rejected (threshold 0), or half of them routed, all are refactorised."""
     threshold(0.0)
     fp64_share(share)
     batch = 16384 + 1028

@@ -164,8 +164,13 @@ def test_pair_sum(oracle):
 
 # ---------------------------------------------------------------- golden vectors
 def golden_sets():
+    """The sets stored as complex128 inputs (the full fixture is complex64 only)."""
     g = np.load(GOLDEN)
-    return sorted({k.split("/")[0] for k in g.files})
+    return sorted({k.split("/")[0] for k in g.files if k.endswith("/A")})
+
+
+def golden_input32(g, name):
+    return g[f"{name}/A32"] if f"{name}/A32" in g.files else g[f"{name}/A"].astype(np.complex64)
 
 
 @pytest.mark.parametrize("name", golden_sets())
@@ -196,6 +201,52 @@ def test_golden_vs_reference_float32(oracle, name):
     tol = 2e-5
     assert np.abs(np.log(np.abs(d32)) - la).max() < tol * max(1.0, np.abs(la).max())
     assert dphase(np.angle(d32), ph).max() < tol * 10
+
+
+@pytest.mark.parametrize("name", golden_sets() + ["ref_fixture_all"])
+def test_float32_restatement_bit_exact(oracle, name):
+    """The restatement instantiated in float32 reproduces the reference's own
+    compiled LUCoreCPU::determinant bit for bit: the complex64 determinant and
+    the factors it leaves in place (so every pivot and every row swap), on all
+    1000 matrices of the reference's fixture file and on the seeded sets."""
+    g = np.load(GOLDEN)
+    r = oracle.lup_det_f32(golden_input32(g, name))
+    want = g[f"{name}/ref_det_f32"]
+    assert np.array_equal(r["det"].view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(oracle.factor_digests(r["factors"]), g[f"{name}/ref_factor_digest"])
+
+
+def test_fixture_fp64_restatement_pivots(oracle):
+    """On the reference's fixture the FP64 restatement takes the float32
+    restatement's (hence the reference's) pivots, and its log-determinants are
+    the committed ones bit for bit."""
+    g = np.load(GOLDEN)
+    A32 = g["ref_fixture_all/A32"]
+    r32 = oracle.lup_det_f32(A32)
+    r64 = oracle.lup_det(A32.astype(np.complex128))
+    assert (r64["piv"] == r32["piv"]).all()
+    assert (r64["piv"] == g["ref_fixture_all/piv"]).all()
+    assert np.array_equal(r64["logabs"], g["ref_fixture_all/logabs"])
+    assert np.array_equal(r64["phase"], g["ref_fixture_all/phase"])
+    la, ph, _ = oracle.logdet_dd(A32.astype(np.complex128))
+    assert rel(r64["logabs"], la).max() < 1e-12
+    assert dphase(r64["phase"], ph).max() < 1e-12
+
+
+def test_float32_restatement_live(oracle):
+    """Where the reference was compiled here: bit-identical on fresh seeded
+    Gaussian and lowest-Landau-level inputs of several sizes."""
+    if not oracle.ref_available():
+        pytest.skip("reference CPU determinant not built on this machine")
+    rng = np.random.default_rng(15)
+    sets = [cgauss(rng, 500, n) for n in (1, 3, 8, 17)]
+    sets += [oracle.gen_lll(500, n, seed=40 + n)[0] for n in (6, 12, 24)]
+    for A in sets:
+        A32 = A.astype(np.complex64)
+        r = oracle.lup_det_f32(A32)
+        det, fac = oracle.ref_factor_f32(A32)
+        assert np.array_equal(r["det"].view(np.uint32), det.view(np.uint32))
+        assert np.array_equal(r["factors"].view(np.uint32), fac.view(np.uint32))
 
 
 @pytest.mark.parametrize("name", golden_sets())
