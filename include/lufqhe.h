@@ -193,6 +193,47 @@ int lufqhe_lucoregpu_call_noalloc(void *d_matrices, int n_mat, int mat_side, int
 int lufqhe_pair_sum(const double *d_logabs, const double *d_phase, long long batch, double *d_out,
                     void *stream);
 
+/*
+ * The same wavefunction sum straight from the matrices, the pair product and
+ * the sum fused into the factorisation: replaces LUCoreGPU::CALL with
+ * PERFORM_PROD (LU-fqhe/src/LUCoreGPU.cu:403-425) followed by
+ * LUCoreGPU::globalReduction (LU-fqhe/src/LUCoreGPU.cu:113-156, :444-557).
+ * In the plain modes at n <= 32 one kernel does it all: each warp factorises
+ * both matrices of a pair and adds their product to a running complex
+ * log-sum-exp; no per-matrix result is written. In mixed mode, and for
+ * n > 32, the batched call writes log-polar determinants to pool temporaries
+ * and one log-sum-exp pass reduces them. d_out (device, 2 doubles) receives
+ * log|S| and arg S (-inf and 0 for S = 0, NaN if any matrix is not finite).
+ * Layout, dtype and modes as lufqhe_batch_lup_det; an odd last matrix is
+ * dropped (LU-fqhe/src/LUCoreCPU.cu:83). Reproducible for a given device.
+ */
+int lufqhe_batch_pair_sum(const void *d_A, int n, int lda, long long batch, int dtype, int mode,
+                          double *d_out, void *stream);
+
+/* ---- several devices: the host side (plain C, no device call) ---- */
+/*
+ * Complex log-sum-exp of k partial sums given as (log|S_r|, arg S_r) pairs in
+ * parts[2r], parts[2r+1]: out = (log|sum_r S_r|, arg sum_r S_r). The
+ * reduction of per-device (or per-rank) wavefunction sums, which the
+ * reference does with MPI_Reduce on direct complex values
+ * (LU-fqhe/src/MonteCarloLoop.cu:373-392). -inf parts add nothing; a NaN part
+ * gives NaN.
+ */
+int lufqhe_combine_log_sums(const double *parts, long long k, double *out);
+
+/*
+ * Split a batch made of `ngroups` groups of same-size matrices (group g: count[g]
+ * matrices of side n[g], in this order) into `nshards` contiguous shards of
+ * nearly equal factorisation cost (the flops of one n x n LUP per matrix),
+ * for one device each. Shard s takes matrices [begin[s*ngroups+g],
+ * end[s*ngroups+g]) of group g. With pair_aligned, every boundary inside a
+ * group falls on an even index, so no determinant pair of the wavefunction sum
+ * is split. The reference splits by matrix count (LU-fqhe/src/RunInfo.cpp:53,
+ * LU-fqhe/src/MonteCarloLoop.cu:141-148).
+ */
+int lufqhe_shard_by_cost(const int *n, const long long *count, int ngroups, int nshards,
+                         int pair_aligned, long long *begin, long long *end);
+
 /* ---- mixed-size batches: one persistent launch, autotuned, graph-captured ---- */
 /* One group of same-size matrices of a mixed-size batch. Its results go to
  * indices out_offset .. out_offset + count - 1 of the output arrays. */

@@ -363,16 +363,43 @@ def pair_sum(out: DetResult, stream=None):
     return res
 
 
+def batch_pair_sum(A, mode: int = MODE_PLAIN_FP64, stream=None):
+    """log|S| and arg S of S = sum_i det(A_2i) det(A_2i+1) straight from a
+    (batch, n, lda) complex128 / complex64 CUDA tensor (a device tensor of 2)."""
+    import torch
+    batch, n, lda = _shape(A, None)
+    res = torch.empty(2, dtype=torch.float64, device=A.device)
+    rc = lib().lufqhe_batch_pair_sum(A.data_ptr(), n, lda, batch, _dtype_code(A), mode,
+                                     res.data_ptr(), _stream_ptr(stream))
+    _native.check(rc, "lufqhe_batch_pair_sum")
+    return res
+
+
 def combine_log_sums(parts):
     """Complex log-sum-exp of partial sums given as (log|S_r|, arg S_r) pairs:
-    the host-side reduction of per-rank (or per-batch) wavefunction sums."""
-    parts = [(float(a), float(b)) for a, b in parts if a == a and a != float("-inf")]
-    if not parts:
-        return float("-inf"), 0.0
-    m = max(a for a, _ in parts)
-    re = sum(math.exp(a - m) * math.cos(b) for a, b in parts)
-    im = sum(math.exp(a - m) * math.sin(b) for a, b in parts)
-    return m + math.log(math.hypot(re, im)), math.atan2(im, re)
+    the host-side reduction of per-rank (or per-batch) wavefunction sums,
+    computed by the library's C function (lufqhe_combine_log_sums)."""
+    import ctypes
+    flat = [float(v) for p in parts for v in p]
+    arr = (ctypes.c_double * max(1, len(flat)))(*flat)
+    out = (ctypes.c_double * 2)()
+    _native.check(lib().lufqhe_combine_log_sums(arr, len(flat) // 2, out),
+                  "lufqhe_combine_log_sums")
+    return out[0], out[1]
+
+
+def shard_by_cost(groups, nshards: int, pair_aligned: bool = True):
+    """groups: [(n, count), ...] -> per shard, per group, (begin, end) index
+    ranges of nearly equal LUP cost (lufqhe_shard_by_cost)."""
+    import ctypes
+    ng = len(groups)
+    ns = (ctypes.c_int * max(1, ng))(*[g[0] for g in groups])
+    cs = (ctypes.c_longlong * max(1, ng))(*[g[1] for g in groups])
+    b = (ctypes.c_longlong * max(1, ng * nshards))()
+    e = (ctypes.c_longlong * max(1, ng * nshards))()
+    _native.check(lib().lufqhe_shard_by_cost(ns, cs, ng, nshards, int(pair_aligned), b, e),
+                  "lufqhe_shard_by_cost")
+    return [[(b[s * ng + g], e[s * ng + g]) for g in range(ng)] for s in range(nshards)]
 
 
 def allreduce_log_sum(part, group=None):

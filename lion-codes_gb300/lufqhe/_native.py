@@ -29,6 +29,9 @@ SIGNATURES = {
     "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_lucoregpu_call_c64": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_pair_sum": (I32, [P, P, I64, P, P]),
+    "lufqhe_batch_pair_sum": (I32, [P, I32, I32, I64, I32, I32, P, P]),
+    "lufqhe_combine_log_sums": (I32, [P, I64, P]),
+    "lufqhe_shard_by_cost": (I32, [P, P, I32, I32, I32, P, P]),
     "lufqhe_plan_create": (I32, [P, P, I32, I32, P, P, P, P, I32, P]),
     "lufqhe_plan_execute": (I32, [P, P]),
     "lufqhe_plan_launch_direct": (I32, [P, P]),

@@ -26,7 +26,8 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
-SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "lup_mixed_c64.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu"]
+SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "lup_mixed_c64.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu",
+           "host_reduce.cu"]
 
 
 def _nvcc() -> str:

@@ -181,3 +181,58 @@ def test_reference_shaped_call_validation(lufqhe_mod, fn):
     assert f(FAKE, 0, 8, 8, 0, None) == 0
     if fn.endswith("_c64"):
         assert f(ctypes.c_void_p(0x1004), 4, 8, 8, 0, None) == -1
+
+
+def test_combine_log_sums_c(lufqhe_mod):
+    """lufqhe_combine_log_sums: the complex log-sum-exp of (log|S_r|, arg S_r)
+    parts, against the direct sum where it does not overflow; -inf parts add
+    nothing, NaN poisons, no part gives -inf."""
+    rng = np.random.default_rng(8)
+    parts = list(zip(rng.uniform(-5, 5, 9), rng.uniform(-3, 3, 9)))
+    s = sum(np.exp(a + 1j * b) for a, b in parts)
+    la, ar = lufqhe_mod.combine_log_sums(parts)
+    assert abs(la - np.log(abs(s))) < 1e-13 and abs(ar - np.angle(s)) < 1e-13
+    big = [(a + 700.0, b) for a, b in parts] + [(-np.inf, 0.3)]
+    la2, ar2 = lufqhe_mod.combine_log_sums(big)
+    assert abs(la2 - (la + 700.0)) < 1e-12 and abs(ar2 - ar) < 1e-12
+    assert lufqhe_mod.combine_log_sums([]) == (-np.inf, 0.0)
+    assert np.isnan(lufqhe_mod.combine_log_sums(parts + [(np.nan, 0.0)])[0])
+
+
+@pytest.mark.parametrize("groups,nshards", [
+    ([(24, 32768)], 4), ([(6, 1000), (8, 999), (48, 3001), (64, 10)], 3),
+    ([(16, 5)], 8), ([(8, 0), (32, 100), (8, 0)], 2), ([], 3)])
+def test_shard_by_cost(lufqhe_mod, groups, nshards):
+    """Shards cover every matrix exactly once, in order, boundaries inside a
+    group fall on even indices, and the shards' LUP costs differ by at most
+    two matrices of the largest size."""
+    import bench
+    shards = lufqhe_mod.shard_by_cost(groups, nshards, pair_aligned=True)
+    assert len(shards) == nshards
+    cost = []
+    for g, (n, count) in enumerate(groups):
+        pos = 0
+        for s in range(nshards):
+            b, e = shards[s][g]
+            assert b == pos and b <= e <= count
+            if 0 < e < count:
+                assert e % 2 == 0
+            pos = e
+        assert pos == count
+    for s in range(nshards):
+        cost.append(sum((e - b) * max(1.0, bench.flops_per_matrix(groups[g][0]))
+                        for g, (b, e) in enumerate(shards[s])))
+    if groups and sum(c for _, c in groups) > 4 * nshards:
+        biggest = max(bench.flops_per_matrix(n) for n, c in groups if c)
+        assert max(cost) - min(cost) <= 4 * biggest
+
+
+def test_shard_by_cost_rejects(lufqhe_mod):
+    lib = lufqhe_mod.lib()
+    n = (ctypes.c_int * 1)(8)
+    c = (ctypes.c_longlong * 1)(10)
+    b = (ctypes.c_longlong * 2)()
+    e = (ctypes.c_longlong * 2)()
+    assert lib.lufqhe_shard_by_cost(n, c, 1, 0, 1, b, e) == -1
+    bad = (ctypes.c_int * 1)(0)
+    assert lib.lufqhe_shard_by_cost(bad, c, 1, 2, 1, b, e) == -1
