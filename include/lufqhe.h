@@ -53,6 +53,8 @@ extern "C" {
 #define LUFQHE_ST_FALLBACK 8   /* mixed mode: refactorised in FP64 (result is the FP64 one) */
 #define LUFQHE_ST_FP64 16      /* mixed mode: routed straight to the FP64 routine so the FP64
                                   pipe works beside the FP32 pipes (result is the FP64 one) */
+#define LUFQHE_ST_WAIT_TIMEOUT 32 /* a bounded wait inside the kernel (for the copy engine's
+                                     staging of the matrix) ran out: logabs = phase = NaN */
 
 /* ---- element types ---- */
 #define LUFQHE_C128 0
@@ -365,6 +367,11 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
  * they launch, on the launching stream, for lufqhe_kernel_times (not while
  * the stream is being captured); 0 (default): no events. */
 #define LUFQHE_OPT_KERNEL_TIMING 6
+/* 1 (default): the plain FP64 warp kernel and the n >= 24 mixed FP32 pass
+ * stage each complex128 matrix from device memory into shared memory with
+ * the copy engine's bulk copies (one per row, completing on an mbarrier) and
+ * prefetch the next matrix into L2; 0: per-lane vector loads. Same bits. */
+#define LUFQHE_OPT_BULK_LOADS 7
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

@@ -183,6 +183,18 @@ int lib_free_async(void *p, cudaStream_t s) {
   return check_cuda(cudaFreeAsync(p, s), "cudaFreeAsync");
 }
 
+int g_bulk_loads = 1;
+
+bool is_device_memory(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice;
+}
+
 const void *device_address(const void *p) {
   if (!p) return p;
   cudaPointerAttributes a{};
@@ -390,6 +402,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_mixed_refine = (int)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_BULK_LOADS) {
+    if (!(value == 0.0 || value == 1.0)) {
+      set_error("lufqhe_set_option: bulk loads must be 0 or 1");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_bulk_loads = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   if (option == LUFQHE_OPT_KERNEL_TIMING) {
     if (!(value == 0.0 || value == 1.0)) {
       set_error("lufqhe_set_option: kernel timing must be 0 or 1");
@@ -409,6 +429,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_HOST_CHUNK_MB) return (double)g_host_chunk_mb;
   if (option == LUFQHE_OPT_MIXED_REFINE) return (double)g_mixed_refine;
   if (option == LUFQHE_OPT_KERNEL_TIMING) return (double)g_kernel_timing;
+  if (option == LUFQHE_OPT_BULK_LOADS) return (double)g_bulk_loads;
   return NAN;
 }
 

@@ -21,6 +21,10 @@ size_t device_smem_optin();
 // Device address of p: p itself for device memory, the mapped view for
 // page-locked host memory (which kernels then read and write over the host link).
 const void *device_address(const void *p);
+// True if p points into device memory (not mapped host memory): the bulk-copy
+// loads are used only there.
+bool is_device_memory(const void *p);
+extern int g_bulk_loads;  // option LUFQHE_OPT_BULK_LOADS
 // Stream-ordered device memory from the library's own pool.
 int lib_malloc_async(void **p, size_t bytes, cudaStream_t s);
 int lib_free_async(void *p, cudaStream_t s);

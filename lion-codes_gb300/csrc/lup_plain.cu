@@ -12,6 +12,9 @@
 
 #include <cmath>
 
+#include <type_traits>
+
+#include "bulk_copy.cuh"
 #include "lup_fp64.cuh"
 
 namespace lufqhe {
@@ -27,7 +30,7 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
     lup_plain_kernel(Src src, Out *__restrict__ Aout, int n, int lda,
                      long long batch, double *__restrict__ logabs, double *__restrict__ phase,
                      int8_t *__restrict__ parity, int32_t *__restrict__ status,
-                     int status_or) {
+                     int status_or, int bulk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
@@ -39,11 +42,36 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
                  warp * 2 * n;
   const int nn = n * n;
 
-  for (long long b = (long long)blockIdx.x * warps + warp; b < batch;
-       b += (long long)gridDim.x * warps) {
+  // complex128 device batches: each matrix staged by bulk copies (bulk != 0),
+  // the next one prefetched into L2 meanwhile
+  constexpr bool BULK = std::is_same<Src, DenseSource>::value;
+  __shared__ __align__(8) uint64_t bars[kMaxWarpsPlain];
+  WarpBulk wb;
+  if constexpr (BULK)
+    if (bulk) wb.init(&bars[warp], lane);
+  const long long stride = (long long)gridDim.x * warps;
+  for (long long b = (long long)blockIdx.x * warps + warp; b < batch; b += stride) {
     __syncwarp();
     int par = 0;
-    int st = src.load(b, n, M, lds, lane) ? LUFQHE_ST_NONFINITE : 0;
+    int st = -1;
+    if constexpr (BULK) {
+      if (bulk && !wb.broken) {
+        if (b + stride < batch && lane == 0)
+          prefetch_matrix_l2(src.A + (size_t)(b + stride) * n * src.lda, n, src.lda);
+        if (wb.load(src.A + (size_t)b * n * src.lda, n, src.lda, M, lds, lane)) {
+          bool bad = false;
+          BlockWalk w(lane, n);
+          for (int e = lane; e < nn; e += 32) {
+            bad |= !finite_c(M[w.i * lds + w.k]);
+            w.next(n);
+          }
+          st = __any_sync(kFull, bad) ? LUFQHE_ST_NONFINITE : 0;
+        } else {
+          st = LUFQHE_ST_WAIT_TIMEOUT;
+        }
+      }
+    }
+    if (st < 0) st = src.load(b, n, M, lds, lane) ? LUFQHE_ST_NONFINITE : 0;
     if (!st) st = lup_fp64_warp<ARITH>(M, lds, hold, n, lane, &par);
 
     double la, ph;
@@ -158,6 +186,13 @@ __global__ void __launch_bounds__(kGroupWarps * 32)
   }
 }
 
+// the bulk-copy staging for complex128 matrices in device memory only
+inline int bulk_for(const DenseSource &s) { return g_bulk_loads && is_device_memory(s.A); }
+template <class S>
+inline int bulk_for(const S &) {
+  return 0;
+}
+
 size_t plain_smem_per_warp(int n) {
   return (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
 }
@@ -219,7 +254,7 @@ int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int ar
   int grid = (int)(want < cap ? want : cap);
   KernelTimer timer(arith == ARITH_REF ? "lup_plain_kernel_ref" : "lup_plain_kernel", n, stream);
   kern<<<grid, warps * 32, smem, stream>>>(src, Aout, n, lda, batch, logabs, phase, parity, status,
-                                           status_or);
+                                           status_or, bulk_for(src));
   timer.stop();
   return check_cuda(cudaGetLastError(), "lup_plain_kernel launch");
 }

@@ -527,6 +527,17 @@ __device__ __forceinline__ bool route_fp64(const double2 *src, unsigned int shar
   return route_fp64_entry(COHERENT ? __ldcg(src) : __ldg(src), share64k);
 }
 
+// A bounded wait inside the kernel ran out (never expected): NaN result.
+__device__ __forceinline__ void emit_wait_timeout(int lane, long long b, double *logabs,
+                                                  double *phase, int8_t *parity, int32_t *status) {
+  if (lane == 0) {
+    logabs[b] = NAN;
+    if (phase) phase[b] = NAN;
+    if (parity) parity[b] = 0;
+    if (status) status[b] = LUFQHE_ST_WAIT_TIMEOUT;
+  }
+}
+
 __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *logabs,
                                                double *phase, int8_t *parity, int32_t *status) {
   if (lane == 0) {
@@ -727,7 +738,9 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
 //    masks; the pivots 1 + d_t go to `diag` and their logs are taken one per
 //    lane at the end.
 // Outcome of the tile path for one matrix.
-enum { TILE_REJECT = 0, TILE_ACCEPT = 1, TILE_REFINE = 2 };
+// TILE_NONFINITE: a NaN or Inf entry (only for matrices whose load did not
+// check it: the bulk-copied ones)
+enum { TILE_REJECT = 0, TILE_ACCEPT = 1, TILE_REFINE = 2, TILE_NONFINITE = 3 };
 
 template <int N>
 struct TileRegs {
@@ -1055,16 +1068,20 @@ __device__ int mixed_factor_tile_ex(float4 *HL, float2 *F, int *er, int *ec, int
   constexpr int SB = TileGeom<N>::SB;
   const double2 *A = reinterpret_cast<const double2 *>(HL);
 
-  // 1. exponents, columns first
+  // 1. exponents, columns first (a NaN or Inf entry has the exponent field
+  //    of 2^1024: the matrix is reported non-finite)
   int esum = 0;
+  bool bad = false;
   if (lane < N) {
     int m = -2000;
 #pragma unroll 4
     for (int i = 0; i < N; ++i) m = max(m, cexp_field(A[i * LDS + lane]));
+    bad = m == 1024;
     if (m == -2000) m = 0;
     ec[lane] = m;
     esum = m;
   }
+  if (__any_sync(kFull, bad)) return TILE_NONFINITE;
   __syncwarp();
   if (lane < N) {
     int m = -2000;

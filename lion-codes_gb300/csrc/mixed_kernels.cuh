@@ -58,6 +58,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "bulk_copy.cuh"
 #include "mixed_core.cuh"
 
 namespace lufqhe {
@@ -228,7 +229,7 @@ template <int N, class Src, bool INPLACE = false>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     lup_mixed_tile_kernel(Src src, long long batch, float theta2,
                           unsigned int share64k, CallHead *head, unsigned int *pend,
-                          double2 *spill, unsigned char *refine, long long refine_cap,
+                          double2 *spill, unsigned char *refine, long long refine_cap, int bulk,
                           double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
@@ -238,6 +239,8 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   // INPLACE keeps them in this kernel: for a batch read over the host link,
   // where the FP32 pass waits on the link and has compute to spare.
   constexpr bool DEFER = !INPLACE && N >= kDeferMinN;
+  // complex128 device batches: the matrix is staged by bulk copies (bulk != 0)
+  constexpr bool BULK = DEFER && std::is_same<Src, DenseSource>::value;
   constexpr int LDS = N + 1;
   constexpr size_t NL = (size_t)N * LDS;
   const int warps = blockDim.x >> 5;
@@ -256,11 +259,22 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   // KB per warp, so the copies stay in L2); an FP64 refactorisation reloads
   // it from there instead of reading the matrix over the host link again
   double2 *own = INPLACE ? spill + ((size_t)blockIdx.x * warps + warp) * N * N : nullptr;
+  __shared__ __align__(8) uint64_t bars[kMaxWarpsMixed];
+  WarpBulk wb;
+  if constexpr (BULK)
+    if (bulk) wb.init(&bars[warp], lane);
 
   DeferredOut out;
-  for (long long b = claim_matrix(head, lane, -1); b < batch; b = claim_matrix(head, lane, b)) {
+  // the next matrix is claimed one ahead, so that its bytes can be on their
+  // way to L2 while the current one is factorised
+  long long b = claim_matrix(head, lane, -1);
+  long long nb = b < batch ? claim_matrix(head, lane, b) : batch;
+  for (; b < batch; b = nb, nb = b < batch ? claim_matrix(head, lane, b) : batch) {
     __syncwarp();
     double2 *M = reinterpret_cast<double2 *>(HL);
+    if constexpr (BULK)
+      if (bulk && nb < batch && lane == 0)
+        prefetch_matrix_l2(src.A + (size_t)nb * N * src.lda, N, src.lda);
     if (share64k && route_fp64_entry(src.first(b, N), share64k)) {
       if constexpr (DEFER)
         defer_fp64(head, pend, b, lane, true);
@@ -269,7 +283,17 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
                           LUFQHE_ST_FP64);
       continue;
     }
-    if (src.load(b, N, M, LDS, lane)) {
+    bool staged = false;
+    if constexpr (BULK) {
+      if (bulk && !wb.broken) {
+        if (!wb.load(src.A + (size_t)b * N * src.lda, N, src.lda, M, LDS, lane)) {
+          emit_wait_timeout(lane, b, logabs, phase, parity, status);
+          continue;
+        }
+        staged = true;  // finite check: in the exponent pass
+      }
+    }
+    if (!staged && src.load(b, N, M, LDS, lane)) {
       emit_nonfinite(lane, b, logabs, phase, parity, status);
       continue;
     }
@@ -288,6 +312,8 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
           mixed_factor_tile_ex<N, true>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
       if (code == TILE_ACCEPT)
         out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
+      else if (code == TILE_NONFINITE)
+        emit_nonfinite(lane, b, logabs, phase, parity, status);
       // a matrix within theta but above the FP32 solves' cap gets its back
       // substitution refined in the next pass, if the buffer has room
       else if (!(code == TILE_REFINE && refine &&
@@ -417,6 +443,13 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
   }
 }
 
+// the bulk-copy staging for complex128 matrices in device memory only
+inline int bulk_for(const DenseSource &s) { return g_bulk_loads && is_device_memory(s.A); }
+template <class S>
+inline int bulk_for(const S &) {
+  return 0;
+}
+
 // A call's state block: the head, the pending list (pend_cap entries), the
 // saved matrices of the refinement (refine_bytes) and the host-link copies
 // (spill_bytes), each 256-byte aligned; the head is zeroed on `stream`.
@@ -540,8 +573,8 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     KernelTimer timer(inplace ? "lup_mixed_tile_kernel_hostlink" : "lup_mixed_tile_kernel", N,
                       stream);
     kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), cs.head, cs.pend,
-                                             cs.spill, cs.refine, refine_cap, logabs, phase,
-                                             parity, status);
+                                             cs.spill, cs.refine, refine_cap, bulk_for(src),
+                                             logabs, phase, parity, status);
     timer.stop();
   }
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
