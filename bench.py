@@ -714,10 +714,14 @@ def run_plan(args, world, rank, local, full=True):
 
 
 def run_serve(args, world, rank, local, full=True):
-    """Config 5: offline capacity per size class, then the Poisson walker
-    stream at 70% of it and at the configured 20k requests/s; p50/p99 latency
-    (arrival to result on the host) and throughput; mixed and (with `full`)
-    FP64 servers."""
+    """Config 5: a Poisson stream of single-particle moves of device-resident
+    walkers (k log-uniform 1..4096, n uniform over 8/16/32/64, 100 moves per
+    walker). Three servers: O(n^2) moves against kept FP64 factors (the
+    default), and servers that refactorise every move, mixed and FP64. For
+    each: its capacity (the determinants/s of a saturating stream), then the
+    stream at 70% of that capacity and at the configured 20k requests/s, with
+    p50/p99 latency (arrival to result on the host) and throughput. The
+    batched factorisation rates of the size mix are reported beside them."""
     import numpy as np
     import torch
 
@@ -744,47 +748,58 @@ def run_serve(args, world, rank, local, full=True):
         torch.cuda.synchronize()
         return count / (e0.elapsed_time(e1) / 3 * 1e-3)
 
+    def summary(lat, ns, el, mats, rate, capacity):
+        per = {}
+        for n in SERVE_SIZES:
+            m = ns == n
+            if m.any():
+                per[str(n)] = {"p50_ms": float(np.percentile(lat[m], 50) / 1e3),
+                               "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
+                               "requests": int(m.sum())}
+        return {"rate_req_s": rate, "requests": int(len(lat)),
+                "p50_ms": float(np.percentile(lat, 50) / 1e3),
+                "p99_ms": float(np.percentile(lat, 99) / 1e3),
+                "throughput_dets_s": mats / el,
+                "fraction_of_capacity": (mats / el) / capacity if capacity else None,
+                "per_n": per}
+
+    variants = [("moves", lufqhe.MODE_MIXED, True), ("mixed_refactor", lufqhe.MODE_MIXED, False),
+                ("fp64_refactor", lufqhe.MODE_PLAIN_FP64_FUSED, False)]
     result = {}
-    modes = (("mixed", lufqhe.MODE_MIXED), ("fp64", lufqhe.MODE_PLAIN_FP64_FUSED))
-    for label, mode in (modes if full else modes[:1]):
+    for label, mode, moves in (variants if full else variants[:2]):
         rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
-        sec_per_matrix = float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
-        offline_mps = 1.0 / sec_per_matrix                  # matrices/s of the mix
-        cap_req = offline_mps / mean_k                      # requests/s at full load
-        inv = np.array([1.0 / rates[n] for n in SERVE_SIZES])
-        sms = np.maximum(2, np.round(152 * inv / inv.sum())).astype(int)
+        batched_mix = 1.0 / float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
+        # SM shares per class: by the batched cost for refactorising servers;
+        # by an O(n^2) move plus a share of refactorisations for the moves one
+        if moves:
+            cost = np.array([n * n * 8.0 + 0.15 * n ** 3 / 3.0 * 4.0 for n in SERVE_SIZES])
+        else:
+            cost = np.array([1.0 / rates[n] for n in SERVE_SIZES])
+        sms = np.maximum(2, np.round(152 * cost / cost.sum())).astype(int)
         sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
-        srv = lufqhe.Server(64 << 30, mode=mode, classes=SERVE_SIZES, class_sms=list(map(int, sms)),
-                            max_k=4096, tile=8)
-        runs = {}
-        for tag, rate, nr in (("at_70pct_offline", 0.7 * cap_req, nreq),
+        srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES,
+                            class_sms=list(map(int, sms)), max_k=4096, tile=8, moves=moves)
+        # capacity: a stream far faster than the server can take
+        lat, ns, el, mats = srv.run_stream(rate_hz=1e6, nrequests=max(400, nreq // 2), moves=100,
+                                           k_min=1, k_max=4096, seed=seed + 1)
+        capacity = mats / el
+        runs = {"saturated": summary(lat, ns, el, mats, 1e6, capacity)}
+        for tag, rate, nr in (("at_70pct_capacity", 0.7 * capacity / mean_k, nreq),
                               ("at_20k_req_s", 20000.0, max(200, nreq // 4))):
             lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100, k_min=1,
                                                k_max=4096, seed=seed)
-            per = {}
-            for n in SERVE_SIZES:
-                m = ns == n
-                if m.any():
-                    per[str(n)] = {"p50_ms": float(np.percentile(lat[m], 50) / 1e3),
-                                   "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
-                                   "requests": int(m.sum())}
-            runs[tag] = {"rate_req_s": rate, "requests": int(len(lat)),
-                         "p50_ms": float(np.percentile(lat, 50) / 1e3),
-                         "p99_ms": float(np.percentile(lat, 99) / 1e3),
-                         "throughput_dets_s": mats / el,
-                         "fraction_of_offline": (mats / el) / offline_mps,
-                         "per_n": per}
+            runs[tag] = summary(lat, ns, el, mats, rate, capacity)
         srv.close()
-        result[label] = {"offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
-                         "offline_mix_dets_per_s": offline_mps,
-                         "offline_capacity_req_s": cap_req, "class_sms": list(map(int, sms)),
-                         "runs": runs}
+        result[label] = {"capacity_dets_per_s": capacity,
+                         "batched_offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
+                         "batched_offline_mix_dets_per_s": batched_mix,
+                         "class_sms": list(map(int, sms)), "runs": runs}
     if rank != 0:
         return None
-    r70 = result["mixed"]["runs"]["at_70pct_offline"]
+    r70 = result["moves"]["runs"]["at_70pct_capacity"]
     return {"value": r70["throughput_dets_s"], "unit": "dets/s",
             "p50_ms": r70["p50_ms"], "p99_ms": r70["p99_ms"],
-            "fraction_of_offline": r70["fraction_of_offline"],
+            "fraction_of_capacity": r70["fraction_of_capacity"],
             "config": workload_config("serving", world) | {"mean_k": mean_k},
             "serving": result}
 

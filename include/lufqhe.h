@@ -372,6 +372,15 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
  * the copy engine's bulk copies (one per row, completing on an mbarrier) and
  * prefetch the next matrix into L2; 0: per-lane vector loads. Same bits. */
 #define LUFQHE_OPT_BULK_LOADS 7
+/* Servers created while this is 1 (default) keep each walker matrix's FP64
+ * L\U factors and take a move's determinant ratio from an O(n^2) solve
+ * against them (matrix determinant lemma, Woodbury over the moves since the
+ * last factorisation), checked before use (residual of the solve against the
+ * resident matrix, cancellation in the ratio); a move that fails a check, or
+ * the 9th since the last factorisation, refactorises in FP64. Every
+ * factorisation is then FP64 (status LUFQHE_ST_FP64 in mixed mode). 0: every
+ * move refactorises (mixed mode's FP32 path where the policy allows). */
+#define LUFQHE_OPT_SERVE_MOVES 8
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

@@ -184,6 +184,7 @@ int lib_free_async(void *p, cudaStream_t s) {
 }
 
 int g_bulk_loads = 1;
+int g_serve_moves = 1;
 
 bool is_device_memory(const void *p) {
   if (!p) return false;
@@ -402,6 +403,14 @@ extern "C" int lufqhe_set_option(int option, double value) {
     g_mixed_refine = (int)value;
     return LUFQHE_SUCCESS;
   }
+  if (option == LUFQHE_OPT_SERVE_MOVES) {
+    if (!(value == 0.0 || value == 1.0)) {
+      set_error("lufqhe_set_option: serve moves must be 0 or 1");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_serve_moves = (int)value;
+    return LUFQHE_SUCCESS;
+  }
   if (option == LUFQHE_OPT_BULK_LOADS) {
     if (!(value == 0.0 || value == 1.0)) {
       set_error("lufqhe_set_option: bulk loads must be 0 or 1");
@@ -430,6 +439,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_MIXED_REFINE) return (double)g_mixed_refine;
   if (option == LUFQHE_OPT_KERNEL_TIMING) return (double)g_kernel_timing;
   if (option == LUFQHE_OPT_BULK_LOADS) return (double)g_bulk_loads;
+  if (option == LUFQHE_OPT_SERVE_MOVES) return (double)g_serve_moves;
   return NAN;
 }
 

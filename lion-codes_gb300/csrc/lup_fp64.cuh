@@ -239,10 +239,16 @@ __device__ __forceinline__ double div_rn_markstein(double a, double b, double y,
 // other a_k by more than 16 ulps, RN(q_m) > RN(q_k) for all k, so m is the
 // reference's choice; otherwise (near-ties, zero or extreme quotients) the
 // exact quotients are computed and compared with the reference's rule.
+//
+// perm (optional, n ints of shared memory): perm[j] receives the original row
+// of pivoted row j, for callers that keep the factors for later solves.
 template <int ARITH>
-__device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane, int *parity) {
+__device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane, int *parity,
+                             int *perm = nullptr) {
   int par = 0;
   double *rhold = hold + n;
+  if (perm)
+    for (int i = lane; i < n; i += 32) perm[i] = i;
   {
     bool tiny = false;
     const long long tiny_bits = __double_as_longlong(1e-24);
@@ -323,6 +329,11 @@ __device__ int lup_fp64_warp(double2 *M, int lds, double *hold, int n, int lane,
       if (lane == 0) {
         hold[p] = hold[j];
         rhold[p] = rhold[j];
+        if (perm) {
+          const int t = perm[p];
+          perm[p] = perm[j];
+          perm[j] = t;
+        }
       }
       par ^= 1;
     }
@@ -405,8 +416,10 @@ struct NamedBarrier {
 // nthr number the group's threads. Group-uniform return value.
 template <int ARITH, class Bar = CtaBarrier>
 __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid, int nthr,
-                              long long *red, int *parity, Bar bar = Bar()) {
+                              long long *red, int *parity, Bar bar = Bar(), int *perm = nullptr) {
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+  if (perm)
+    for (int i = tid; i < n; i += nthr) perm[i] = i;
   long long *red_k = red;
   int *red_i = reinterpret_cast<int *>(red + nw);
   unsigned *red_n = reinterpret_cast<unsigned *>(red_i + nw);
@@ -503,6 +516,11 @@ __device__ int lup_fp64_group(double2 *M, int lds, double *hold, int n, int tid,
       if (tid == 0) {
         hold[p] = hold[j];
         rhold[p] = rhold[j];
+        if (perm) {
+          const int t = perm[p];
+          perm[p] = perm[j];
+          perm[j] = t;
+        }
       }
       par ^= 1;
     }

@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   // where the FP32 pass waits on the link and has compute to spare.
   constexpr bool DEFER = !INPLACE && N >= kDeferMinN;
   // complex128 device batches: the matrix is staged by bulk copies (bulk != 0)
-  constexpr bool BULK = DEFER && std::is_same<Src, DenseSource>::value;
+  constexpr bool BULK = !INPLACE && std::is_same<Src, DenseSource>::value;
   constexpr int LDS = N + 1;
   constexpr size_t NL = (size_t)N * LDS;
   const int warps = blockDim.x >> 5;
@@ -323,8 +323,18 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     } else {
       // in place: the refinement (refine_cap != 0), then FP64 (n < 24, where
       // both are rare, and the host-link variant, which has compute to spare)
-      if (mixed_factor_tile<N>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par,
-                               refine_cap != 0))
+      const int code =
+          mixed_factor_tile_ex<N, true>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par);
+      if (code == TILE_NONFINITE) {  // a staged matrix (the others were checked on load)
+        emit_nonfinite(lane, b, logabs, phase, parity, status);
+        continue;
+      }
+      if (code == TILE_ACCEPT ||
+          (code == TILE_REFINE && refine_cap != 0 &&
+           mixed_refine_tile<N>(F, reinterpret_cast<float2 *>(HL),
+                                reinterpret_cast<float2 *>(HL) + N * (N + 1),
+                                reinterpret_cast<float2 *>(er), lane, theta2,
+                                tile_la_est(prod, exp_sum), corr)))
         out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
       else if constexpr (INPLACE)
         fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,

@@ -36,12 +36,16 @@
 #include <vector>
 
 #include "mixed_core.cuh"
+#include "serve_moves.cuh"
 
 namespace lufqhe {
 
 namespace {
 
 using namespace mixed;
+
+// Moves kept per matrix between refactorisations (the O(n^2) move path)
+constexpr int kMoveK = 8;
 
 constexpr unsigned kRing = 1u << 16;                  // tiles per class ring
 constexpr unsigned long long kIdleNs = 200000000ull;  // 0.2 s without a claim
@@ -65,7 +69,13 @@ struct ServeTile {
   int count;
   int particle;
   int build;                 // 1: build every row from z first (a walker's first request)
-  int pad;
+  int moves;                 // 1: O(n^2) moves against kept factors (the arrays below)
+  // per-matrix move arrays of the tile's first matrix (serve_moves.cuh)
+  double2 *lu;               // n x n each
+  int *perm;                 // n each
+  double2 *w, *v;            // kMoveK x n each
+  double2 *cap;              // kMoveK x kMoveK each
+  MoveState *mst;
 };
 
 struct ClassCtl {                // device memory, one per class
@@ -93,7 +103,8 @@ __device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) 
 // Apply the move to the tile's matrices: z_particle <- znew, then rebuild that
 // row (lane j handles matrix j); with t.build every row of every matrix is
 // built from z instead (lanes over rows), which is how a walker's matrices are
-// first made, inside the loop so no other kernel needs an SM.
+// first made, inside the loop so no other kernel needs an SM. With t.moves the
+// row is left to the move path, which needs the old row too.
 __device__ void apply_move(const ServeTile &t, int n, int lane) {
   if (t.particle >= 0 && t.znew) {
     for (int j0 = 0; j0 < t.count; j0 += 32) {
@@ -101,7 +112,8 @@ __device__ void apply_move(const ServeTile &t, int n, int lane) {
       if (j < t.count) {
         const double2 z = __ldcv(t.znew + j);
         t.z[(size_t)j * n + t.particle] = z;
-        if (!t.build) lll_row_rn(z, n, t.mats + (size_t)j * n * n + (size_t)t.particle * n);
+        if (!t.build && !t.moves)
+          lll_row_rn(z, n, t.mats + (size_t)j * n * n + (size_t)t.particle * n);
       }
     }
     __syncwarp();
@@ -118,17 +130,81 @@ __device__ void apply_move(const ServeTile &t, int n, int lane) {
 // Shared memory per warp: the FP64 matrix (as double2, aliased by the FP32
 // path's hi/lo copy) and the row scales come first; the FP32 factor and the
 // exponents follow and are left out when every matrix takes the FP64 kernel.
-size_t serve_smem_per_warp(int n, bool fp64_only) {
+// With moves (every factorisation FP64, its factors kept) the FP32 arrays give
+// way to the move path's scratch.
+size_t serve_smem_per_warp(int n, bool fp64_only, bool moves) {
   const size_t nl = (size_t)n * (n + 1);
   size_t b = nl * sizeof(float4) + 2 * (size_t)n * sizeof(double);
+  if (moves) return b + ((MoveScratch::bytes(n, kMoveK) + 15) & ~(size_t)15);
   if (!fp64_only) b += nl * sizeof(float2) + 2 * (size_t)n * sizeof(int);
   return b;
+}
+
+// Matrix j of a tile with moves: its arrays.
+__device__ __forceinline__ MoveArrays move_arrays(const ServeTile &t, int n, int j) {
+  MoveArrays a;
+  a.A = t.mats + (size_t)j * n * n;
+  a.LU = t.lu + (size_t)j * n * n;
+  a.perm = t.perm + (size_t)j * n;
+  a.W = t.w + (size_t)j * kMoveK * n;
+  a.V = t.v + (size_t)j * kMoveK * n;
+  a.C = t.cap + (size_t)j * kMoveK * kMoveK;
+  a.st = t.mst + j;
+  return a;
+}
+
+// The new row of particle i of matrix j (lane 0 builds it; all lanes see it).
+__device__ __forceinline__ void move_new_row(const ServeTile &t, int n, int j, double2 *r,
+                                             int lane) {
+  if (lane == 0) lll_row_rn(__ldcg(t.z + (size_t)j * n + t.particle), n, r);
+  __syncwarp();
+}
+
+// Outputs of matrix j of a tile: log|det|, wrapped phase, status.
+__device__ __forceinline__ void serve_emit(const ServeTile &t, int j, double la, double ph,
+                                           int st) {
+  t.logabs[j] = la;
+  t.phase[j] = (la == la && la > -INFINITY) ? wrap_phase(ph) : ph;
+  t.status[j] = st;
+}
+
+// FP64 factorisation of the tile's matrix j (already in M) by one warp, keeping
+// its factors, pivot order and log-determinant for later moves.
+__device__ void refactor_keep_warp(const MoveArrays &a, int n, double2 *M, int lds, double *hold,
+                                   int *perm, int lane, double *la, double *ph, int *st) {
+  int par = 0;
+  *st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par, perm);
+  if (*st == 0) {
+    logdet_from_diag(M, lds, n, lane, par, la, ph);
+  } else if (*st == LUFQHE_ST_SINGULAR) {
+    *la = -INFINITY;
+    *ph = 0.0;
+  } else {
+    *la = NAN;
+    *ph = NAN;
+  }
+  __syncwarp();
+  BlockWalk w(lane, n);
+  for (int e = lane; e < n * n; e += 32) {
+    a.LU[e] = M[w.i * lds + w.k];
+    w.next(n);
+  }
+  for (int p = lane; p < n; p += 32) a.perm[p] = perm[p];
+  if (lane == 0) {
+    MoveState s;
+    s.la = *st == 0 ? *la : NAN;  // a singular matrix is refactorised again next move
+    s.ph = *ph;
+    s.m = 0;
+    s.pad = 0;
+    *a.st = s;
+  }
 }
 
 template <int NC>
 __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
     serve_kernel(const ServeTile *ring, const unsigned int *published, const unsigned int *stop,
-                 ClassCtl *ctl, int mode, float theta2, unsigned int share64k, int refine) {
+                 ClassCtl *ctl, int mode, float theta2, unsigned int share64k, int refine,
+                 int moves) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = NC + 1;
   constexpr size_t NL = (size_t)NC * LDS;
@@ -141,10 +217,16 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
   double *hold = reinterpret_cast<double *>(base) + warp * 2 * NC;
   base += warps * 2 * (size_t)NC * sizeof(double);
   // FP32-path arrays: only addressed when some matrix takes the FP32 path
+  // (never with moves, whose scratch takes their place)
   float2 *F = reinterpret_cast<float2 *>(base) + warp * NL;
-  base += warps * NL * sizeof(float2);
-  int *er = reinterpret_cast<int *>(base) + warp * 2 * NC;
+  int *er = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(base) +
+                                    warps * NL * sizeof(float2)) +
+            warp * 2 * NC;
   int *ec = er + NC;
+  MoveScratch S;
+  constexpr size_t kScratch = (MoveScratch::bytes(NC, kMoveK) + 15) & ~(size_t)15;
+  S.bind(base + warp * kScratch, NC, kMoveK);
+  (void)moves;
 
   for (;;) {
     // claim the next published tile; give up when the class has been idle
@@ -199,6 +281,35 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
       __syncwarp();
       const double2 *src = t.mats + (size_t)j * NC * NC;
       double2 *M = reinterpret_cast<double2 *>(HL);
+      if (t.moves) {
+        // O(n^2) move against the kept factors; an FP64 refactorisation (its
+        // factors kept) for a walker's first request, a recompute, or a move
+        // that fails its checks
+        const MoveArrays a = move_arrays(t, NC, j);
+        const int flag = mode == LUFQHE_MODE_MIXED ? LUFQHE_ST_FP64 : 0;
+        double la = 0.0, ph = 0.0;
+        bool done = false;
+        if (!t.build && t.particle >= 0) {
+          move_new_row(t, NC, j, S.r, lane);
+          done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
+          __syncwarp();
+        }
+        int st = 0;
+        if (!done) {
+          if (load_matrix_fp64<true>(src, NC, NC, M, LDS, lane)) {
+            st = LUFQHE_ST_NONFINITE;
+            la = ph = NAN;
+            if (lane == 0) a.st->la = NAN;  // refactorised again by the next move
+          } else {
+            refactor_keep_warp(a, NC, M, LDS, hold, S.perm, lane, &la, &ph, &st);
+            st |= flag;
+          }
+        } else {
+          st = flag;
+        }
+        if (lane == 0) serve_emit(t, j, la, ph, st);
+        continue;
+      }
       if (load_matrix_fp64<true>(src, NC, NC, M, LDS, lane)) {
         emit_nonfinite(lane, j, t.logabs, t.phase, nullptr, t.status);
         continue;
@@ -302,10 +413,11 @@ template <int NC>
 __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
     serve_group_kernel(const ServeTile *ring, const unsigned int *published,
                        const unsigned int *stop, ClassCtl *ctl, int mode, float theta2,
-                       unsigned int share64k, int refine) {
+                       unsigned int share64k, int refine, int moves) {
   (void)theta2;
   (void)share64k;
   (void)refine;
+  (void)moves;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LDS = NC + 1;
   constexpr size_t NL = (size_t)NC * LDS;
@@ -314,12 +426,20 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
   __shared__ long long red_s[kServeGroupsMax][3 * kFp64GroupWarps];
   __shared__ unsigned long long tile_s[kServeGroupsMax][TW];
   __shared__ int go_s[kServeGroupsMax];
+  __shared__ int moved_s[kServeGroupsMax];
   const int groups = blockDim.x / GT;
   const int g = threadIdx.x / GT;
   const int tid = threadIdx.x - g * GT, lane = tid & 31;
   double2 *M = reinterpret_cast<double2 *>(smem_raw) + g * NL;
   double *hold =
       reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) + groups * NL) + g * 2 * NC;
+  // the move path's scratch, one per group, after the row scales
+  constexpr size_t kScratch = (MoveScratch::bytes(NC, kMoveK) + 15) & ~(size_t)15;
+  MoveScratch S;
+  S.bind(reinterpret_cast<unsigned char *>(reinterpret_cast<double *>(
+             reinterpret_cast<double2 *>(smem_raw) + groups * NL) + groups * 2 * NC) +
+             g * kScratch,
+         NC, kMoveK);
   const NamedBarrier bar{1 + g, GT};
   for (;;) {
     if (tid == 0) {
@@ -349,6 +469,67 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
     for (int j = 0; j < t.count; ++j) {
       bar.sync();  // the move's rows are written; M is free again
       const double2 *src = t.mats + (size_t)j * NC * NC;
+      if (t.moves) {
+        // warp 0 tries the O(n^2) move; if it is refused (or this is a
+        // walker's first request or a recompute) the group refactorises in
+        // FP64 and keeps the factors
+        const MoveArrays a = move_arrays(t, NC, j);
+        const int flag = mode == LUFQHE_MODE_MIXED ? LUFQHE_ST_FP64 : 0;
+        if (tid < 32) {
+          double la = 0.0, ph = 0.0;
+          bool done = false;
+          if (!t.build && t.particle >= 0) {
+            move_new_row(t, NC, j, S.r, lane);
+            done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
+          }
+          if (done && lane == 0) serve_emit(t, j, la, ph, flag);
+          if (lane == 0) moved_s[g] = done;
+        }
+        bar.sync();
+        if (moved_s[g]) continue;
+        bool bad = false;
+        StrideWalk w(tid, GT, NC);
+        for (int e = tid; e < NC * NC; e += GT) {
+          const double2 v = __ldcg(src + (size_t)w.i * NC + w.k);
+          bad |= !finite_c(v);
+          M[w.i * LDS + w.k] = v;
+          w.next(NC);
+        }
+        bad = bar.sync_or(bad);
+        int par = 0;
+        const int st = bad ? LUFQHE_ST_NONFINITE
+                           : lup_fp64_group<ARITH_FUSED>(M, LDS, hold, NC, tid, GT, red_s[g], &par,
+                                                         bar, S.perm);
+        bar.sync();
+        StrideWalk w2(tid, GT, NC);
+        for (int e = tid; e < NC * NC; e += GT) {
+          a.LU[e] = M[w2.i * LDS + w2.k];
+          w2.next(NC);
+        }
+        for (int p = tid; p < NC; p += GT) a.perm[p] = S.perm[p];
+        if (tid < 32) {
+          double la, ph;
+          if (st == 0) {
+            logdet_from_diag(M, LDS, NC, lane, par, &la, &ph);
+          } else if (st == LUFQHE_ST_SINGULAR) {
+            la = -INFINITY;
+            ph = 0.0;
+          } else {
+            la = NAN;
+            ph = NAN;
+          }
+          if (lane == 0) {
+            MoveState s;
+            s.la = st == 0 ? la : NAN;
+            s.ph = ph;
+            s.m = 0;
+            s.pad = 0;
+            *a.st = s;
+            serve_emit(t, j, la, ph, bad ? st : st | flag);
+          }
+        }
+        continue;
+      }
       bool bad = false;
       StrideWalk w(tid, GT, NC);
       for (int e = tid; e < NC * NC; e += GT) {
@@ -396,7 +577,37 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
 }
 
 using ServeKernel = void (*)(const ServeTile *, const unsigned int *, const unsigned int *,
-                             ClassCtl *, int, float, unsigned int, int);
+                             ClassCtl *, int, float, unsigned int, int, int);
+
+// A walker's block in the HBM pool: its matrices and coordinates, and with
+// moves the per-matrix move arrays, each part 256-byte aligned.
+struct WalkerLayout {
+  size_t mats, z, lu, perm, w, v, cap, mst, total;
+  WalkerLayout(int n, int k, bool moves) {
+    auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    size_t o = 0;
+    mats = o;
+    o += up((size_t)k * n * n * sizeof(double2));
+    z = o;
+    o += up((size_t)k * n * sizeof(double2));
+    lu = perm = w = v = cap = mst = o;
+    if (moves) {
+      lu = o;
+      o += up((size_t)k * n * n * sizeof(double2));
+      perm = o;
+      o += up((size_t)k * n * sizeof(int));
+      w = o;
+      o += up((size_t)k * kMoveK * n * sizeof(double2));
+      v = o;
+      o += up((size_t)k * kMoveK * n * sizeof(double2));
+      cap = o;
+      o += up((size_t)k * kMoveK * kMoveK * sizeof(double2));
+      mst = o;
+      o += up((size_t)k * sizeof(MoveState));
+    }
+    total = o;
+  }
+};
 
 ServeKernel serve_group_kernel_for(int n) {
   switch (n) {
@@ -478,6 +689,7 @@ struct lufqhe_server_s {
   int tile = 8;
   float theta2 = 0.01f;
   int refine = 1;  // in-place refinement of the tile path (option 5)
+  int moves = 1;   // O(n^2) moves against kept FP64 factors (option 8)
   std::vector<SClass> classes;
   // HBM pool with a first-fit free list
   unsigned char *pool = nullptr;
@@ -552,7 +764,7 @@ int ensure_running(lufqhe_server_s *s, SClass &c) {
   // (the shared memory of an FP64-only class holds no FP32 arrays, so the
   // share is the one fixed when the class was created)
   c.kern<<<c.grid, c.warps * 32, c.smem, c.stream>>>(c.ring_d, c.pub_d, s->stop_d, c.ctl, s->mode,
-                                                     s->theta2, c.share64k, s->refine);
+                                                     s->theta2, c.share64k, s->refine, s->moves);
   int rc = check_cuda(cudaGetLastError(), "serve kernel launch");
   if (rc) return rc;
   c.running = true;
@@ -597,6 +809,7 @@ int host_mapped(T **h, T **d, size_t count, const char *what) {
 namespace lufqhe {
 extern float g_mixed_theta;
 extern int g_mixed_refine;
+extern int g_serve_moves;
 }
 
 extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
@@ -617,6 +830,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
   s->tile = tile;
   s->theta2 = g_mixed_theta * g_mixed_theta;
   s->refine = g_mixed_refine;
+  s->moves = g_serve_moves;
   s->slots.resize(kReqSlots);
   int rc = LUFQHE_SUCCESS;
   const int sms = device_sm_count();
@@ -634,13 +848,15 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     sc.sms = std::max(1, std::min(want, sms_left - (nclasses - 1 - c)));
     sms_left -= sc.sms;
     sc.share64k = mode == LUFQHE_MODE_MIXED ? fp64_share_64k(sc.n) : 0u;
-    const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u;
+    // with moves every factorisation is FP64 (its factors are kept)
+    const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u || s->moves;
     const size_t optin = device_smem_optin();
     size_t used = 0;
     if (fp64_only && serve_group_kernel_for(sc.n)) {
       // warp groups, one matrix each
       sc.kern = serve_group_kernel_for(sc.n);
-      const size_t per_group = serve_group_smem(sc.n);
+      const size_t per_group = serve_group_smem(sc.n) +
+                               ((MoveScratch::bytes(sc.n, kMoveK) + 15) & ~(size_t)15);
       const int groups = std::min<int>(kServeGroupsMax, (int)((optin - 4096) / per_group));
       if (groups < 1) {
         set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per matrix", sc.n,
@@ -651,7 +867,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
       sc.warps = groups * kFp64GroupWarps;
       used = per_group * groups;
     } else {
-      const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only);
+      const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only, s->moves != 0);
       sc.warps = std::max(1, std::min<int>(serve_max_warps(sc.n), (int)(optin / per_warp)));
       if (per_warp * sc.warps > optin) {
         set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per warp", sc.n,
@@ -719,7 +935,8 @@ extern "C" int lufqhe_server_walker_create(lufqhe_server_t *s, int n, int k, con
     set_error("lufqhe_server_walker_create: no class for n=%d", n);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
-  const size_t bytes = (size_t)k * n * n * sizeof(double2) + (size_t)k * n * sizeof(double2);
+  const WalkerLayout lay(n, k, s->moves != 0);
+  const size_t bytes = lay.total;
   size_t off = 0;
   if (pool_alloc(s, bytes, &off) != LUFQHE_SUCCESS) {
     set_error("lufqhe_server_walker_create: HBM budget exhausted (%zu bytes needed)", bytes);
@@ -744,8 +961,7 @@ extern "C" int lufqhe_server_walker_create(lufqhe_server_t *s, int n, int k, con
   W.bytes = bytes;
   W.busy = false;
   W.built = false;
-  double2 *mats = reinterpret_cast<double2 *>(s->pool + off);
-  double2 *z = mats + (size_t)k * n * n;
+  double2 *z = reinterpret_cast<double2 *>(s->pool + off + lay.z);
   // only the coordinates cross now (copy engine); the matrices are built by
   // the class loop when the walker's first request runs
   cudaStream_t st = s->setup;
@@ -829,11 +1045,20 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
   R.first_tile = C.published;
   R.last_tile = C.published + ntiles;
   __atomic_store_n(&s->comp_h[slot], 0u, __ATOMIC_RELAXED);
-  double2 *mats = reinterpret_cast<double2 *>(s->pool + W.offset);
-  double2 *z = mats + (size_t)W.k * W.n * W.n;
+  const WalkerLayout lay(W.n, W.k, s->moves != 0);
+  unsigned char *blk = s->pool + W.offset;
+  double2 *mats = reinterpret_cast<double2 *>(blk + lay.mats);
+  double2 *z = reinterpret_cast<double2 *>(blk + lay.z);
   for (unsigned int t = 0; t < ntiles; ++t) {
     const int first = (int)t * s->tile;
     ServeTile T;
+    T.moves = s->moves;
+    T.lu = reinterpret_cast<double2 *>(blk + lay.lu) + (size_t)first * W.n * W.n;
+    T.perm = reinterpret_cast<int *>(blk + lay.perm) + (size_t)first * W.n;
+    T.w = reinterpret_cast<double2 *>(blk + lay.w) + (size_t)first * kMoveK * W.n;
+    T.v = reinterpret_cast<double2 *>(blk + lay.v) + (size_t)first * kMoveK * W.n;
+    T.cap = reinterpret_cast<double2 *>(blk + lay.cap) + (size_t)first * kMoveK * kMoveK;
+    T.mst = reinterpret_cast<MoveState *>(blk + lay.mst) + first;
     T.mats = mats + (size_t)first * W.n * W.n;
     T.z = z + (size_t)first * W.n;
     T.znew = particle >= 0 ? s->znew_d + sbase + first : nullptr;
@@ -847,7 +1072,6 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
     T.count = std::min(s->tile, W.k - first);
     T.particle = particle;
     T.build = W.built ? 0 : 1;
-    T.pad = 0;
     s->classes[W.cls].ring_h[(C.published + t) % kRing] = T;
   }
   std::atomic_thread_fence(std::memory_order_seq_cst);

@@ -273,14 +273,22 @@ class Server:
     """Device-resident walkers and the persistent request loop (lufqhe_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int, mode: int = MODE_MIXED, classes=(8, 16, 32, 64),
-                 class_sms=None, max_k: int = 4096, tile: int = 8):
+                 class_sms=None, max_k: int = 4096, tile: int = 8, moves: bool | None = None):
+        """moves: O(n^2) determinant-ratio moves against kept FP64 factors
+        (LUFQHE_OPT_SERVE_MOVES, read at creation); None keeps the option's value."""
         import ctypes
         self._h = None
         cn = (ctypes.c_int * len(classes))(*classes)
         cs = (ctypes.c_int * len(classes))(*class_sms) if class_sms else None
         h = ctypes.c_void_p()
-        rc = lib().lufqhe_server_create(ctypes.byref(h), int(hbm_budget_bytes), mode, cn, cs,
-                                        len(classes), max_k, tile)
+        old = lib().lufqhe_get_option(8)
+        if moves is not None:
+            lib().lufqhe_set_option(8, 1.0 if moves else 0.0)
+        try:
+            rc = lib().lufqhe_server_create(ctypes.byref(h), int(hbm_budget_bytes), mode, cn, cs,
+                                            len(classes), max_k, tile)
+        finally:
+            lib().lufqhe_set_option(8, old)
         _native.check(rc, "lufqhe_server_create")
         self._h = h
         self.max_k = max_k

@@ -73,9 +73,10 @@ def test_alone_and_in_mix_give_the_same_bits(server):
 
 
 def test_hbm_admission(lufqhe_mod, cuda):
+    """Without moves a walker holds its matrices and coordinates only."""
     n, k = 16, 256
     per_walker = k * n * n * 16 + k * n * 16
-    srv = lufqhe_mod.Server(3 * per_walker + 4096, classes=(16,), max_k=256)
+    srv = lufqhe_mod.Server(3 * per_walker + 4096, classes=(16,), max_k=256, moves=False)
     rng = np.random.default_rng(3)
     ws = [srv.walker(zdraw(rng, k, n)) for _ in range(3)]
     assert all(w is not None for w in ws)
@@ -133,10 +134,10 @@ def test_large_class_follows_precision_policy(lufqhe_mod, cuda, oracle):
 def test_large_class_matches_batched_fp64_bits(lufqhe_mod, cuda, mode):
     """The n = 64 class factorises each matrix with a warp group (one named
     barrier per group, several groups per CTA): results equal the batched FP64
-    fused kernel's on the same matrices bit for bit, before and after a move,
-    with many tiles in flight at once."""
+    fused kernel's on the same matrices bit for bit, before and after a move
+    (every move refactorising), with many tiles in flight at once."""
     import torch
-    srv = lufqhe_mod.Server(1 << 30, mode=mode, classes=(64,), max_k=512, tile=8)
+    srv = lufqhe_mod.Server(1 << 30, mode=mode, classes=(64,), max_k=512, tile=8, moves=False)
     try:
         rng = np.random.default_rng(8)
         z = zdraw(rng, 300, 64)
@@ -156,3 +157,75 @@ def test_large_class_matches_batched_fp64_bits(lufqhe_mod, cuda, mode):
         srv.destroy_walker(w)
     finally:
         srv.close()
+
+
+@pytest.mark.parametrize("n,tol", [(8, 1e-10), (16, 1e-10), (32, None), (64, None)])
+def test_moves_against_double_double(lufqhe_mod, cuda, oracle, n, tol):
+    """O(n^2) moves (kept FP64 factors, determinant lemma, Woodbury over the
+    moves since the last factorisation, checked before use): after 10 and 100
+    single-particle moves every walker matrix's log-determinant against the
+    double-double oracle. n = 8, 16: within 1e-10. n = 32, 64, where FP64 LU
+    itself misses 1e-10 on a tail of these orbital matrices: no worse than a
+    fresh FP64 factorisation of the same matrices, by more than a factor 10,
+    above 1e-10."""
+    import json
+    import torch
+    k = 128
+    srv = lufqhe_mod.Server(4 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(n,), max_k=k,
+                            moves=True)
+    rec = {}
+    try:
+        rng = np.random.default_rng(600 + n)
+        z = zdraw(rng, k, n)
+        w = srv.walker(z)
+        la, ph, st = srv.result(srv.submit(w, -1), k)
+        for move in range(1, 101):
+            p = int(rng.integers(n))
+            znew = zdraw(rng, k, 1)[:, 0]
+            la, ph, st = srv.result(srv.submit(w, p, znew), k)
+            z[:, p] = znew
+            if move in (10, 100):
+                want, wph, _ = oracle.logdet_dd(lll_host(z))
+                scale = np.maximum(1, np.abs(want))
+                err = np.maximum(np.abs(la - want),
+                                 np.abs(np.angle(np.exp(1j * (ph - wph))))) / scale
+                fresh = lufqhe_mod.lll_det(torch.from_numpy(z).cuda(),
+                                           mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED)
+                fl = fresh.logabs.cpu().numpy()
+                fp = fresh.phase.cpu().numpy()
+                ferr = np.maximum(np.abs(fl - want),
+                                  np.abs(np.angle(np.exp(1j * (fp - wph))))) / scale
+                rec[move] = {"max": float(err.max()), "median": float(np.median(err)),
+                             "above_1e-10": int((err > 1e-10).sum()),
+                             "fresh_fp64_max": float(ferr.max()),
+                             "fresh_fp64_above_1e-10": int((ferr > 1e-10).sum())}
+                assert (st == lufqhe_mod.ST_FP64).all()
+                if tol is not None:
+                    assert err.max() < tol, rec
+                else:
+                    assert (err <= np.maximum(1e-10, 10 * ferr)).all(), rec
+        srv.destroy_walker(w)
+    finally:
+        srv.close()
+    print("moves accuracy", n, json.dumps(rec))
+
+
+def test_moves_bits_after_build_match_batched(lufqhe_mod, cuda):
+    """A walker's first request (with moves on) is an FP64 factorisation whose
+    results equal the batched FP64 kernel's bit for bit (the factors it keeps
+    are that factorisation's)."""
+    import torch
+    for n in (16, 64):
+        srv = lufqhe_mod.Server(1 << 30, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED, classes=(n,),
+                                max_k=256, moves=True)
+        try:
+            z = zdraw(np.random.default_rng(700 + n), 200, n)
+            w = srv.walker(z)
+            la, ph, st = srv.result(srv.submit(w, -1), 200)
+            ref = lufqhe_mod.lll_det(torch.from_numpy(z).cuda(),
+                                     mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED)
+            assert np.array_equal(la, ref.logabs.cpu().numpy())
+            assert np.array_equal(ph, ref.phase.cpu().numpy())
+            srv.destroy_walker(w)
+        finally:
+            srv.close()
