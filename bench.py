@@ -779,12 +779,17 @@ def run_serve(args, world, rank, local, full=True):
         sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
         srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES,
                             class_sms=list(map(int, sms)), max_k=4096, tile=8, moves=moves)
-        # capacity: a stream far faster than the server can take
-        lat, ns, el, mats = srv.run_stream(rate_hz=1e6, nrequests=max(400, nreq // 2), moves=100,
-                                           k_min=1, k_max=4096, seed=seed + 1)
+        # capacity: a closed loop of walkers, each moving again as soon as its
+        # last move completes (the open stream's work mix: 100 moves, then a
+        # new walker whose first request builds its matrices)
+        done, el, mats = srv.run_closed(walkers=args.serve_walkers, nrequests=max(1000, nreq),
+                                        moves=100, k_min=1, k_max=4096, seed=seed + 1)
         capacity = mats / el
-        runs = {"saturated": summary(lat, ns, el, mats, 1e6, capacity)}
-        for tag, rate, nr in (("at_70pct_capacity", 0.7 * capacity / mean_k, nreq),
+        moved, refac = srv.stats()
+        runs = {"closed_loop_capacity": {"walkers": args.serve_walkers, "requests": done,
+                                         "seconds": el, "dets_per_s": capacity,
+                                         "requests_per_s": done / el}}
+        for tag, rate, nr in (("at_70pct_capacity", 0.7 * done / el, nreq),
                               ("at_20k_req_s", 20000.0, max(200, nreq // 4))):
             lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100, k_min=1,
                                                k_max=4096, seed=seed)
@@ -793,7 +798,8 @@ def run_serve(args, world, rank, local, full=True):
         result[label] = {"capacity_dets_per_s": capacity,
                          "batched_offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
                          "batched_offline_mix_dets_per_s": batched_mix,
-                         "class_sms": list(map(int, sms)), "runs": runs}
+                         "class_sms": list(map(int, sms)), "runs": runs,
+                         "moves_o_n2": moved, "moves_refactorised": refac}
     if rank != 0:
         return None
     r70 = result["moves"]["runs"]["at_70pct_capacity"]
@@ -899,6 +905,8 @@ def main():
     # 16 cores at n = 24): short steps let OpenMP start-up and box noise skew it
     ap.add_argument("--ref-sample", type=int, default=32768)
     ap.add_argument("--serve-requests", type=int, default=4000)
+    ap.add_argument("--serve-walkers", type=int, default=128,
+                    help="live walkers of the closed loop that measures a server's capacity")
     ap.add_argument("--no-subconfigs", action="store_true",
                     help="default workload only: leave out the compact config 1/2/4/5 results")
     args = ap.parse_args()

@@ -316,6 +316,21 @@ long long lufqhe_server_run_stream(lufqhe_server_t *server, double rate_hz, long
                                    int moves, int k_min, int k_max, unsigned long long seed,
                                    double *lat_us, int *rec_n, long long max_records,
                                    double *elapsed_s, long long *matrices);
+/* Closed loop: `walkers` live walkers (k log-uniform in [k_min, k_max], n
+ * uniform over the classes) each submit their next move when the previous one
+ * completes; a walker retires after `moves` moves and a new one (whose first
+ * request builds its matrices) takes its place. The first builds are made
+ * before the clock starts. Returns the requests completed; *elapsed_s the
+ * wall time, *matrices the determinants: the server's capacity for the open
+ * stream's work mix. */
+long long lufqhe_server_run_closed(lufqhe_server_t *server, int walkers, long long nrequests,
+                                   int moves, int k_min, int k_max, unsigned long long seed,
+                                   double *elapsed_s, long long *matrices);
+/* Since the server was created, for its class of size class_n (0: all
+ * classes): matrix moves taken by the O(n^2) path, and matrix moves that
+ * refactorised instead (a failed check, or a full history). Synchronous. */
+int lufqhe_server_stats(lufqhe_server_t *server, int class_n, long long *moved,
+                        long long *refactored);
 
 /* ---- on-device synthetic inputs (seeded; identical on every device) ---- */
 /* i.i.d. complex Gaussian entries, Re and Im ~ N(0, sigma^2/2). */

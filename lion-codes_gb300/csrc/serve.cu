@@ -82,6 +82,10 @@ struct ClassCtl {                // device memory, one per class
   unsigned int claimed;          // tiles claimed so far (never above published)
   unsigned int exited;           // warps that left the loop
   unsigned long long last_ns;    // %globaltimer of the class's latest claim
+  unsigned int pub_seen;         // device mirror of the host's published count
+  unsigned int pad;
+  unsigned long long moved;      // moves taken by the O(n^2) path
+  unsigned long long refactored; // moves that refactorised instead
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -97,6 +101,59 @@ __device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
 }
 __device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) {
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Claim the next published tile of a class (one thread): a compare-and-swap
+// on the claim counter while it is below the published count. Returns false
+// when the class has had no claim for kIdleNs or the server is stopping.
+// The host's published count lives in mapped host memory, and every read of
+// it crosses the host link: thousands of idle warps reading it in a loop had
+// saturated that link and slowed every tile's own host-memory traffic. So
+// the count is mirrored in device memory (ctl->pub_seen): a claim looks at the
+// mirror first, and only when the mirror shows nothing to claim does the
+// thread read the host count (acquire) and raise the mirror (after a fence, so
+// a tile claimed through the mirror is ordered after the host's writes of it).
+// Idle threads back off exponentially between host reads, up to ~8 us.
+__device__ bool claim_tile(const unsigned int *published, const unsigned int *stop, ClassCtl *ctl,
+                           unsigned int &idx) {
+  const unsigned long long t0 = global_ns();
+  volatile unsigned int *claimed = &ctl->claimed;
+  unsigned int backoff = 128;
+  for (;;) {
+    const unsigned int c = *claimed;
+    const unsigned int p = ld_acquire_gpu(&ctl->pub_seen);
+    if ((int)(p - c) > 0) {
+      if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
+        idx = c;
+        atomicMax(&ctl->last_ns, global_ns());
+        return true;
+      }
+      continue;
+    }
+    const unsigned int ph = ld_acquire_sys(published);
+    if ((int)(ph - p) > 0) {
+      __threadfence();
+      unsigned int old = p;
+      while ((int)(ph - old) > 0) {  // raise the mirror (wrap-safe)
+        const unsigned int prev = atomicCAS(&ctl->pub_seen, old, ph);
+        if (prev == old) break;
+        old = prev;
+      }
+      backoff = 128;
+      continue;
+    }
+    if (ld_acquire_sys(stop)) return false;
+    const unsigned long long now = global_ns();
+    const unsigned long long last = *(volatile unsigned long long *)&ctl->last_ns;
+    if (now - (last > t0 ? last : t0) > kIdleNs) return false;
+    __nanosleep(backoff);
+    backoff = backoff < 8192u ? 2u * backoff : 8192u;
+  }
 }
 
 
@@ -232,33 +289,7 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
     // claim the next published tile; give up when the class has been idle
     unsigned int idx = 0;
     int give_up = 0;
-    if (lane == 0) {
-      const unsigned long long t0 = global_ns();
-      volatile unsigned int *claimed = &ctl->claimed;
-      for (;;) {
-        const unsigned int c = *claimed;
-        const unsigned int p = ld_acquire_sys(published);
-        if ((int)(p - c) > 0) {
-          if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
-            idx = c;
-            break;
-          }
-          continue;
-        }
-        if (ld_acquire_sys(stop)) {
-          give_up = 1;
-          break;
-        }
-        const unsigned long long now = global_ns();
-        const unsigned long long last = *(volatile unsigned long long *)&ctl->last_ns;
-        if (now - (last > t0 ? last : t0) > kIdleNs) {
-          give_up = 1;
-          break;
-        }
-        __nanosleep(256);
-      }
-      if (!give_up) atomicMax(&ctl->last_ns, global_ns());
-    }
+    if (lane == 0) give_up = claim_tile(published, stop, ctl, idx) ? 0 : 1;
     idx = __shfl_sync(kFull, idx, 0);
     give_up = __shfl_sync(kFull, give_up, 0);
     if (give_up) {
@@ -293,10 +324,11 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
           move_new_row(t, NC, j, S.r, lane);
           done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
           __syncwarp();
+          if (lane == 0) atomicAdd(done ? &ctl->moved : &ctl->refactored, 1ull);
         }
         int st = 0;
         if (!done) {
-          if (load_matrix_fp64<true>(src, NC, NC, M, LDS, lane)) {
+          if (stage_matrix_checked(M, LDS, src, NC, lane)) {
             st = LUFQHE_ST_NONFINITE;
             la = ph = NAN;
             if (lane == 0) a.st->la = NAN;  // refactorised again by the next move
@@ -374,32 +406,6 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
   }
 }
 
-// Claim the next published tile of a class (one thread): a compare-and-swap
-// on the claim counter while it is below the published count. Returns false
-// when the class has had no claim for kIdleNs or the server is stopping.
-__device__ bool claim_tile(const unsigned int *published, const unsigned int *stop, ClassCtl *ctl,
-                           unsigned int &idx) {
-  const unsigned long long t0 = global_ns();
-  volatile unsigned int *claimed = &ctl->claimed;
-  for (;;) {
-    const unsigned int c = *claimed;
-    const unsigned int p = ld_acquire_sys(published);
-    if ((int)(p - c) > 0) {
-      if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
-        idx = c;
-        atomicMax(&ctl->last_ns, global_ns());
-        return true;
-      }
-      continue;
-    }
-    if (ld_acquire_sys(stop)) return false;
-    const unsigned long long now = global_ns();
-    const unsigned long long last = *(volatile unsigned long long *)&ctl->last_ns;
-    if (now - (last > t0 ? last : t0) > kIdleNs) return false;
-    __nanosleep(256);
-  }
-}
-
 // FP64-only classes with n >= kFp64GroupMinN: the CTA's warps work in groups
 // of kFp64GroupWarps. Each group claims tiles like a warp of serve_kernel and
 // factorises their matrices one at a time with all its threads
@@ -470,17 +476,21 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
       bar.sync();  // the move's rows are written; M is free again
       const double2 *src = t.mats + (size_t)j * NC * NC;
       if (t.moves) {
-        // warp 0 tries the O(n^2) move; if it is refused (or this is a
-        // walker's first request or a recompute) the group refactorises in
-        // FP64 and keeps the factors
+        // one warp of the group tries the O(n^2) move; if it is refused (or
+        // this is a walker's first request or a recompute) the group
+        // refactorises in FP64 and keeps the factors. Group g moves with its
+        // warp g mod 4, so the groups of a CTA move on different SM
+        // sub-partitions (warp w runs on sub-partition w mod 4) and their FP64
+        // work does not queue on one FP64 unit.
         const MoveArrays a = move_arrays(t, NC, j);
         const int flag = mode == LUFQHE_MODE_MIXED ? LUFQHE_ST_FP64 : 0;
-        if (tid < 32) {
+        if ((tid >> 5) == g % kFp64GroupWarps) {
           double la = 0.0, ph = 0.0;
           bool done = false;
           if (!t.build && t.particle >= 0) {
             move_new_row(t, NC, j, S.r, lane);
             done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
+            if (lane == 0) atomicAdd(done ? &ctl->moved : &ctl->refactored, 1ull);
           }
           if (done && lane == 0) serve_emit(t, j, la, ph, flag);
           if (lane == 0) moved_s[g] = done;
@@ -676,6 +686,7 @@ struct SClass {
   bool running = false;
   unsigned int relaunches = 0;
   unsigned int share64k = 0;       // FP64 routing share, fixed at creation
+  double last_query = 0.0;         // when the loop was last seen running (host clock)
 };
 
 }  // namespace
@@ -752,8 +763,18 @@ int class_index(lufqhe_server_s *s, int n) {
 }
 
 // (Re)launch a class kernel if it is not running.
+// A running loop exits only after kIdleNs without a claim, so while it has
+// been seen running within the last kQueryGapS its stream is not queried again
+// (a driver call per submit and poll had capped a server at a few thousand
+// requests per second); a tile published in the race with an exit waits at
+// most that long for the relaunch.
+constexpr double kQueryGapS = 1e-3;
+
 int ensure_running(lufqhe_server_s *s, SClass &c) {
   if (c.running) {
+    const double t = now_s();
+    if (t - c.last_query < kQueryGapS) return LUFQHE_SUCCESS;
+    c.last_query = t;
     cudaError_t q = cudaStreamQuery(c.stream);
     if (q == cudaErrorNotReady) return LUFQHE_SUCCESS;
     c.running = false;
@@ -768,6 +789,7 @@ int ensure_running(lufqhe_server_s *s, SClass &c) {
   int rc = check_cuda(cudaGetLastError(), "serve kernel launch");
   if (rc) return rc;
   c.running = true;
+  c.last_query = now_s();
   ++c.relaunches;
   return LUFQHE_SUCCESS;
 }
@@ -1129,6 +1151,27 @@ extern "C" int lufqhe_server_destroy(lufqhe_server_t *s) {
   return LUFQHE_SUCCESS;
 }
 
+extern "C" int lufqhe_server_stats(lufqhe_server_t *s, int class_n, long long *moved,
+                                   long long *refactored) {
+  if (!s || !moved || !refactored) {
+    set_error("lufqhe_server_stats: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  *moved = *refactored = 0;
+  for (SClass &c : s->classes) {
+    if (class_n > 0 && c.n != class_n) continue;
+    ClassCtl ctl{};
+    // a plain copy: the class loop keeps running on its own (non-blocking) stream
+    const int rc = check_cuda(cudaMemcpy(&ctl, c.ctl, sizeof(ctl), cudaMemcpyDeviceToHost),
+                              "server stats");
+    if (rc) return rc;
+    *moved += (long long)ctl.moved;
+    *refactored += (long long)ctl.refactored;
+  }
+  return LUFQHE_SUCCESS;
+}
+
 // Simulated Monte Carlo walker stream (Poisson arrivals of move requests).
 // Walkers: k log-uniform in [k_min, k_max], n uniform over the server's
 // classes; each makes `moves` single-particle moves; a request arrives at the
@@ -1278,4 +1321,117 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
   for (auto &A : act) lufqhe_server_walker_destroy(s, A.id);
   release_tables();
   return std::min(recorded, max_records);
+}
+
+// Closed-loop walker population: `walkers` walkers (k log-uniform in
+// [k_min, k_max], n uniform over the classes) each submit their next move as
+// soon as the previous one completes; a walker that has made `moves` moves is
+// retired and replaced by a new one, whose first request builds and factorises
+// its matrices. The first `walkers` requests (the initial builds) are made
+// before the clock starts. Returns the requests completed in the timed part;
+// *elapsed_s the wall time and *matrices the determinants. This is the
+// server's capacity for the same work mix as the open stream.
+extern "C" long long lufqhe_server_run_closed(lufqhe_server_t *s, int walkers, long long nrequests,
+                                              int moves, int k_min, int k_max,
+                                              unsigned long long seed, double *elapsed_s,
+                                              long long *matrices) {
+  if (!s || walkers < 1 || nrequests < 1 || moves < 1 || k_min < 1 || k_max < k_min ||
+      k_max > s->max_k) {
+    set_error("lufqhe_server_run_closed: invalid argument");
+    return LUFQHE_ERR_INVALID_ARG;
+  }
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  std::normal_distribution<double> gauss(0.0, 1.0);
+  const int nclass = (int)s->classes.size();
+  std::vector<double> zbuf;
+  auto fill = [&](int n, size_t count) -> const double * {
+    zbuf.resize(count);
+    const double sig = std::sqrt((double)n / 2.0);
+    for (size_t i = 0; i < count; ++i) zbuf[i] = gauss(rng) * sig;
+    return zbuf.data();
+  };
+  struct W {
+    int id = -1, n = 0, k = 0, left = 0;
+    long long ticket = 0;
+  };
+  std::vector<W> pop(walkers);
+  // a new walker (LUFQHE_ERR_BUSY while the HBM budget is spent: tried again
+  // on a later sweep, after others have retired)
+  auto spawn = [&](W &w) -> int {
+    w.n = s->classes[(int)(uni(rng) * nclass) % nclass].n;
+    const double lk = std::log((double)k_min) +
+                      uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
+    w.k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
+    w.left = moves;
+    w.id = -1;
+    const int rc =
+        lufqhe_server_walker_create(s, w.n, w.k, fill(w.n, (size_t)2 * w.k * w.n), &w.id);
+    if (rc) w.id = -1;
+    return rc;
+  };
+  auto submit = [&](W &w, bool build) -> int {
+    for (;;) {  // a full ring or slot table frees as requests complete
+      const int particle = build ? -1 : (int)(uni(rng) * w.n) % w.n;
+      const int rc = lufqhe_server_submit(s, w.id, particle,
+                                          build ? nullptr : fill(w.n, (size_t)2 * w.k), &w.ticket);
+      if (rc != LUFQHE_ERR_BUSY) return rc;
+      std::this_thread::yield();
+    }
+  };
+  // the initial builds, untimed (as many walkers as the budget admits)
+  int started = 0;
+  for (W &w : pop) {
+    int rc = spawn(w);
+    if (rc == LUFQHE_ERR_BUSY) break;
+    if (!rc) rc = submit(w, true);
+    if (rc) return rc;
+    ++started;
+  }
+  if (started == 0) {
+    set_error("lufqhe_server_run_closed: the HBM budget admits no walker");
+    return LUFQHE_ERR_BUSY;
+  }
+  for (W &w : pop) {
+    if (w.id < 0) continue;
+    int rc = lufqhe_server_poll(s, w.ticket, 60000000, nullptr, nullptr, nullptr);
+    if (!rc) rc = submit(w, false);
+    if (rc) return rc;
+  }
+  long long done = 0, mats = 0, issued = started;
+  const double start = now_s();
+  for (;;) {
+    bool live = false;
+    for (W &w : pop) {
+      int rc = LUFQHE_SUCCESS;
+      if (w.id < 0) {
+        if (issued >= nrequests) continue;
+        live = true;
+        rc = spawn(w);
+        if (rc == LUFQHE_ERR_BUSY) continue;
+        if (!rc) rc = submit(w, true);  // a new walker's build is part of the mix
+        if (rc) return rc;
+        ++issued;
+        continue;
+      }
+      live = true;
+      rc = lufqhe_server_poll(s, w.ticket, 0, nullptr, nullptr, nullptr);
+      if (rc == LUFQHE_ERR_BUSY) continue;
+      if (rc) return rc;
+      ++done;
+      mats += w.k;
+      if (--w.left == 0 || issued >= nrequests) {
+        rc = lufqhe_server_walker_destroy(s, w.id);
+        w.id = -1;
+      } else {
+        rc = submit(w, false);
+        ++issued;
+      }
+      if (rc) return rc;
+    }
+    if (!live) break;
+  }
+  if (elapsed_s) *elapsed_s = now_s() - start;
+  if (matrices) *matrices = mats;
+  return done;
 }

@@ -21,6 +21,13 @@
 // history full (m = K), refactorises A' in FP64 instead and restarts from it.
 // The work per accepted move is O(n^2 + n K + K^3), against O(n^3) for a new
 // factorisation.
+//
+// A move is a chain of short dependent steps on one warp, so the code keeps
+// that chain short: the matrices are staged into shared memory by
+// asynchronous copies issued all at once, the diagonal reciprocals of U are
+// taken lane-parallel before the back substitution, the residual is formed
+// one row per lane from shared memory (no reductions), and the m dot products
+// against the history are reduced side by side.
 #pragma once
 
 #include "lup_fp64.cuh"
@@ -56,13 +63,19 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 csubmul(double2 s, double2 a, double2 b) {  // s - a b
   return cmsub<ARITH_FUSED>(s, a, b);
 }
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-  const double d = __fma_rn(b.x, b.x, __dmul_rn(b.y, b.y));
-  return make_double2(__ddiv_rn(__fma_rn(a.x, b.x, __dmul_rn(a.y, b.y)), d),
-                      __ddiv_rn(__fma_rn(a.y, b.x, -__dmul_rn(a.x, b.y)), d));
-}
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+// 1 / b to within a few ulps (one reciprocal), for the solves, whose result is
+// checked by its residual
+__device__ __forceinline__ double2 crcp(double2 b) {
+  const double r = __drcp_rn(__fma_rn(b.x, b.x, __dmul_rn(b.y, b.y)));
+  return make_double2(__dmul_rn(b.x, r), -__dmul_rn(b.y, r));
+}
 
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, off));
+  return v;
+}
 __device__ __forceinline__ double2 warp_sum2(double2 v) {
 #pragma unroll
   for (int off = 16; off; off >>= 1) {
@@ -71,21 +84,69 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   }
   return v;
 }
-__device__ __forceinline__ double warp_max(double v) {
-#pragma unroll
-  for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, off));
-  return v;
+
+// An n x n complex128 matrix (row-major, contiguous) from global memory into
+// shared memory (row stride lds) by asynchronous 16-byte copies: every lane
+// issues all of its copies before waiting once, so the loads overlap instead
+// of one round trip each.
+__device__ __forceinline__ void stage_matrix_async(double2 *dst, int lds, const double2 *src, int n,
+                                                   int lane) {
+  BlockWalk w(lane, n);
+  for (int e = lane; e < n * n; e += 32) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + w.i * lds + w.k);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src + e) : "memory");
+    w.next(n);
+  }
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+  __syncwarp();
 }
 
-// sum_p a[p] b[p] over n entries (a in global or shared, b in shared), all lanes
-__device__ __forceinline__ double2 warp_dot(const double2 *a, const double2 *b, int n, int lane) {
-  double2 s = make_double2(0.0, 0.0);
-  for (int p = lane; p < n; p += 32) {
-    const double2 t = cmul(__ldcg(a + p), b[p]);
-    s.x += t.x;
-    s.y += t.y;
+// The same staging followed by a scan for NaN/Inf entries (warp-uniform
+// result: true if there is one).
+__device__ __forceinline__ bool stage_matrix_checked(double2 *dst, int lds, const double2 *src,
+                                                     int n, int lane) {
+  stage_matrix_async(dst, lds, src, n, lane);
+  bool bad = false;
+  BlockWalk w(lane, n);
+  for (int e = lane; e < n * n; e += 32) {
+    bad |= !finite_c(dst[w.i * lds + w.k]);
+    w.next(n);
   }
-  return warp_sum2(s);
+  return __any_sync(kFull, bad);
+}
+
+// out[s] = sum_p X[s n + p] b[p] for s < m (m <= K; X in global memory, b in
+// shared memory): each lane accumulates all m partial sums, then the m warp
+// reductions run side by side. out is shared memory, written by lane 0.
+template <int K>
+__device__ __forceinline__ void warp_dots(const double2 *X, const double2 *b, int n, int m,
+                                          int lane, double2 *out) {
+  double2 acc[K];
+#pragma unroll
+  for (int s = 0; s < K; ++s) acc[s] = make_double2(0.0, 0.0);
+  for (int p = lane; p < n; p += 32) {
+    const double2 bp = b[p];
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if (s < m) {
+        const double2 t = cmul(__ldcg(X + (size_t)s * n + p), bp);
+        acc[s].x += t.x;
+        acc[s].y += t.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1)
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      acc[s].x += __shfl_xor_sync(kFull, acc[s].x, off);
+      acc[s].y += __shfl_xor_sync(kFull, acc[s].y, off);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int s = 0; s < K; ++s)
+      if (s < m) out[s] = acc[s];
+  __syncwarp();
 }
 
 // Shared-memory scratch of one move, after the n x lds factor area.
@@ -108,10 +169,10 @@ struct MoveScratch {
 };
 
 // Try the move of row i to the new row r' (in S.r) for one matrix, one warp.
-// Ls (row stride lds) receives the factors. True (warp-uniform) if the move
-// was accepted: the state, W, V, C and row i of A are updated and (*la, *ph)
-// is the new log-determinant. False: only row i of A has been rewritten; the
-// caller refactorises A.
+// Ls (row stride lds) receives the factors, then the current matrix. True
+// (warp-uniform) if the move was accepted: the state, W, V, C and row i of A
+// are updated and (*la, *ph) is the new log-determinant. False: only row i of
+// A has been rewritten; the caller refactorises A.
 template <int K>
 __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int lds,
                           const MoveScratch &S, int lane, double *la_out, double *ph_out) {
@@ -119,15 +180,8 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
   const int m = st.m;
   bool ok = m < K && st.la == st.la;
   // 1. the factors of A0 into shared memory (rows in pivoted order)
-  {
-    BlockWalk w(lane, n);
-    for (int e = lane; e < n * n; e += 32) {
-      Ls[w.i * lds + w.k] = __ldcg(a.LU + e);
-      w.next(n);
-    }
-    for (int p = lane; p < n; p += 32) S.perm[p] = __ldcg(a.perm + p);
-  }
-  __syncwarp();
+  for (int p = lane; p < n; p += 32) S.perm[p] = __ldcg(a.perm + p);
+  stage_matrix_async(Ls, lds, a.LU, n, lane);
   // q: the pivoted position of row i
   int q = n;
   for (int p = lane; p < n; p += 32)
@@ -136,8 +190,13 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
   for (int off = 16; off; off >>= 1) q = min(q, __shfl_xor_sync(kFull, q, off));
   ok = ok && q < n;
   if (ok) {
-    // 2. c = U^-1 L^-1 e_q: forward from q (unit lower), then backward
-    for (int p = lane; p < n; p += 32) S.c[p] = make_double2(p == q ? 1.0 : 0.0, 0.0);
+    // 2. c = U^-1 L^-1 e_q: forward from q (unit lower), then backward; the
+    //    reciprocals of U's diagonal first, lane-parallel, into S.x (free
+    //    until step 3), so each backward step is a multiply
+    for (int p = lane; p < n; p += 32) {
+      S.c[p] = make_double2(p == q ? 1.0 : 0.0, 0.0);
+      S.x[p] = crcp(Ls[p * lds + p]);
+    }
     __syncwarp();
     for (int j = q; j + 1 < n; ++j) {
       const double2 yj = S.c[j];
@@ -145,21 +204,19 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
       __syncwarp();
     }
     for (int j = n - 1; j >= 0; --j) {
-      const double2 cj = cdiv(S.c[j], Ls[j * lds + j]);
+      const double2 cj = cmul(S.c[j], S.x[j]);
       __syncwarp();
       if (lane == 0) S.c[j] = cj;
       for (int p = lane; p < j; p += 32) S.c[p] = csubmul(S.c[p], Ls[p * lds + j], cj);
       __syncwarp();
     }
-    // 3. x = c - W C^-1 V^T c
-    for (int s = 0; s < m; ++s) {
-      const double2 v = warp_dot(a.V + (size_t)s * n, S.c, n, lane);
-      if (lane == 0) S.rhs[s] = v;
-    }
+    // 3. x = c - W C^-1 V^T c (the m dot products reduced together)
+    warp_dots<K>(a.V, S.c, n, m, lane, S.rhs);
     for (int e = lane; e < m * m; e += 32) S.Cs[e] = __ldcg(a.C + (e / m) * K + (e % m));
     __syncwarp();
     if (lane == 0 && m > 0) {
-      // C z = V^T c by Gaussian elimination with partial pivoting (m <= K)
+      // C z = V^T c by Gaussian elimination with partial pivoting (m <= K);
+      // each pivot is kept as its reciprocal
       double2 *Cm = S.Cs;
       double2 *z = S.rhs;
       for (int j = 0; j < m; ++j) {
@@ -176,8 +233,10 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
           z[p] = z[j];
           z[j] = t;
         }
+        const double2 rj = crcp(Cm[j * m + j]);
+        Cm[j * m + j] = rj;
         for (int r = j + 1; r < m; ++r) {
-          const double2 l = cdiv(Cm[r * m + j], Cm[j * m + j]);
+          const double2 l = cmul(Cm[r * m + j], rj);
           for (int k = j + 1; k < m; ++k) Cm[r * m + k] = csubmul(Cm[r * m + k], l, Cm[j * m + k]);
           z[r] = csubmul(z[r], l, z[j]);
         }
@@ -185,7 +244,7 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
       for (int j = m - 1; j >= 0; --j) {
         double2 t = z[j];
         for (int k = j + 1; k < m; ++k) t = csubmul(t, Cm[j * m + k], z[k]);
-        z[j] = cdiv(t, Cm[j * m + j]);
+        z[j] = cmul(t, Cm[j * m + j]);
       }
     }
     __syncwarp();
@@ -194,34 +253,35 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
       for (int s = 0; s < m; ++s) t = csubmul(t, __ldcg(a.W + (size_t)s * n + p), S.rhs[s]);
       S.x[p] = t;
     }
-    __syncwarp();
     // 4. a-posteriori check of x against the current matrix: the residual
-    //    A x - e_i, relative to ||A||_inf ||x||_inf
+    //    A x - e_i, relative to ||A||_inf ||x||_inf. The factors are done
+    //    with: A takes their place in shared memory, and each lane forms whole
+    //    rows (no reductions).
+    __syncwarp();
+    stage_matrix_async(Ls, lds, a.A, n, lane);
     double res = 0.0, anorm = 0.0, xnorm = 0.0;
-    for (int p = lane; p < n; p += 32) xnorm = fmax(xnorm, cabs1(S.x[p]));
-    for (int row = 0; row < n; ++row) {
-      double2 s = make_double2(0.0, 0.0);
+    for (int p = lane; p < n; p += 32) {
+      xnorm = fmax(xnorm, cabs1(S.x[p]));
+      double2 s = make_double2(p == i ? -1.0 : 0.0, 0.0);
       double rs = 0.0;
-      for (int k = lane; k < n; k += 32) {
-        const double2 v = __ldcg(a.A + (size_t)row * n + k);
+      for (int k = 0; k < n; ++k) {
+        const double2 v = Ls[p * lds + k];
         const double2 t = cmul(v, S.x[k]);
         s.x += t.x;
         s.y += t.y;
         rs += cabs1(v);
       }
-      s = warp_sum2(s);
-#pragma unroll
-      for (int off = 16; off; off >>= 1) rs += __shfl_xor_sync(kFull, rs, off);
-      if (row == i) s.x -= 1.0;
       res = fmax(res, cabs1(s));
       anorm = fmax(anorm, rs);
     }
+    res = warp_max(res);
+    anorm = warp_max(anorm);
     xnorm = warp_max(xnorm);
     // 5. d = r' - r_i, the ratio 1 + d^T x and its cancellation; d replaces x
     //    in shared memory (each lane its own entries)
     double2 dx = make_double2(0.0, 0.0);
     for (int k = lane; k < n; k += 32) {
-      const double2 ri = __ldcg(a.A + (size_t)i * n + k);
+      const double2 ri = Ls[i * lds + k];
       const double2 d = make_double2(__dsub_rn(S.r[k].x, ri.x), __dsub_rn(S.r[k].y, ri.y));
       const double2 t = cmul(d, S.x[k]);
       dx.x += t.x;
@@ -246,13 +306,12 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
         a.V[(size_t)m * n + k] = S.x[k];
       }
       // C[m][s] = d^T W[s] and C[s][m] = V[s]^T c for s < m; C[m][m] = 1 + d^T c
-      for (int s = 0; s < m; ++s) {
-        const double2 row = warp_dot(a.W + (size_t)s * n, S.x, n, lane);
-        const double2 col = warp_dot(a.V + (size_t)s * n, S.c, n, lane);
-        if (lane == 0) {
-          a.C[m * K + s] = row;
-          a.C[s * K + m] = col;
-        }
+      // (the m x 2 dot products reduced together; S.rhs and S.Cs are free)
+      warp_dots<K>(a.W, S.x, n, m, lane, S.rhs);
+      warp_dots<K>(a.V, S.c, n, m, lane, S.Cs);
+      for (int s = lane; s < m; s += 32) {
+        a.C[m * K + s] = S.rhs[s];
+        a.C[s * K + m] = S.Cs[s];
       }
       double2 dd = make_double2(0.0, 0.0);
       for (int k = lane; k < n; k += 32) {

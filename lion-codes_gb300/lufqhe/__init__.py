@@ -349,6 +349,27 @@ class Server:
             _native.check(int(r), "lufqhe_server_run_stream")
         return lat[:r], ns[:r], el.value, mats.value
 
+    def run_closed(self, walkers: int, nrequests: int, moves: int = 100, k_min: int = 1,
+                   k_max: int = 4096, seed: int = 5):
+        """Closed-loop capacity: (requests, elapsed_s, matrices)."""
+        import ctypes
+        el = ctypes.c_double()
+        mats = ctypes.c_longlong()
+        r = lib().lufqhe_server_run_closed(self._h, walkers, nrequests, moves, k_min, k_max, seed,
+                                           ctypes.byref(el), ctypes.byref(mats))
+        if r < 0:
+            _native.check(int(r), "lufqhe_server_run_closed")
+        return r, el.value, mats.value
+
+    def stats(self, class_n: int = 0):
+        """(moves taken by the O(n^2) path, moves that refactorised instead)."""
+        import ctypes
+        a = ctypes.c_longlong()
+        b = ctypes.c_longlong()
+        _native.check(lib().lufqhe_server_stats(self._h, class_n, ctypes.byref(a), ctypes.byref(b)),
+                      "lufqhe_server_stats")
+        return a.value, b.value
+
     def close(self):
         if self._h:
             lib().lufqhe_server_destroy(self._h)
