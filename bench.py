@@ -716,8 +716,9 @@ def run_plan(args, world, rank, local, full=True):
 def run_serve(args, world, rank, local, full=True):
     """Config 5: a Poisson stream of single-particle moves of device-resident
     walkers (k log-uniform 1..4096, n uniform over 8/16/32/64, 100 moves per
-    walker). Three servers: O(n^2) moves against kept FP64 factors (the
-    default), and servers that refactorise every move, mixed and FP64. For
+    walker). Three servers: the default (O(n^2) moves against kept FP64
+    factors for the classes n <= 16, mixed refactorisation for the others),
+    and servers that refactorise every move, mixed and FP64. For
     each: its capacity (the determinants/s of a saturating stream), then the
     stream at 70% of that capacity and at the configured 20k requests/s, with
     p50/p99 latency (arrival to result on the host) and throughput. The
@@ -763,20 +764,35 @@ def run_serve(args, world, rank, local, full=True):
                 "fraction_of_capacity": (mats / el) / capacity if capacity else None,
                 "per_n": per}
 
-    variants = [("moves", lufqhe.MODE_MIXED, True), ("mixed_refactor", lufqhe.MODE_MIXED, False),
+    # the library's default server (O(n^2) moves for the classes n <= 16,
+    # mixed refactorisation above), then servers that refactorise every move
+    variants = [("default", lufqhe.MODE_MIXED, "auto"),
+                ("mixed_refactor", lufqhe.MODE_MIXED, False),
                 ("fp64_refactor", lufqhe.MODE_PLAIN_FP64_FUSED, False)]
+    def class_rate(n, mode, moves):
+        """Determinants/s of one class alone on the whole GPU, closed loop
+        (the same walker mix restricted to size n)."""
+        srv = lufqhe.Server(96 << 30, mode=mode, classes=(n,), class_sms=[nsm], max_k=4096,
+                            tile=8, moves=moves)
+        try:
+            _, el, mats = srv.run_closed(walkers=args.serve_walkers, nrequests=1000, moves=100,
+                                         k_min=1, k_max=4096, seed=seed + 2)
+        finally:
+            srv.close()
+        return mats / el
+
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
     result = {}
     for label, mode, moves in (variants if full else variants[:2]):
         rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
         batched_mix = 1.0 / float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
-        # SM shares per class: by the batched cost for refactorising servers;
-        # by an O(n^2) move plus a share of refactorisations for the moves one
-        if moves:
-            cost = np.array([n * n * 8.0 + 0.15 * n ** 3 / 3.0 * 4.0 for n in SERVE_SIZES])
-        else:
-            cost = np.array([1.0 / rates[n] for n in SERVE_SIZES])
-        sms = np.maximum(2, np.round(152 * cost / cost.sum())).astype(int)
-        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - 152)
+        # SM shares per class in proportion to its measured cost per
+        # determinant when served alone (k is drawn independently of n, so
+        # every class carries the same expected number of determinants)
+        alone = {n: class_rate(n, mode, moves) for n in SERVE_SIZES}
+        cost = np.array([1.0 / alone[n] for n in SERVE_SIZES])
+        sms = np.maximum(2, np.round(nsm * cost / cost.sum())).astype(int)
+        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - nsm)
         srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES,
                             class_sms=list(map(int, sms)), max_k=4096, tile=8, moves=moves)
         # capacity: a closed loop of walkers, each moving again as soon as its
@@ -798,11 +814,12 @@ def run_serve(args, world, rank, local, full=True):
         result[label] = {"capacity_dets_per_s": capacity,
                          "batched_offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
                          "batched_offline_mix_dets_per_s": batched_mix,
+                         "class_alone_dets_per_s": {str(n): alone[n] for n in SERVE_SIZES},
                          "class_sms": list(map(int, sms)), "runs": runs,
                          "moves_o_n2": moved, "moves_refactorised": refac}
     if rank != 0:
         return None
-    r70 = result["moves"]["runs"]["at_70pct_capacity"]
+    r70 = result["default"]["runs"]["at_70pct_capacity"]
     return {"value": r70["throughput_dets_s"], "unit": "dets/s",
             "p50_ms": r70["p50_ms"], "p99_ms": r70["p99_ms"],
             "fraction_of_capacity": r70["fraction_of_capacity"],

@@ -387,15 +387,25 @@ long long lufqhe_read_matrices_f32(const char *path, int n, long long first, lon
  * the copy engine's bulk copies (one per row, completing on an mbarrier) and
  * prefetch the next matrix into L2; 0: per-lane vector loads. Same bits. */
 #define LUFQHE_OPT_BULK_LOADS 7
-/* Servers created while this is 1 (default) keep each walker matrix's FP64
+/* Servers created while this is 1 keep each walker matrix's FP64
  * L\U factors and take a move's determinant ratio from an O(n^2) solve
  * against them (matrix determinant lemma, Woodbury over the moves since the
- * last factorisation), checked before use (residual of the solve against the
- * resident matrix, cancellation in the ratio); a move that fails a check, or
- * the 9th since the last factorisation, refactorises in FP64. Every
- * factorisation is then FP64 (status LUFQHE_ST_FP64 in mixed mode). 0: every
- * move refactorises (mixed mode's FP32 path where the policy allows). */
+ * last factorisation), checked before use (an error estimate of the ratio, see
+ * LUFQHE_OPT_MOVE_TOL); a move that fails the check, or the 9th since the last
+ * factorisation, refactorises in FP64. Every factorisation of such a class is
+ * then FP64 (status LUFQHE_ST_FP64 in mixed mode). 2 (default): the classes
+ * with n <= 16 only (on ill-conditioned orbital matrices the check refuses
+ * most moves at n >= 32, where refactorising is as fast); 0: every move
+ * refactorises (mixed mode's FP32 path where the policy allows). */
 #define LUFQHE_OPT_SERVE_MOVES 8
+/* Error tolerance of the O(n^2) moves, read when a server is created: a move
+ * is taken only if the a-posteriori estimate of its determinant ratio's
+ * relative error (the solve's first-order error, from its residual and the
+ * transposed solve A^-T d, plus the typical effect of the residual's own
+ * rounding) is at most this value; otherwise it refactorises. Default 1e-12
+ * (the 8 moves between factorisations add about 8e-12 to log|det|);
+ * 0 < value < 1. */
+#define LUFQHE_OPT_MOVE_TOL 9
 int lufqhe_set_option(int option, double value);
 double lufqhe_get_option(int option);
 

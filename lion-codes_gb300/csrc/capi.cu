@@ -184,7 +184,8 @@ int lib_free_async(void *p, cudaStream_t s) {
 }
 
 int g_bulk_loads = 1;
-int g_serve_moves = 1;
+int g_serve_moves = 2;
+double g_move_tol = 1e-12;
 
 bool is_device_memory(const void *p) {
   if (!p) return false;
@@ -404,11 +405,19 @@ extern "C" int lufqhe_set_option(int option, double value) {
     return LUFQHE_SUCCESS;
   }
   if (option == LUFQHE_OPT_SERVE_MOVES) {
-    if (!(value == 0.0 || value == 1.0)) {
-      set_error("lufqhe_set_option: serve moves must be 0 or 1");
+    if (!(value == 0.0 || value == 1.0 || value == 2.0)) {
+      set_error("lufqhe_set_option: serve moves must be 0, 1 or 2");
       return LUFQHE_ERR_INVALID_ARG;
     }
     g_serve_moves = (int)value;
+    return LUFQHE_SUCCESS;
+  }
+  if (option == LUFQHE_OPT_MOVE_TOL) {
+    if (!(value > 0.0 && value < 1.0)) {
+      set_error("lufqhe_set_option: move error bound must be in (0, 1)");
+      return LUFQHE_ERR_INVALID_ARG;
+    }
+    g_move_tol = value;
     return LUFQHE_SUCCESS;
   }
   if (option == LUFQHE_OPT_BULK_LOADS) {
@@ -440,6 +449,7 @@ extern "C" double lufqhe_get_option(int option) {
   if (option == LUFQHE_OPT_KERNEL_TIMING) return (double)g_kernel_timing;
   if (option == LUFQHE_OPT_BULK_LOADS) return (double)g_bulk_loads;
   if (option == LUFQHE_OPT_SERVE_MOVES) return (double)g_serve_moves;
+  if (option == LUFQHE_OPT_MOVE_TOL) return g_move_tol;
   return NAN;
 }
 

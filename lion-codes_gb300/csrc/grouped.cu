@@ -75,9 +75,11 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
                                double *logabs, double *phase, int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
+  // a group on the FP32 path has F and 2n ints (n <= nm) for the correction
+  const CorrScratch cs{F, er, hold};
   if (MODE == LUFQHE_MODE_MIXED && route_fp64(src, share64k)) {
     fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
-                  LUFQHE_ST_FP64);
+                  LUFQHE_ST_FP64, &cs);
     return;
   }
   if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
@@ -109,7 +111,8 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
     if (ok)
       out.push(lane, ob, prod, exp_sum, corr, par, logabs, phase, parity, status);
     else
-      fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status);
+      fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
+                    LUFQHE_ST_FALLBACK, &cs);
   } else {
     int par = 0;
     int st = MODE == LUFQHE_MODE_PLAIN_FP64 ? lup_fp64_warp<ARITH_REF>(M, lds, hold, n, lane, &par)

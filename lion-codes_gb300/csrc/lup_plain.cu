@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "bulk_copy.cuh"
+#include "fp64_correct.cuh"
 #include "lup_fp64.cuh"
 
 namespace lufqhe {
@@ -24,8 +25,10 @@ namespace {
 constexpr int kMaxWarpsPlain = 8;
 
 // Out: element type of the in-place factors (double2, or float2 for the
-// reference's complex64 buffers)
-template <int ARITH, class Src, class Out = double2>
+// reference's complex64 buffers). CORRECT: the mixed mode's FP64 route for
+// 17 <= n <= 32, whose log-determinants get the extended-precision correction
+// (fp64_correct_warp; its scratch follows the row scales in shared memory).
+template <int ARITH, class Src, class Out = double2, bool CORRECT = false>
 __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
     lup_plain_kernel(Src src, Out *__restrict__ Aout, int n, int lda,
                      long long batch, double *__restrict__ logabs, double *__restrict__ phase,
@@ -37,9 +40,16 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
   const int lane = threadIdx.x & 31;
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
-  double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
-                                            (size_t)warps * n * lds) +
-                 warp * 2 * n;
+  double *hold_all = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
+                                                (size_t)warps * n * lds);
+  double *hold = hold_all + warp * 2 * n;
+  CorrScratch cs{};
+  if constexpr (CORRECT) {
+    float2 *F_all = reinterpret_cast<float2 *>(hold_all + (size_t)warps * 2 * n);
+    cs = CorrScratch{F_all + (size_t)warp * n * lds,
+                     reinterpret_cast<int *>(F_all + (size_t)warps * n * lds) + warp * 2 * n,
+                     hold};
+  }
   const int nn = n * n;
 
   // complex128 device batches: each matrix staged by bulk copies (bulk != 0),
@@ -72,11 +82,12 @@ __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
       }
     }
     if (st < 0) st = src.load(b, n, M, lds, lane) ? LUFQHE_ST_NONFINITE : 0;
-    if (!st) st = lup_fp64_warp<ARITH>(M, lds, hold, n, lane, &par);
+    if (!st) st = lup_fp64_warp<ARITH>(M, lds, hold, n, lane, &par, CORRECT ? cs.ints : nullptr);
 
     double la, ph;
     if (st == 0) {
       logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+      if constexpr (CORRECT) fp64_correct_warp(src, b, n, M, lds, cs, lane, &la, &ph);
     } else if (st == LUFQHE_ST_SINGULAR) {
       la = -INFINITY;
       ph = 0.0;
@@ -228,7 +239,12 @@ int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int ar
     timer.stop();
     return check_cuda(cudaGetLastError(), "lup_plain_group_kernel launch");
   }
-  const size_t per_warp = plain_smem_per_warp(n);
+  // the mixed mode's FP64 route (status_or set, no factors written back)
+  const bool correct = status_or != 0 && arith == ARITH_FUSED && Aout == nullptr &&
+                       n >= kCorrectMinN && n <= 32;
+  const size_t per_warp =
+      plain_smem_per_warp(n) +
+      (correct ? (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int) : 0);
   const size_t optin = device_smem_optin();
   int warps = (int)(optin / per_warp);
   if (warps > 4) warps = 4;
@@ -238,8 +254,9 @@ int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int ar
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
   const size_t smem = per_warp * warps;
-  auto kern = arith == ARITH_REF ? lup_plain_kernel<ARITH_REF, Src, Out>
-                                 : lup_plain_kernel<ARITH_FUSED, Src, Out>;
+  auto kern = correct              ? lup_plain_kernel<ARITH_FUSED, Src, Out, true>
+              : arith == ARITH_REF ? lup_plain_kernel<ARITH_REF, Src, Out>
+                                   : lup_plain_kernel<ARITH_FUSED, Src, Out>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem),
                       "cudaFuncSetAttribute(plain)");

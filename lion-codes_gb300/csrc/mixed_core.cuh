@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "lup_fp64.cuh"
+#include "fp64_correct.cuh"
 
 namespace lufqhe {
 namespace mixed {
@@ -549,19 +550,25 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
 }
 
 // FP64 refactorisation of matrix sb of `src` (reloaded into M), results into
-// slot b, status |= flag (FALLBACK, or FP64 for the routed share).
+// slot b, status |= flag (FALLBACK, or FP64 for the routed share). With
+// scratch (cs, 17 <= n <= 32) the log-determinant gets the extended-precision
+// correction of fp64_correct_warp, which brings the FP64 route within the
+// mixed mode's error bound on ill-conditioned matrices.
 template <class Src, bool COHERENT = false>
 __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *M, int lds,
                                   double *hold, int lane, long long b, double *logabs,
                                   double *phase, int8_t *parity, int32_t *status,
-                                  int flag = LUFQHE_ST_FALLBACK) {
+                                  int flag = LUFQHE_ST_FALLBACK,
+                                  const CorrScratch *cs = nullptr) {
   __syncwarp();
   src.template load<COHERENT>(sb, n, M, lds, lane);
   int par = 0;
-  int st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par);
+  const bool correct = cs != nullptr && n >= kCorrectMinN && n <= 32;
+  int st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par, correct ? cs->ints : nullptr);
   double la, ph;
   if (st == 0) {
     logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+    if (correct) fp64_correct_warp(src, sb, n, M, lds, *cs, lane, &la, &ph);
   } else if (st == LUFQHE_ST_SINGULAR) {
     la = -INFINITY;
     ph = 0.0;
@@ -582,9 +589,10 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
 template <bool COHERENT = false>
 __device__ void fallback_fp64(const double2 *src, int n, int lda, double2 *M, int lds,
                               double *hold, int lane, long long b, double *logabs, double *phase,
-                              int8_t *parity, int32_t *status, int flag = LUFQHE_ST_FALLBACK) {
+                              int8_t *parity, int32_t *status, int flag = LUFQHE_ST_FALLBACK,
+                              const CorrScratch *cs = nullptr) {
   fallback_fp64_src<DenseSource, COHERENT>(DenseSource{src, lda}, 0, n, M, lds, hold, lane, b,
-                                           logabs, phase, parity, status, flag);
+                                           logabs, phase, parity, status, flag, cs);
 }
 
 // ---------------------------------------------------------------------------

@@ -197,6 +197,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
   base += warps * 2 * (size_t)n * sizeof(double);
   S.er = reinterpret_cast<int *>(base) + warp * 2 * n;
   S.ec = S.er + n;
+  const CorrScratch cs{S.Af, S.er, S.hold};
 
   DeferredOut out;
   for (long long b = claim_matrix(head, lane, -1); b < batch; b = claim_matrix(head, lane, b)) {
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     double2 *M = reinterpret_cast<double2 *>(S.SC);
     if (share64k && route_fp64_entry(src.first(b, n), share64k)) {
       fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status,
-                        LUFQHE_ST_FP64);
+                        LUFQHE_ST_FP64, &cs);
       continue;
     }
     if (src.load(b, n, M, lds, lane)) {
@@ -219,7 +220,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32)
     else if (pend)
       defer_fp64(head, pend, b, lane, false);
     else
-      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status);
+      fallback_fp64_src(src, b, n, M, lds, S.hold, lane, b, logabs, phase, parity, status,
+                        LUFQHE_ST_FALLBACK, &cs);
   }
   out.flush(lane, logabs, phase, parity, status);
 }
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   base += warps * 2 * (size_t)N * sizeof(double);
   int *er = reinterpret_cast<int *>(base) + warp * 2 * N;
   int *ec = er + N;
+  const CorrScratch cs{F, er, hold};
   // INPLACE: this warp's copy of its current matrix in global memory (a few
   // KB per warp, so the copies stay in L2); an FP64 refactorisation reloads
   // it from there instead of reading the matrix over the host link again
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
         defer_fp64(head, pend, b, lane, true);
       else
         fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                          LUFQHE_ST_FP64);
+                          LUFQHE_ST_FP64, &cs);
       continue;
     }
     bool staged = false;
@@ -338,9 +341,11 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
         out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
       else if constexpr (INPLACE)
         fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
-                                             logabs, phase, parity, status);
+                                             logabs, phase, parity, status, LUFQHE_ST_FALLBACK,
+                                             &cs);
       else
-        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status);
+        fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
+                          LUFQHE_ST_FALLBACK, &cs);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -375,6 +380,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   double *hold = reinterpret_cast<double *>(base) + warp * 2 * N;
   base += warps * 2 * (size_t)N * sizeof(double);
   float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
+  const CorrScratch cs{F, reinterpret_cast<int *>(diag), hold};
   // 1. the FP32 pass's rejections, dealt out
   const unsigned long long listed = head->pend_count;
   const unsigned long long stride = (unsigned long long)warps * gridDim.x;
@@ -383,7 +389,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     const unsigned int e = pend[j];
     const long long b = e & ~kPendRouted;
     fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK, &cs);
   }
   // 2. the saved matrices, claimed; a failed refinement is refactorised here
   DeferredOut out;
@@ -412,7 +418,8 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
                                corr))
         out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
       else
-        fallback_fp64_src(src, h.b, N, M, LDS, hold, lane, h.b, logabs, phase, parity, status);
+        fallback_fp64_src(src, h.b, N, M, LDS, hold, lane, h.b, logabs, phase, parity, status,
+                          LUFQHE_ST_FALLBACK, &cs);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -439,9 +446,14 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
   const int lane = threadIdx.x & 31;
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * n * lds;
-  double *hold = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
-                                            (size_t)warps * n * lds) +
-                 warp * 2 * n;
+  double *hold_all = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
+                                                (size_t)warps * n * lds);
+  double *hold = hold_all + warp * 2 * n;
+  // n <= 32: the correction's scratch after the row scales (fallback_smem_per_warp)
+  float2 *F_all = reinterpret_cast<float2 *>(hold_all + (size_t)warps * 2 * n);
+  const CorrScratch cs{F_all + (size_t)warp * n * lds,
+                       reinterpret_cast<int *>(F_all + (size_t)warps * n * lds) + warp * 2 * n,
+                       hold};
   const unsigned long long listed = head->pend_count;
   const unsigned long long stride = (unsigned long long)warps * gridDim.x;
   for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
@@ -449,7 +461,8 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
     const unsigned int e = pend[j];
     const long long b = e & ~kPendRouted;
     fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
-                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK);
+                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK,
+                      n <= 32 ? &cs : nullptr);
   }
 }
 
@@ -500,11 +513,19 @@ inline bool needs_counter(long long batch, long long grid_warps) {
   return batch > 2 * grid_warps;
 }
 
+// Shared memory of one warp of the FP64 pass: the matrix and its row scales;
+// for n <= 32 also the correction's float2 matrix and 2n ints.
+inline size_t fallback_smem_per_warp(int n) {
+  size_t b = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
+  if (n <= 32) b += (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int);
+  return b;
+}
+
 template <class Src>
 int launch_fallback(Src src, int n, const CallHead *head, const unsigned int *pend,
                     long long batch, double *logabs, double *phase, int8_t *parity,
                     int32_t *status, cudaStream_t stream) {
-  const size_t per_warp = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
+  const size_t per_warp = fallback_smem_per_warp(n);
   int warps = (int)(device_smem_optin() / per_warp);
   if (warps > kFallbackMaxWarps) warps = kFallbackMaxWarps;
   if (warps < 1) warps = 1;

@@ -46,6 +46,13 @@ using namespace mixed;
 
 // Moves kept per matrix between refactorisations (the O(n^2) move path)
 constexpr int kMoveK = 8;
+// With moves on by size (option 8 = 2, the default), the classes that keep
+// factors: on the orbital matrices of the serving workload the moves' error
+// estimate refuses most moves at n >= 32 (their conditioning), where a
+// refactorisation is then as fast or faster (measured closed-loop capacity
+// per class: n = 8 8.1M moves vs 7.4M refactorising, n = 16 12.0M vs 10.7M,
+// n = 32 4.1M vs 8.9M, n = 64 1.0M vs 1.4M dets/s)
+constexpr int kMovesAutoMaxN = 16;
 
 constexpr unsigned kRing = 1u << 16;                  // tiles per class ring
 constexpr unsigned long long kIdleNs = 200000000ull;  // 0.2 s without a claim
@@ -74,7 +81,7 @@ struct ServeTile {
   double2 *lu;               // n x n each
   int *perm;                 // n each
   double2 *w, *v;            // kMoveK x n each
-  double2 *cap;              // kMoveK x kMoveK each
+  double2 *cap;              // kMoveK x kMoveK each (inverse capacitance)
   MoveState *mst;
 };
 
@@ -86,6 +93,7 @@ struct ClassCtl {                // device memory, one per class
   unsigned int pad;
   unsigned long long moved;      // moves taken by the O(n^2) path
   unsigned long long refactored; // moves that refactorised instead
+  double move_tol;               // the moves' error bound
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -205,7 +213,7 @@ __device__ __forceinline__ MoveArrays move_arrays(const ServeTile &t, int n, int
   a.perm = t.perm + (size_t)j * n;
   a.W = t.w + (size_t)j * kMoveK * n;
   a.V = t.v + (size_t)j * kMoveK * n;
-  a.C = t.cap + (size_t)j * kMoveK * kMoveK;
+  a.Ci = t.cap + (size_t)j * kMoveK * kMoveK;
   a.st = t.mst + j;
   return a;
 }
@@ -322,7 +330,8 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
         bool done = false;
         if (!t.build && t.particle >= 0) {
           move_new_row(t, NC, j, S.r, lane);
-          done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
+          done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, ctl->move_tol, &la,
+                                   &ph);
           __syncwarp();
           if (lane == 0) atomicAdd(done ? &ctl->moved : &ctl->refactored, 1ull);
         }
@@ -365,11 +374,13 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
           S.ec = ec;
           ok = mixed_factor(S, NC, lane, theta2, prod, exp_sum, corr, par);
         }
-        if (ok)
+        if (ok) {
           out.push(lane, j, prod, exp_sum, corr, par, t.logabs, t.phase, nullptr, t.status);
-        else
+        } else {
+          const CorrScratch cs{F, er, hold};
           fallback_fp64<true>(src, NC, NC, M, LDS, hold, lane, j, t.logabs, t.phase, nullptr,
-                              t.status);
+                              t.status, LUFQHE_ST_FALLBACK, &cs);
+        }
       } else {
         int par = 0;
         int st = lup_fp64_warp<ARITH_FUSED>(M, LDS, hold, NC, lane, &par);
@@ -489,7 +500,8 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
           bool done = false;
           if (!t.build && t.particle >= 0) {
             move_new_row(t, NC, j, S.r, lane);
-            done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, &la, &ph);
+            done = move_warp<kMoveK>(a, NC, t.particle, M, LDS, S, lane, ctl->move_tol, &la,
+                                     &ph);
             if (lane == 0) atomicAdd(done ? &ctl->moved : &ctl->refactored, 1ull);
           }
           if (done && lane == 0) serve_emit(t, j, la, ph, flag);
@@ -686,6 +698,7 @@ struct SClass {
   bool running = false;
   unsigned int relaunches = 0;
   unsigned int share64k = 0;       // FP64 routing share, fixed at creation
+  int moves = 0;                   // this class keeps factors and takes O(n^2) moves
   double last_query = 0.0;         // when the loop was last seen running (host clock)
 };
 
@@ -700,7 +713,7 @@ struct lufqhe_server_s {
   int tile = 8;
   float theta2 = 0.01f;
   int refine = 1;  // in-place refinement of the tile path (option 5)
-  int moves = 1;   // O(n^2) moves against kept FP64 factors (option 8)
+  int moves = 2;   // O(n^2) moves: 0 off, 1 every class, 2 classes n <= kMovesAutoMaxN (option 8)
   std::vector<SClass> classes;
   // HBM pool with a first-fit free list
   unsigned char *pool = nullptr;
@@ -785,7 +798,7 @@ int ensure_running(lufqhe_server_s *s, SClass &c) {
   // (the shared memory of an FP64-only class holds no FP32 arrays, so the
   // share is the one fixed when the class was created)
   c.kern<<<c.grid, c.warps * 32, c.smem, c.stream>>>(c.ring_d, c.pub_d, s->stop_d, c.ctl, s->mode,
-                                                     s->theta2, c.share64k, s->refine, s->moves);
+                                                     s->theta2, c.share64k, s->refine, c.moves);
   int rc = check_cuda(cudaGetLastError(), "serve kernel launch");
   if (rc) return rc;
   c.running = true;
@@ -832,6 +845,7 @@ namespace lufqhe {
 extern float g_mixed_theta;
 extern int g_mixed_refine;
 extern int g_serve_moves;
+extern double g_move_tol;
 }
 
 extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
@@ -871,7 +885,8 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     sms_left -= sc.sms;
     sc.share64k = mode == LUFQHE_MODE_MIXED ? fp64_share_64k(sc.n) : 0u;
     // with moves every factorisation is FP64 (its factors are kept)
-    const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u || s->moves;
+    sc.moves = s->moves == 1 || (s->moves == 2 && sc.n <= kMovesAutoMaxN);
+    const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u || sc.moves;
     const size_t optin = device_smem_optin();
     size_t used = 0;
     if (fp64_only && serve_group_kernel_for(sc.n)) {
@@ -889,7 +904,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
       sc.warps = groups * kFp64GroupWarps;
       used = per_group * groups;
     } else {
-      const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only, s->moves != 0);
+      const size_t per_warp = serve_smem_per_warp(sc.n, fp64_only, sc.moves != 0);
       sc.warps = std::max(1, std::min<int>(serve_max_warps(sc.n), (int)(optin / per_warp)));
       if (per_warp * sc.warps > optin) {
         set_error("lufqhe_server_create: n=%d needs %zu bytes of shared memory per warp", sc.n,
@@ -917,6 +932,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     if (!rc) rc = check_cuda(cudaMalloc(&sc.ctl, sizeof(ClassCtl)), "serve ctl");
     if (!rc) {
       ClassCtl z{};
+      z.move_tol = g_move_tol;
       rc = check_cuda(cudaMemcpy(sc.ctl, &z, sizeof(z), cudaMemcpyHostToDevice), "serve ctl init");
     }
     s->classes.push_back(sc);
@@ -957,7 +973,7 @@ extern "C" int lufqhe_server_walker_create(lufqhe_server_t *s, int n, int k, con
     set_error("lufqhe_server_walker_create: no class for n=%d", n);
     return LUFQHE_ERR_UNSUPPORTED_N;
   }
-  const WalkerLayout lay(n, k, s->moves != 0);
+  const WalkerLayout lay(n, k, s->classes[cls].moves != 0);
   const size_t bytes = lay.total;
   size_t off = 0;
   if (pool_alloc(s, bytes, &off) != LUFQHE_SUCCESS) {
@@ -1067,14 +1083,14 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
   R.first_tile = C.published;
   R.last_tile = C.published + ntiles;
   __atomic_store_n(&s->comp_h[slot], 0u, __ATOMIC_RELAXED);
-  const WalkerLayout lay(W.n, W.k, s->moves != 0);
+  const WalkerLayout lay(W.n, W.k, s->classes[W.cls].moves != 0);
   unsigned char *blk = s->pool + W.offset;
   double2 *mats = reinterpret_cast<double2 *>(blk + lay.mats);
   double2 *z = reinterpret_cast<double2 *>(blk + lay.z);
   for (unsigned int t = 0; t < ntiles; ++t) {
     const int first = (int)t * s->tile;
     ServeTile T;
-    T.moves = s->moves;
+    T.moves = s->classes[W.cls].moves;
     T.lu = reinterpret_cast<double2 *>(blk + lay.lu) + (size_t)first * W.n * W.n;
     T.perm = reinterpret_cast<int *>(blk + lay.perm) + (size_t)first * W.n;
     T.w = reinterpret_cast<double2 *>(blk + lay.w) + (size_t)first * kMoveK * W.n;

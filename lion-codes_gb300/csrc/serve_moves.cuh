@@ -11,23 +11,37 @@
 //   LU    the FP64 L\U factors of A0, the matrix at the last refactorisation
 //         (pivoted rows), and perm[j], the row of A0 in pivoted row j
 //   W, V  for the m moves since then: W[s] = A0^-1 e_{i_s}, V[s] = d_s
-//   C     the m x m capacitance matrix I + V^T W
+//   Ci    the inverse of the m x m capacitance matrix C = I + V^T W
 //   st    log|det A|, arg det A and m
 // so that A = A0 + sum_s e_{i_s} d_s^T and, by Woodbury,
-//   A^-1 e_i = c - W C^-1 V^T c,   c = A0^-1 e_i   (two triangular solves).
-// Each move is checked before its ratio is used: the residual
-// A x - e_i of the solve against the resident current matrix, and the
-// cancellation in 1 + d^T x. A move that fails a check, or finds the
-// history full (m = K), refactorises A' in FP64 instead and restarts from it.
-// The work per accepted move is O(n^2 + n K + K^3), against O(n^3) for a new
+//   A^-1 e_i = c - W Ci V^T c,   c = A0^-1 e_i   (two triangular solves).
+// Accepting a move borders C with the column V^T c, the row d^T W and the
+// corner 1 + d^T c; the Schur complement of that border is 1 + d^T x, the
+// determinant ratio itself, so Ci grows by a rank-one update and a border
+// (O(m^2), lane-parallel) instead of being refactorised.
+// Each move is checked before its ratio is used. With y = A^-T d (a
+// transposed solve against the same factors and history) and s = A x - e_i
+// the residual of the solve against the resident current matrix, the ratio's
+// first-order error is y^T s, so the ratio is taken as 1 + d^T x - y^T s and
+// its error estimated as |y^T s| + 3 u (sum_p |y_p|^2 (|A| |x|)_p^2)^(1/2),
+// the second term the typical size of y^T times the rounding of s itself (a
+// worst-case bound, u sum_p |y_p| (|A| |x|)_p n, exceeds the errors actually
+// made by two to three orders of magnitude on these matrices and refuses
+// nearly every move at n >= 32). A move whose estimate exceeds the tolerance
+// times |ratio|, or that finds the history full (m = K), refactorises A' in
+// FP64 instead and restarts from it. (A residual test alone does not suffice:
+// on ill-conditioned orbital matrices a solve with a residual at rounding
+// level can still carry a forward error of 1e-5 in the direction of d.)
+// The work per accepted move is O(n^2 + n K + K^2), against O(n^3) for a new
 // factorisation.
 //
-// A move is a chain of short dependent steps on one warp, so the code keeps
-// that chain short: the matrices are staged into shared memory by
-// asynchronous copies issued all at once, the diagonal reciprocals of U are
-// taken lane-parallel before the back substitution, the residual is formed
-// one row per lane from shared memory (no reductions), and the m dot products
-// against the history are reduced side by side.
+// On this GPU a warp's FP64 instruction costs the FP64 pipe the same time
+// whether one lane or 32 are active, so the code counts FP64 instructions,
+// not flops: the matrices are staged into shared memory by asynchronous
+// copies issued all at once, the diagonal reciprocals of U are taken
+// lane-parallel before the back substitution, the residual is formed one row
+// per lane from shared memory (no reductions), the K dot products against the
+// history run in K lane groups at once, and nothing runs on one lane alone.
 #pragma once
 
 #include "lup_fp64.cuh"
@@ -45,16 +59,15 @@ struct MoveArrays {
   double2 *A;
   double2 *LU;
   int *perm;
-  double2 *W;  // K x n
-  double2 *V;  // K x n
-  double2 *C;  // K x K, row-major
+  double2 *W;   // K x n
+  double2 *V;   // K x n
+  double2 *Ci;  // K x K, row-major: the inverse capacitance matrix
   MoveState *st;
 };
 
-// A move is accepted when max_p |(A x - e_i)_p| <= kMoveResTol ||A||_inf ||x||_inf
-// and |1 + d^T x| >= kMoveCancel max(1, |d^T x|).
-constexpr double kMoveResTol = 1e-14;
-constexpr double kMoveCancel = 1e-2;
+// the typical rounding of a residual formed in FP64, per unit of |A| |x|
+// (three standard deviations of u)
+constexpr double kMoveNoise = 3.0 * 1.1102230246251565e-16;
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(__fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y)),
@@ -62,6 +75,12 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 __device__ __forceinline__ double2 csubmul(double2 s, double2 a, double2 b) {  // s - a b
   return cmsub<ARITH_FUSED>(s, a, b);
+}
+__device__ __forceinline__ void cmac(double2 &s, double2 a, double2 b) {  // s += a b
+  s.x = __fma_rn(a.x, b.x, s.x);
+  s.x = __fma_rn(-a.y, b.y, s.x);
+  s.y = __fma_rn(a.x, b.y, s.y);
+  s.y = __fma_rn(a.y, b.x, s.y);
 }
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
 // 1 / b to within a few ulps (one reciprocal), for the solves, whose result is
@@ -116,71 +135,69 @@ __device__ __forceinline__ bool stage_matrix_checked(double2 *dst, int lds, cons
 }
 
 // out[s] = sum_p X[s n + p] b[p] for s < m (m <= K; X in global memory, b in
-// shared memory): each lane accumulates all m partial sums, then the m warp
-// reductions run side by side. out is shared memory, written by lane 0.
+// shared memory): the warp splits into K groups of 32 / K lanes, group s
+// forms dot s over a stride of p, and the groups reduce side by side. out is
+// shared memory.
 template <int K>
-__device__ __forceinline__ void warp_dots(const double2 *X, const double2 *b, int n, int m,
-                                          int lane, double2 *out) {
-  double2 acc[K];
+__device__ __forceinline__ void group_dots(const double2 *X, const double2 *b, int n, int m,
+                                           int lane, double2 *out) {
+  static_assert(32 % K == 0, "K divides the warp");
+  constexpr int G = 32 / K;
+  const int s = lane / G, r = lane % G;
+  double2 acc = make_double2(0.0, 0.0);
+  if (s < m)
+    for (int p = r; p < n; p += G) cmac(acc, __ldcg(X + (size_t)s * n + p), b[p]);
 #pragma unroll
-  for (int s = 0; s < K; ++s) acc[s] = make_double2(0.0, 0.0);
-  for (int p = lane; p < n; p += 32) {
-    const double2 bp = b[p];
-#pragma unroll
-    for (int s = 0; s < K; ++s) {
-      if (s < m) {
-        const double2 t = cmul(__ldcg(X + (size_t)s * n + p), bp);
-        acc[s].x += t.x;
-        acc[s].y += t.y;
-      }
-    }
+  for (int off = G / 2; off; off >>= 1) {
+    acc.x += __shfl_xor_sync(kFull, acc.x, off);
+    acc.y += __shfl_xor_sync(kFull, acc.y, off);
   }
-#pragma unroll
-  for (int off = 16; off; off >>= 1)
-#pragma unroll
-    for (int s = 0; s < K; ++s) {
-      acc[s].x += __shfl_xor_sync(kFull, acc[s].x, off);
-      acc[s].y += __shfl_xor_sync(kFull, acc[s].y, off);
-    }
-  if (lane == 0)
-#pragma unroll
-    for (int s = 0; s < K; ++s)
-      if (s < m) out[s] = acc[s];
+  if (r == 0 && s < m) out[s] = acc;
   __syncwarp();
 }
 
 // Shared-memory scratch of one move, after the n x lds factor area.
 struct MoveScratch {
-  double2 *c, *x, *r;  // n each
-  double2 *Cs;         // K x K
-  double2 *rhs;        // K
-  int *perm;           // n
+  double2 *c, *x, *r, *d, *y, *rd;  // n each
+  double2 *b, *z, *g, *h;           // K each: V^T c, Ci b, W^T d, Ci^T g
+  int *perm;                        // n
   static constexpr size_t bytes(int n, int K) {
-    return (3 * (size_t)n + (size_t)K * K + K) * sizeof(double2) + (size_t)n * sizeof(int);
+    return (6 * (size_t)n + 4 * (size_t)K) * sizeof(double2) + (size_t)n * sizeof(int);
   }
   __device__ void bind(unsigned char *p, int n, int K) {
     c = reinterpret_cast<double2 *>(p);
     x = c + n;
     r = x + n;
-    Cs = r + n;
-    rhs = Cs + K * K;
-    perm = reinterpret_cast<int *>(rhs + K);
+    d = r + n;
+    y = d + n;
+    rd = y + n;
+    b = rd + n;
+    z = b + K;
+    g = z + K;
+    h = g + K;
+    perm = reinterpret_cast<int *>(h + K);
   }
 };
 
 // Try the move of row i to the new row r' (in S.r) for one matrix, one warp.
 // Ls (row stride lds) receives the factors, then the current matrix. True
-// (warp-uniform) if the move was accepted: the state, W, V, C and row i of A
+// (warp-uniform) if the move was accepted: the state, W, V, Ci and row i of A
 // are updated and (*la, *ph) is the new log-determinant. False: only row i of
 // A has been rewritten; the caller refactorises A.
 template <int K>
 __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int lds,
-                          const MoveScratch &S, int lane, double *la_out, double *ph_out) {
+                          const MoveScratch &S, int lane, double tol, double *la_out,
+                          double *ph_out) {
   const MoveState st = *a.st;
   const int m = st.m;
   bool ok = m < K && st.la == st.la;
-  // 1. the factors of A0 into shared memory (rows in pivoted order)
+  // 1. the factors of A0 into shared memory (rows in pivoted order); d = r' -
+  //    r_i from the current row i in global memory meanwhile
   for (int p = lane; p < n; p += 32) S.perm[p] = __ldcg(a.perm + p);
+  for (int k = lane; k < n; k += 32) {
+    const double2 ri = __ldcg(a.A + (size_t)i * n + k);
+    S.d[k] = make_double2(__dsub_rn(S.r[k].x, ri.x), __dsub_rn(S.r[k].y, ri.y));
+  }
   stage_matrix_async(Ls, lds, a.LU, n, lane);
   // q: the pivoted position of row i
   int q = n;
@@ -191,11 +208,10 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
   ok = ok && q < n;
   if (ok) {
     // 2. c = U^-1 L^-1 e_q: forward from q (unit lower), then backward; the
-    //    reciprocals of U's diagonal first, lane-parallel, into S.x (free
-    //    until step 3), so each backward step is a multiply
+    //    reciprocals of U's diagonal first, lane-parallel
     for (int p = lane; p < n; p += 32) {
       S.c[p] = make_double2(p == q ? 1.0 : 0.0, 0.0);
-      S.x[p] = crcp(Ls[p * lds + p]);
+      S.rd[p] = crcp(Ls[p * lds + p]);
     }
     __syncwarp();
     for (int j = q; j + 1 < n; ++j) {
@@ -204,124 +220,125 @@ __device__ bool move_warp(const MoveArrays &a, int n, int i, double2 *Ls, int ld
       __syncwarp();
     }
     for (int j = n - 1; j >= 0; --j) {
-      const double2 cj = cmul(S.c[j], S.x[j]);
+      const double2 cj = cmul(S.c[j], S.rd[j]);
       __syncwarp();
       if (lane == 0) S.c[j] = cj;
       for (int p = lane; p < j; p += 32) S.c[p] = csubmul(S.c[p], Ls[p * lds + j], cj);
       __syncwarp();
     }
-    // 3. x = c - W C^-1 V^T c (the m dot products reduced together)
-    warp_dots<K>(a.V, S.c, n, m, lane, S.rhs);
-    for (int e = lane; e < m * m; e += 32) S.Cs[e] = __ldcg(a.C + (e / m) * K + (e % m));
-    __syncwarp();
-    if (lane == 0 && m > 0) {
-      // C z = V^T c by Gaussian elimination with partial pivoting (m <= K);
-      // each pivot is kept as its reciprocal
-      double2 *Cm = S.Cs;
-      double2 *z = S.rhs;
-      for (int j = 0; j < m; ++j) {
-        int p = j;
-        for (int r = j + 1; r < m; ++r)
-          if (cabs1(Cm[r * m + j]) > cabs1(Cm[p * m + j])) p = r;
-        if (p != j) {
-          for (int k = 0; k < m; ++k) {
-            const double2 t = Cm[p * m + k];
-            Cm[p * m + k] = Cm[j * m + k];
-            Cm[j * m + k] = t;
-          }
-          const double2 t = z[p];
-          z[p] = z[j];
-          z[j] = t;
-        }
-        const double2 rj = crcp(Cm[j * m + j]);
-        Cm[j * m + j] = rj;
-        for (int r = j + 1; r < m; ++r) {
-          const double2 l = cmul(Cm[r * m + j], rj);
-          for (int k = j + 1; k < m; ++k) Cm[r * m + k] = csubmul(Cm[r * m + k], l, Cm[j * m + k]);
-          z[r] = csubmul(z[r], l, z[j]);
-        }
+    // 3. x = c - W z, z = Ci V^T c (lane s forms z_s); g = W^T d, h = Ci^T g
+    group_dots<K>(a.V, S.c, n, m, lane, S.b);
+    group_dots<K>(a.W, S.d, n, m, lane, S.g);
+    if (lane < m) {
+      double2 t = make_double2(0.0, 0.0), u2 = make_double2(0.0, 0.0);
+      for (int u = 0; u < m; ++u) {
+        cmac(t, __ldcg(a.Ci + lane * K + u), S.b[u]);
+        cmac(u2, S.g[u], __ldcg(a.Ci + u * K + lane));
       }
-      for (int j = m - 1; j >= 0; --j) {
-        double2 t = z[j];
-        for (int k = j + 1; k < m; ++k) t = csubmul(t, Cm[j * m + k], z[k]);
-        z[j] = cmul(t, Cm[j * m + j]);
-      }
+      S.z[lane] = t;
+      S.h[lane] = u2;
     }
     __syncwarp();
+    // x, and d' = d - V h (into S.y) for the transposed solve
     for (int p = lane; p < n; p += 32) {
-      double2 t = S.c[p];
-      for (int s = 0; s < m; ++s) t = csubmul(t, __ldcg(a.W + (size_t)s * n + p), S.rhs[s]);
+      double2 t = S.c[p], e = S.d[p];
+      for (int u = 0; u < m; ++u) {
+        t = csubmul(t, __ldcg(a.W + (size_t)u * n + p), S.z[u]);
+        e = csubmul(e, __ldcg(a.V + (size_t)u * n + p), S.h[u]);
+      }
       S.x[p] = t;
+      S.y[p] = e;
     }
-    // 4. a-posteriori check of x against the current matrix: the residual
-    //    A x - e_i, relative to ||A||_inf ||x||_inf. The factors are done
-    //    with: A takes their place in shared memory, and each lane forms whole
-    //    rows (no reductions).
+    __syncwarp();
+    // 4. y = A^-T d = P^T L^-T U^-T d': with A0 = P^T L U, forward through
+    //    U^T (rows of U as axpys), then backward through L^T (rows of L)
+    for (int j = 0; j < n; ++j) {
+      const double2 tj = cmul(S.y[j], S.rd[j]);
+      __syncwarp();
+      if (lane == 0) S.y[j] = tj;
+      for (int p = j + 1 + lane; p < n; p += 32) S.y[p] = csubmul(S.y[p], Ls[j * lds + p], tj);
+      __syncwarp();
+    }
+    for (int j = n - 1; j > 0; --j) {
+      const double2 wj = S.y[j];
+      for (int p = lane; p < j; p += 32) S.y[p] = csubmul(S.y[p], Ls[j * lds + p], wj);
+      __syncwarp();
+    }
+    // y_perm[j] = w_j, in place through registers (n <= 64); |x_k| into S.rd
+    // (the reciprocals are done with) for the residual's bound
+    double2 wv[2];
+    int wp[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int j = lane + 32 * t;
+      wv[t] = j < n ? S.y[j] : make_double2(0.0, 0.0);
+      wp[t] = j < n ? S.perm[j] : 0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+      if (lane + 32 * t < n) S.y[wp[t]] = wv[t];
+    for (int k = lane; k < n; k += 32) S.rd[k].x = cabs1(S.x[k]);
+    // 5. the current matrix replaces the factors; residual s = A x - e_i and
+    //    q = |A| |x|, one row per lane; the ratio's first-order error y^T s
+    //    and the size of y^T times the rounding of s, (sum |y_p|^2 q_p^2)^(1/2)
     __syncwarp();
     stage_matrix_async(Ls, lds, a.A, n, lane);
-    double res = 0.0, anorm = 0.0, xnorm = 0.0;
+    double noise2 = 0.0;
+    double2 yts = make_double2(0.0, 0.0), dx = make_double2(0.0, 0.0);
     for (int p = lane; p < n; p += 32) {
-      xnorm = fmax(xnorm, cabs1(S.x[p]));
-      double2 s = make_double2(p == i ? -1.0 : 0.0, 0.0);
-      double rs = 0.0;
+      double2 sres = make_double2(p == i ? -1.0 : 0.0, 0.0);
+      double qa = 0.0;
       for (int k = 0; k < n; ++k) {
         const double2 v = Ls[p * lds + k];
-        const double2 t = cmul(v, S.x[k]);
-        s.x += t.x;
-        s.y += t.y;
-        rs += cabs1(v);
+        const double2 xk = S.x[k];
+        cmac(sres, v, xk);
+        qa = __fma_rn(cabs1(v), S.rd[k].x, qa);
       }
-      res = fmax(res, cabs1(s));
-      anorm = fmax(anorm, rs);
+      const double2 yp = S.y[p];
+      const double yq = __dmul_rn(cabs1(yp), qa);
+      noise2 = __fma_rn(yq, yq, noise2);
+      cmac(yts, yp, sres);
+      cmac(dx, S.d[p], S.x[p]);
     }
-    res = warp_max(res);
-    anorm = warp_max(anorm);
-    xnorm = warp_max(xnorm);
-    // 5. d = r' - r_i, the ratio 1 + d^T x and its cancellation; d replaces x
-    //    in shared memory (each lane its own entries)
-    double2 dx = make_double2(0.0, 0.0);
-    for (int k = lane; k < n; k += 32) {
-      const double2 ri = Ls[i * lds + k];
-      const double2 d = make_double2(__dsub_rn(S.r[k].x, ri.x), __dsub_rn(S.r[k].y, ri.y));
-      const double2 t = cmul(d, S.x[k]);
-      dx.x += t.x;
-      dx.y += t.y;
-      S.x[k] = d;
-    }
+    noise2 = warp_sum2(make_double2(noise2, 0.0)).x;
+    yts = warp_sum2(yts);
     dx = warp_sum2(dx);
-    __syncwarp();
-    const double2 ratio = make_double2(1.0 + dx.x, dx.y);
+    // 6. the ratio, first-order corrected; taken if within the bound
+    const double2 sigma = make_double2(1.0 + dx.x, dx.y);  // the Schur complement
+    const double2 ratio = make_double2(sigma.x - yts.x, sigma.y - yts.y);
     const double rmag = fmax(fabs(ratio.x), fabs(ratio.y));
-    ok = (res <= kMoveResTol * anorm * xnorm) && finite_d(res) &&
-         rmag >= kMoveCancel * fmax(1.0, cabs1(dx)) && finite_c(ratio);
+    const double est = __fma_rn(kMoveNoise, sqrt(noise2), cabs1(yts));
+    ok = finite_d(est) && finite_c(ratio) && est <= tol * rmag && rmag > 0.0;
     ok = __shfl_sync(kFull, ok, 0);
     if (ok) {
-      // 6. accept: the log-determinant, then the history (W[m] = c, V[m] = d,
-      //    the new row and column of C), then row i of A
+      // 7. accept: the log-determinant; the history (W[m] = c, V[m] = d);
+      //    Ci bordered by the Schur complement sigma = 1 + d^T x: with
+      //    s = 1 / sigma, Ci += z s h^T, column m = -z s, row m = -s h^T,
+      //    corner s
       double lg, ar;
       log_arg_c(ratio, lg, ar);
       const double la = st.la + lg, ph = st.ph + ar;
       for (int k = lane; k < n; k += 32) {
         a.W[(size_t)m * n + k] = S.c[k];
-        a.V[(size_t)m * n + k] = S.x[k];
+        a.V[(size_t)m * n + k] = S.d[k];
       }
-      // C[m][s] = d^T W[s] and C[s][m] = V[s]^T c for s < m; C[m][m] = 1 + d^T c
-      // (the m x 2 dot products reduced together; S.rhs and S.Cs are free)
-      warp_dots<K>(a.W, S.x, n, m, lane, S.rhs);
-      warp_dots<K>(a.V, S.c, n, m, lane, S.Cs);
-      for (int s = lane; s < m; s += 32) {
-        a.C[m * K + s] = S.rhs[s];
-        a.C[s * K + m] = S.Cs[s];
+      const double2 sr = crcp(sigma);
+      const int m1 = m + 1;
+      for (int e = lane; e < m1 * m1; e += 32) {
+        const int u = e / m1, v = e - u * m1;
+        double2 val;
+        if (u < m && v < m)
+          val = csubmul(__ldcg(a.Ci + u * K + v), cmul(S.z[u], sr), make_double2(-S.h[v].x, -S.h[v].y));
+        else if (u < m)
+          val = cmul(S.z[u], make_double2(-sr.x, -sr.y));
+        else if (v < m)
+          val = cmul(make_double2(-sr.x, -sr.y), S.h[v]);
+        else
+          val = sr;
+        a.Ci[u * K + v] = val;
       }
-      double2 dd = make_double2(0.0, 0.0);
-      for (int k = lane; k < n; k += 32) {
-        const double2 t = cmul(S.x[k], S.c[k]);
-        dd.x += t.x;
-        dd.y += t.y;
-      }
-      dd = warp_sum2(dd);
       if (lane == 0) {
-        a.C[m * K + m] = make_double2(1.0 + dd.x, dd.y);
         MoveState ns;
         ns.la = la;
         ns.ph = ph;

@@ -273,9 +273,12 @@ class Server:
     """Device-resident walkers and the persistent request loop (lufqhe_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int, mode: int = MODE_MIXED, classes=(8, 16, 32, 64),
-                 class_sms=None, max_k: int = 4096, tile: int = 8, moves: bool | None = None):
+                 class_sms=None, max_k: int = 4096, tile: int = 8,
+                 moves: "bool | str | None" = None):
         """moves: O(n^2) determinant-ratio moves against kept FP64 factors
-        (LUFQHE_OPT_SERVE_MOVES, read at creation); None keeps the option's value."""
+        (LUFQHE_OPT_SERVE_MOVES, read at creation): True for every class,
+        False for none, "auto" for the classes n <= 16; None keeps the
+        option's value (default "auto")."""
         import ctypes
         self._h = None
         cn = (ctypes.c_int * len(classes))(*classes)
@@ -283,7 +286,7 @@ class Server:
         h = ctypes.c_void_p()
         old = lib().lufqhe_get_option(8)
         if moves is not None:
-            lib().lufqhe_set_option(8, 1.0 if moves else 0.0)
+            lib().lufqhe_set_option(8, 2.0 if moves == "auto" else (1.0 if moves else 0.0))
         try:
             rc = lib().lufqhe_server_create(ctypes.byref(h), int(hbm_budget_bytes), mode, cn, cs,
                                             len(classes), max_k, tile)

@@ -236,3 +236,30 @@ def test_shard_by_cost_rejects(lufqhe_mod):
     assert lib.lufqhe_shard_by_cost(n, c, 1, 0, 1, b, e) == -1
     bad = (ctypes.c_int * 1)(0)
     assert lib.lufqhe_shard_by_cost(bad, c, 1, 2, 1, b, e) == -1
+
+
+@pytest.mark.parametrize("opt,good,bad", [
+    (1, [0.0, 0.3], [-1.0]),             # mixed threshold
+    (5, [0.0, 1.0], [0.5, 2.0]),         # refinement on/off
+    (6, [0.0, 1.0], [2.0]),              # kernel timing
+    (7, [0.0, 1.0], [3.0]),              # bulk loads
+    (8, [0.0, 1.0, 2.0], [0.5, 3.0]),    # serving moves (2: by size)
+    (9, [1e-12, 1e-8], [0.0, 1.0, -1e-12]),  # move error bound
+])
+def test_options_round_trip_and_validation(lufqhe_mod, opt, good, bad):
+    """Options are host-side settings: set/get round-trips and out-of-range
+    values are rejected (the previous value kept), without a GPU."""
+    lib = lufqhe_mod.lib()
+    invalid = lufqhe_mod._native.header_constants()["LUFQHE_ERR_INVALID_ARG"]
+    old = lib.lufqhe_get_option(opt)
+    try:
+        for v in good:
+            assert lib.lufqhe_set_option(opt, v) == 0
+            assert lib.lufqhe_get_option(opt) == pytest.approx(v)
+        for v in bad:
+            before = lib.lufqhe_get_option(opt)
+            assert lib.lufqhe_set_option(opt, v) == invalid
+            assert lib.lufqhe_get_option(opt) == before
+    finally:
+        lib.lufqhe_set_option(opt, old)
+    assert lib.lufqhe_set_option(99, 1.0) == invalid

@@ -3,7 +3,9 @@ correction + FP64 fallback) against the double-double truth oracle.
 
 Tolerance: the error of the complex log-determinant log|det| + i*phase,
 relative to max(1, |log|det||), is <= 1e-10 in both parts for every matrix the
-mixed path accepts; fallback matrices carry the FP64 fused result bit for bit.
+mixed path accepts and, for 17 <= n <= 32, for every matrix of the FP64 route
+too (the FP64 factorisation plus its extended-precision correction). Outside
+that range the FP64 route carries the fused FP64 kernel's result bit for bit.
 """
 import math
 
@@ -13,6 +15,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-10
+CORRECT_MIN_N, CORRECT_MAX_N = 17, 32   # sizes whose FP64 route is corrected
 
 
 def rel(a, b):
@@ -61,13 +64,25 @@ def check_mixed(lufqhe_mod, oracle, A, max_fallback_frac):
         initial=0) < TOL_MIXED
     fp = fb | routed
     if fp.any():
-        # the FP64 route carries the fused FP64 kernel's result and status bits
-        # (including its scale-below-1e-24 rule, whose result is NaN)
+        # the FP64 route carries the fused FP64 kernel's status bits (including
+        # its scale-below-1e-24 rule, whose result is NaN) and its result:
+        # bit for bit outside the corrected sizes, within the bound inside them
         fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
-        assert np.array_equal(out["logabs"][fp], fused["logabs"][fp], equal_nan=True)
-        assert np.array_equal(out["phase"][fp], fused["phase"][fp], equal_nan=True)
         flags = lufqhe_mod.ST_FALLBACK | lufqhe_mod.ST_FP64
         assert ((out["status"][fp] & ~flags) == fused["status"][fp]).all()
+        n = A.shape[1]
+        if CORRECT_MIN_N <= n <= CORRECT_MAX_N:
+            good = fp & (out["status"] & ~flags == 0)
+            assert rel(out["logabs"][good], la[good]).max(initial=0) < TOL_MIXED
+            assert (dphase(out["phase"][good], ph[good]) /
+                    np.maximum(1.0, np.abs(la[good]))).max(initial=0) < TOL_MIXED
+            # the correction is of rounding size next to the fused result
+            assert rel(out["logabs"][good], fused["logabs"][good]).max(initial=0) < 1e-6
+            bad = fp & ~good
+            assert np.array_equal(out["logabs"][bad], fused["logabs"][bad], equal_nan=True)
+        else:
+            assert np.array_equal(out["logabs"][fp], fused["logabs"][fp], equal_nan=True)
+            assert np.array_equal(out["phase"][fp], fused["phase"][fp], equal_nan=True)
     return out
 
 
@@ -177,10 +192,11 @@ def test_mixed_deterministic_across_batch_positions(cuda, lufqhe_mod):
 
 
 @pytest.mark.parametrize("share", [0.0, 0.5])
-def test_fp64_pass_every_matrix_listed(cuda, lufqhe_mod, threshold, fp64_share, share):
+def test_fp64_pass_every_matrix_listed(cuda, lufqhe_mod, oracle, threshold, fp64_share, share):
     """n = 24 hands every FP64 factorisation to the second pass through the
     call's pending list, which has room for the whole batch: with every matrix
-    rejected (threshold 0), or half of them routed, all are refactorised."""
+    rejected (threshold 0), or half of them routed, all are refactorised, and
+    every (corrected) FP64 result is within 1e-10 of the double-double oracle."""
     threshold(0.0)
     fp64_share(share)
     batch = 16384 + 1028
@@ -191,9 +207,11 @@ def test_fp64_pass_every_matrix_listed(cuda, lufqhe_mod, threshold, fp64_share, 
     assert np.isin(out["status"] & flags, [lufqhe_mod.ST_FALLBACK, lufqhe_mod.ST_FP64]).all()
     routed = ((out["status"] & lufqhe_mod.ST_FP64) != 0).mean()
     assert abs(routed - share) < 0.02
-    assert np.array_equal(out["logabs"], fused["logabs"], equal_nan=True)
-    assert np.array_equal(out["phase"], fused["phase"], equal_nan=True)
     assert ((out["status"] & ~flags) == fused["status"]).all()
+    la, ph, _ = oracle.logdet_dd(A.cpu().numpy())
+    assert rel(out["logabs"], la).max() < TOL_MIXED
+    assert (dphase(out["phase"], ph) / np.maximum(1.0, np.abs(la))).max() < TOL_MIXED
+    assert rel(out["logabs"], fused["logabs"]).max() < 1e-6
     del A
     cuda.cuda.empty_cache()
 
@@ -246,9 +264,9 @@ def test_refinement_pass(cuda, lufqhe_mod, oracle, n):
 @pytest.mark.parametrize("n,batch,seed", [(24, 32768, 2), (32, 16384, 3), (16, 32768, 4)])
 def test_full_size_lll_against_double_double(cuda, lufqhe_mod, oracle, n, batch, seed):
     """The full config-3 batch (and full-size n = 16, 32 LLL batches): every
-    matrix the mixed path accepts, refined ones included, is within 1e-10
-    (relative to max(1, |log|det||)) of the double-double oracle in log|det|
-    and phase; the FP64 ones carry the fused FP64 kernel's bits."""
+    result, accepted (refined ones included) or from the corrected FP64 route,
+    is within 1e-10 (relative to max(1, |log|det||)) of the double-double
+    oracle in log|det| and phase."""
     A, _ = lufqhe_mod.gen_lll(batch, n, seed=seed)
     check_mixed(lufqhe_mod, oracle, A, max_fallback_frac=0.2)
 
