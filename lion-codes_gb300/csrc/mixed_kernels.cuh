@@ -91,6 +91,7 @@ struct CallHead {
   unsigned long long refine_claimed;  // claimed by the finish kernel
   unsigned int pend_count;            // entries of the pending list
   unsigned int pad;
+  unsigned long long corr_count;      // host-link variant: matrices listed for the correction
 };
 constexpr size_t kHeadBytes = 256;
 
@@ -141,6 +142,34 @@ constexpr size_t refine_entry_bytes() {
 // Share of a batch the refinement buffer has room for (the rest go straight
 // to the FP64 pass): on lowest-Landau-level n = 24 matrices about 9% qualify.
 constexpr double kRefineShare = 0.25;
+
+// The host-link variant refactorises rejected matrices in place (it waits on
+// the link and has compute to spare) but hands their extended-precision
+// correction, whose latency would hold the warp off the link for the length
+// of several factorisations, to a pass of its own: the matrix (from the warp's
+// device copy) and its slot go to the call's correction list.
+template <int N>
+constexpr size_t corr_entry_bytes() {
+  return 16 + (size_t)N * N * sizeof(double2);
+}
+// Share of a batch the correction list has room for (beyond it the warp
+// corrects in place).
+constexpr double kCorrShare = 0.25;
+
+template <int N>
+__device__ bool list_correction(CallHead *head, unsigned char *buf, long long cap,
+                                const double2 *own, long long b, int lane) {
+  unsigned long long k = 0;
+  if (lane == 0) k = atomicAdd(&head->corr_count, 1ull);
+  k = __shfl_sync(kFull, k, 0);
+  if (k >= (unsigned long long)cap) return false;
+  unsigned char *e = buf + k * corr_entry_bytes<N>();
+  double2 *dA = reinterpret_cast<double2 *>(e + 16);
+  for (int q = lane; q < N * N; q += 32) dA[q] = __ldcg(own + q);
+  if (lane == 0) *reinterpret_cast<long long *>(e) = b;
+  __syncwarp();
+  return true;
+}
 
 // Save a TILE_REFINE matrix; false (warp-uniform) if the buffer is full.
 template <int N>
@@ -231,7 +260,8 @@ template <int N, class Src, bool INPLACE = false>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     lup_mixed_tile_kernel(Src src, long long batch, float theta2,
                           unsigned int share64k, CallHead *head, unsigned int *pend,
-                          double2 *spill, unsigned char *refine, long long refine_cap, int bulk,
+                          double2 *spill, unsigned char *refine, long long refine_cap,
+                          unsigned char *corr_list, long long corr_cap, int bulk,
                           double *__restrict__ logabs,
                           double *__restrict__ phase, int8_t *__restrict__ parity,
                           int32_t *__restrict__ status) {
@@ -339,10 +369,14 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
                                 reinterpret_cast<float2 *>(er), lane, theta2,
                                 tile_la_est(prod, exp_sum), corr)))
         out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
-      else if constexpr (INPLACE)
+      else if constexpr (INPLACE) {
+        const bool listed =
+            N >= kCorrectMinN && corr_list != nullptr &&
+            list_correction<N>(head, corr_list, corr_cap, own, b, lane);
         fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
                                              logabs, phase, parity, status, LUFQHE_ST_FALLBACK,
-                                             &cs);
+                                             listed ? nullptr : &cs);
+      }
       else
         fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
                           LUFQHE_ST_FALLBACK, &cs);
@@ -466,6 +500,39 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
   }
 }
 
+// The host-link variant's corrections: each listed matrix is refactorised from
+// its device copy (the same bits as the in-place factorisation) and its
+// log-determinant corrected; results overwrite the uncorrected ones.
+template <int N>
+__global__ void __launch_bounds__(kFallbackMaxWarps * 32)
+    lup_mixed_correct_kernel(const CallHead *head, const unsigned char *corr, long long corr_cap,
+                             double *__restrict__ logabs, double *__restrict__ phase,
+                             int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LDS = N + 1;
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * N * LDS;
+  double *hold_all = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
+                                                (size_t)warps * N * LDS);
+  double *hold = hold_all + warp * 2 * N;
+  float2 *F_all = reinterpret_cast<float2 *>(hold_all + (size_t)warps * 2 * N);
+  const CorrScratch cs{F_all + (size_t)warp * N * LDS,
+                       reinterpret_cast<int *>(F_all + (size_t)warps * N * LDS) + warp * 2 * N,
+                       hold};
+  const unsigned long long listed = min(head->corr_count, (unsigned long long)corr_cap);
+  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
+  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
+       j += stride) {
+    const unsigned char *e = corr + j * corr_entry_bytes<N>();
+    const long long b = *reinterpret_cast<const long long *>(e);
+    const double2 *A = reinterpret_cast<const double2 *>(e + 16);
+    fallback_fp64_src<DenseSource, true>(DenseSource{A, N}, 0, N, M, LDS, hold, lane, b, logabs,
+                                         phase, parity, status, LUFQHE_ST_FALLBACK, &cs);
+  }
+}
+
 // the bulk-copy staging for complex128 matrices in device memory only
 inline int bulk_for(const DenseSource &s) { return g_bulk_loads && is_device_memory(s.A); }
 template <class S>
@@ -482,11 +549,14 @@ struct CallState {
   unsigned int *pend = nullptr;
   unsigned char *refine = nullptr;
   double2 *spill = nullptr;
+  unsigned char *corr = nullptr;
 
-  int acquire(size_t pend_cap, size_t refine_bytes, size_t spill_bytes, cudaStream_t stream) {
+  int acquire(size_t pend_cap, size_t refine_bytes, size_t spill_bytes, cudaStream_t stream,
+              size_t corr_bytes = 0) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t pend_bytes = up(pend_cap * sizeof(unsigned int));
-    const size_t total = kHeadBytes + pend_bytes + up(refine_bytes) + up(spill_bytes);
+    const size_t total =
+        kHeadBytes + pend_bytes + up(refine_bytes) + up(spill_bytes) + up(corr_bytes);
     int rc = lib_malloc_async((void **)&block, total, stream);
     if (rc) return rc;
     head = reinterpret_cast<CallHead *>(block);
@@ -496,6 +566,8 @@ struct CallState {
     refine = refine_bytes ? p : nullptr;
     p += up(refine_bytes);
     spill = spill_bytes ? reinterpret_cast<double2 *>(p) : nullptr;
+    p += up(spill_bytes);
+    corr = corr_bytes ? p : nullptr;
     return check_cuda(cudaMemsetAsync(block, 0, kHeadBytes, stream), "memset(call state)");
   }
   int release(cudaStream_t stream, int rc) {
@@ -593,9 +665,16 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     refine_bytes = (size_t)refine_cap * refine_entry_bytes<N>();
   }
   const size_t spill_bytes = inplace ? (size_t)grid * warps * N * N * sizeof(double2) : 0;
+  // the host-link variant's correction list (sizes with a corrected FP64 route)
+  long long corr_cap = 0;
+  if (inplace && N >= kCorrectMinN) {
+    corr_cap = std::max<long long>(256, (long long)(kCorrShare * (double)batch));
+    corr_cap = std::min<long long>(corr_cap, batch);
+  }
   CallState cs;
   if (two_pass || inplace || needs_counter(batch, (long long)grid * warps)) {
-    rc = cs.acquire(two_pass ? (size_t)batch : 0, refine_bytes, spill_bytes, stream);
+    rc = cs.acquire(two_pass ? (size_t)batch : 0, refine_bytes, spill_bytes, stream,
+                    (size_t)corr_cap * corr_entry_bytes<N>());
     if (rc) return cs.release(stream, rc);
   }
   // in-place kernels: refine_cap says whether the refinement is on
@@ -604,11 +683,33 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     KernelTimer timer(inplace ? "lup_mixed_tile_kernel_hostlink" : "lup_mixed_tile_kernel", N,
                       stream);
     kern<<<grid, warps * 32, smem, stream>>>(src, batch, theta2, fp64_share_64k(N), cs.head, cs.pend,
-                                             cs.spill, cs.refine, refine_cap, bulk_for(src),
-                                             logabs, phase, parity, status);
+                                             cs.spill, cs.refine, refine_cap, cs.corr, corr_cap,
+                                             bulk_for(src), logabs, phase, parity, status);
     timer.stop();
   }
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
+  if (!rc && corr_cap > 0) {
+    if constexpr (N >= kCorrectMinN) {
+      auto ck = lup_mixed_correct_kernel<N>;
+      const size_t cper = fallback_smem_per_warp(N);
+      int cw = (int)(device_smem_optin() / cper);
+      cw = std::max(1, std::min(cw, kFallbackMaxWarps));
+      const size_t csmem = cper * cw;
+      rc = check_cuda(cudaFuncSetAttribute(ck, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)csmem),
+                      "cudaFuncSetAttribute(mixed correct)");
+      if (!rc) {
+        // one CTA per SM: the list's length is known only on the device
+        const long long want = (corr_cap + cw - 1) / cw;
+        const int cgrid = (int)std::min<long long>(want, (long long)device_sm_count());
+        KernelTimer timer("lup_mixed_correct_kernel", N, stream);
+        ck<<<cgrid, cw * 32, csmem, stream>>>(cs.head, cs.corr, corr_cap, logabs, phase, parity,
+                                              status);
+        timer.stop();
+        rc = check_cuda(cudaGetLastError(), "lup_mixed_correct_kernel launch");
+      }
+    }
+  }
   // the refinements and the FP64 refactorisations, side by side in one kernel
   if (!rc && two_pass) {
     if constexpr (N >= kDeferMinN) {
