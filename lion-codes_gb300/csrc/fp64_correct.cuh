@@ -9,11 +9,11 @@
 // which is what this step adds back. Two parts:
 //  * R exactly: every product of two doubles is an exact integer of at most
 //    106 bits; the terms of one entry (A'_ij and the products L_ik U_kj) are
-//    summed in a signed 128-bit fixed-point accumulator (two 64-bit words)
-//    whose grid lies 114 bits below its largest term, so R_ij is exact up to the final rounding
-//    to double (terms more than 2^114 below the largest are dropped, far
-//    below R's own size). This is integer work (the ALU and IMAD pipes), not
-//    FP64 work, whose pipe is the narrow one on this GPU.
+//    summed modulo 2^64 on a fixed-point grid placed from the backward-error
+//    bound of the factorisation (mod_mac below), so R_ij comes out exact up
+//    to the final rounding to double (and a truncation 2^-45 below its
+//    typical size). This is integer work (the ALU and IMAD pipes), not FP64
+//    work, whose pipe is the narrow one on this GPU.
 //  * E, to a few digits, by FP32 triangular solves in the row- and
 //    column-scaled frame D_r PA D_c = (D_r L D_r^-1)(D_r U D_c) (powers of
 //    two from the rows of PA and the columns of D_r PA), where every quantity
@@ -52,85 +52,30 @@ __device__ __forceinline__ int exp_field(double x) {
 }
 __device__ __forceinline__ int exp_field_c(double2 v) { return max(exp_field(v.x), exp_field(v.y)); }
 
-// Signed 128-bit fixed-point accumulator as two 64-bit words (two's
-// complement), with the few operations the residual needs written on the
-// words: the compiler's generic 128-bit arithmetic is far slower.
-struct Acc128 {
-  unsigned long long lo;
-  long long hi;
-};
-
-// (hi, lo) = m1 m2, exact (m1, m2 < 2^53)
-__device__ __forceinline__ void mul_53x53(unsigned long long m1, unsigned long long m2,
-                                          unsigned long long &hi, unsigned long long &lo) {
-  lo = m1 * m2;
-  hi = __umul64hi(m1, m2);
+// R_ij is small next to the terms that produce it: LUP with partial pivoting
+// is backward stable, |R_ij| <= n u sum_k |L_ik| |U_kj| <= n^2 2^-53 2^T for
+// terms below 2^T. So the terms are summed in a 64-bit accumulator modulo
+// 2^64 on a grid 2^(T - 103): the bits of every term above the window cancel
+// exactly (the sum's are known to be zero), and the result, below
+// 2^(T - 43) for n <= 32, is the accumulator read as a signed integer (3
+// bits of margin); truncating each term below the grid costs at most n grid
+// units, 2^-45 of a typical |R_ij|. T is the top-bit position of the entry's
+// largest term, found by an exponent pass first.
+//
+// acc += (-1)^neg (m1 m2 >> r) mod 2^64, r >= 0 (m1, m2 < 2^53)
+__device__ __forceinline__ void mod_mac(unsigned long long &acc, unsigned long long m1,
+                                        unsigned long long m2, int r, bool neg) {
+  const unsigned long long lo = m1 * m2, hi = __umul64hi(m1, m2);
+  const int rr = min(r, 127);
+  const unsigned long long v =
+      rr >= 64 ? (hi >> (rr - 64)) : ((lo >> rr) | ((hi << 1) << (63 - rr)));
+  acc = neg ? acc - v : acc + v;
 }
-
-// acc += (-1)^neg (hi, lo) 2^sh for sh <= 8 and (hi, lo) < 2^106; bits below
-// the grid dropped. Branch-free (selects only): the lanes of a warp shift by
-// different amounts, and branches on them would split the warp.
-__device__ __forceinline__ void acc_add_shifted(Acc128 &acc, unsigned long long hi,
-                                                unsigned long long lo, int sh, bool neg) {
-  // pre-shift by 8 (at most 114 bits), then a right shift by r = 8 - sh >= 0
-  hi = (hi << 8) | (lo >> 56);
-  lo <<= 8;
-  const int r = min(8 - sh, 128);
-  const bool big = r >= 64;
-  const int rr = big ? min(r - 64, 63) : r;
-  unsigned long long nlo = big ? (hi >> rr) : ((lo >> rr) | ((hi << 1) << (63 - rr)));
-  unsigned long long nhi = big ? 0ull : (hi >> rr);
-  nlo = r >= 128 ? 0ull : nlo;
-  // two's complement of the term when it is subtracted
-  const unsigned long long clo = ~nlo + 1ull;
-  const unsigned long long chi = ~nhi + (clo == 0ull ? 1ull : 0ull);
-  nlo = neg ? clo : nlo;
-  nhi = neg ? chi : nhi;
-  const unsigned long long slo = acc.lo + nlo;
-  acc.hi = (long long)((unsigned long long)acc.hi + nhi + (slo < nlo ? 1ull : 0ull));
-  acc.lo = slo;
-}
-
-// acc += (-1)^neg a b on the grid 2^(base - 2150)
-__device__ __forceinline__ void exact_mac(Acc128 &acc, const ExactDouble &a, const ExactDouble &b,
-                                          unsigned neg, int base) {
-  unsigned long long hi, lo;
-  mul_53x53(a.m, b.m, hi, lo);
-  acc_add_shifted(acc, hi, lo, a.e + b.e - base, ((a.neg ^ b.neg ^ neg) & 1u) != 0);
-}
-
-// acc += a on the same grid: the mantissa placed like a product's (m 2^53,
-// 106 bits), so the shift stays within acc_add_shifted's range (A' lies at
-// most 2^61 grid units above a product-sized term, 8 after the placement)
-__device__ __forceinline__ void exact_add(Acc128 &acc, const ExactDouble &a, int base) {
-  acc_add_shifted(acc, a.m >> 11, a.m << 53, a.e + 1075 - 53 - base, (a.neg & 1u) != 0);
-}
-
-// acc >>= s (s > 0, arithmetic), the bits below the grid dropped
-__device__ __forceinline__ void exact_rescale(Acc128 &acc, int s) {
-  if (s >= 127) {
-    acc.lo = acc.hi < 0 ? ~0ull : 0ull;
-    acc.hi = acc.hi < 0 ? -1ll : 0ll;
-  } else if (s >= 64) {
-    acc.lo = (unsigned long long)(acc.hi >> (s - 64));
-    acc.hi = acc.hi < 0 ? -1ll : 0ll;
-  } else {
-    acc.lo = (acc.lo >> s) | ((unsigned long long)acc.hi << (64 - s));
-    acc.hi >>= s;
-  }
-}
-
-// sign and magnitude apart: a negative value's two's-complement words would
-// cancel in the sum (hi = -1, lo = 2^64 - |a|)
-__device__ __forceinline__ double exact_to_double(Acc128 a) {
-  const bool neg = a.hi < 0;
-  unsigned long long lo = a.lo, hi = (unsigned long long)a.hi;
-  if (neg) {  // negate
-    lo = ~lo + 1ull;
-    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
-  }
-  const double v = fma((double)hi, 18446744073709551616.0, (double)lo);
-  return neg ? -v : v;
+// acc += (-1)^neg (m << s) mod 2^64 (s < 64; s < 0 shifts right)
+__device__ __forceinline__ void mod_add(unsigned long long &acc, unsigned long long m, int s,
+                                        bool neg) {
+  const unsigned long long v = s >= 0 ? (m << s) : (s > -64 ? (m >> -s) : 0ull);
+  acc = neg ? acc - v : acc + v;
 }
 
 __device__ __forceinline__ float2 cf_sub_mul(float2 s, float2 a, float2 b) {  // s - a b
@@ -256,9 +201,7 @@ __device__ __noinline__ void fp64_correct_warp(const Src src, long long sb, int 
   //    (m, m..n-1), then (m+1..n-1, m); it starts at entry m (2n - m) of
   //    the order), 32 at a time, so the lanes of a step do equal work and
   //    stay converged (with lanes each walking their own runs, the warp had
-  //    run the lanes one after another). The grid follows the largest term
-  //    seen so far: a larger one shifts the accumulators down, dropping bits
-  //    below the new grid.
+  //    run the lanes one after another).
   {
     for (int p0 = 0; p0 < n * n; p0 += 32) {
       const int p = p0 + lane;
@@ -271,32 +214,31 @@ __device__ __noinline__ void fp64_correct_warp(const Src src, long long sb, int 
         const int j = off < n - m ? m + off : m;
         const double2 a = source_entry(src, sb, n, perm[i], j);
         const ExactDouble ar = exact_split(a.x), ai = exact_split(a.y);
+        // exponent pass: mx = the largest e(l) + e(u) (or A's, placed like a
+        // product's), biased fields
         int mx = max(ar.e, ai.e) + 1022;
-        Acc128 re = {0ull, 0ll}, im = {0ull, 0ll};
-        exact_add(re, ar, mx - 8);
-        exact_add(im, ai, mx - 8);
         for (int k = 0; k <= m; ++k) {  // k = m: the term with L_ii = 1 (i <= j) or U_jj
+          const int el = k == i ? 1023 : exp_field_c(M[i * lds + k]);
+          mx = max(mx, el + exp_field_c(M[k * lds + j]));
+        }
+        unsigned long long re = 0ull, im = 0ull;
+        mod_add(re, ar.m, ar.e - mx + 1072, ar.neg != 0u);
+        mod_add(im, ai.m, ai.e - mx + 1072, ai.neg != 0u);
+        for (int k = 0; k <= m; ++k) {
           const double2 u = M[k * lds + j];
-          const ExactDouble ur = exact_split(u.x), ui = exact_split(u.y);
-          const int eu = max(ur.e, ui.e);
           // L_ii = 1 (k == i, a select: the lanes of a step differ here)
           const double2 l = k == i ? make_double2(1.0, 0.0) : M[i * lds + k];
+          const ExactDouble ur = exact_split(u.x), ui = exact_split(u.y);
           const ExactDouble lr = exact_split(l.x), li = exact_split(l.y);
-          const int t = max(lr.e, li.e) + eu;
-          if (t > mx) {
-            exact_rescale(re, t - mx);
-            exact_rescale(im, t - mx);
-            mx = t;
-          }
           // re -= lr ur - li ui; im -= lr ui + li ur
-          exact_mac(re, lr, ur, 1u, mx - 8);
-          exact_mac(re, li, ui, 0u, mx - 8);
-          exact_mac(im, lr, ui, 1u, mx - 8);
-          exact_mac(im, li, ur, 1u, mx - 8);
+          mod_mac(re, lr.m, ur.m, mx + 3 - lr.e - ur.e, (lr.neg ^ ur.neg ^ 1u) != 0u);
+          mod_mac(re, li.m, ui.m, mx + 3 - li.e - ui.e, (li.neg ^ ui.neg) != 0u);
+          mod_mac(im, lr.m, ui.m, mx + 3 - lr.e - ui.e, (lr.neg ^ ui.neg ^ 1u) != 0u);
+          mod_mac(im, li.m, ur.m, mx + 3 - li.e - ur.e, (li.neg ^ ur.neg ^ 1u) != 0u);
         }
-        const int sh = mx - 8 - 2150 - sr[i] - sc[j];
-        F[i * lds + j] = make_float2(__double2float_rn(ldexp(exact_to_double(re), sh)),
-                                     __double2float_rn(ldexp(exact_to_double(im), sh)));
+        const int sh = mx - 2147 - sr[i] - sc[j];
+        F[i * lds + j] = make_float2(__double2float_rn(ldexp((double)(long long)re, sh)),
+                                     __double2float_rn(ldexp((double)(long long)im, sh)));
       }
       __syncwarp();
     }

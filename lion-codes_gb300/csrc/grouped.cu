@@ -70,9 +70,10 @@ __host__ __device__ inline WarpLayout warp_layout(int nm, int nf) {
 
 template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
-                               float2 *F, double *hold, int *er, int *ec, int lane, float theta2,
-                               bool refine, unsigned int share64k, int status_or, DeferredOut &out,
-                               double *logabs, double *phase, int8_t *parity, int32_t *status) {
+                               float2 *F, double *hold, int *er, int *ec, int nm, int lane,
+                               float theta2, bool refine, unsigned int share64k, int status_or,
+                               DeferredOut &out, double *logabs, double *phase, int8_t *parity,
+                               int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
   // a group on the FP32 path has F and 2n ints (n <= nm) for the correction
@@ -114,12 +115,19 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
       fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
                     LUFQHE_ST_FALLBACK, &cs);
   } else {
+    // a mixed plan's FP64 route (status_or set) gets the correction where the
+    // batched mixed mode does; its pass reserves the scratch (nm >= n)
+    const bool correct = MODE == LUFQHE_MODE_PLAIN_FP64_FUSED && status_or != 0 && nm >= n &&
+                         n >= kCorrectMinN && n <= 32;
     int par = 0;
-    int st = MODE == LUFQHE_MODE_PLAIN_FP64 ? lup_fp64_warp<ARITH_REF>(M, lds, hold, n, lane, &par)
-                                            : lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par);
+    int st = MODE == LUFQHE_MODE_PLAIN_FP64
+                 ? lup_fp64_warp<ARITH_REF>(M, lds, hold, n, lane, &par)
+                 : lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par,
+                                              correct ? er : nullptr);
     double la, ph;
     if (st == 0) {
       logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+      if (correct) fp64_correct_warp(DenseSource{src, lda}, 0, n, M, lds, cs, lane, &la, &ph);
     } else if (st == LUFQHE_ST_SINGULAR) {
       la = -INFINITY;
       ph = 0.0;
@@ -167,8 +175,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, lane, theta2, refine != 0, w.share64k, w.status_or, out, logabs,
-                           phase, parity, status);
+                           ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, out,
+                           logabs, phase, parity, status);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
@@ -374,6 +382,10 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
     if (G.count == 0 || pass_of(p, g) != pass) continue;
     L.nf = std::max(L.nf, G.n);
     if (L.mode == LUFQHE_MODE_MIXED) L.nm = std::max(L.nm, G.n);
+    // a mixed plan's FP64 route with corrected sizes: the correction's
+    // scratch (the FP32 path's F and ints) in the layout
+    if (pass == 1 && p->mode == LUFQHE_MODE_MIXED && G.n >= kCorrectMinN && G.n <= 32)
+      L.nm = std::max(L.nm, G.n);
   }
   L.warps = warps;
   L.ctas = 0;

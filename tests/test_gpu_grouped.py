@@ -45,16 +45,18 @@ def test_plan_matches_batched_calls(cuda, lufqhe_mod, mode, autotune):
     old_share = lib.lufqhe_get_option(3)
     lib.lufqhe_set_option(3, 0.0)       # batched mixed results with no FP64 routing
     refs = [host(lufqhe_mod.batch_lup_det(A, mode=mode)) for A, _ in groups]
+    lib.lufqhe_set_option(3, 1.0)       # and with every matrix routed to the FP64 routine
+    routed_refs = [host(lufqhe_mod.batch_lup_det(A, mode=mode)) for A, _ in groups]
     lib.lufqhe_set_option(3, old_share)
-    for (A, off), ref in zip(groups, refs):
-        fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
+    for (A, off), ref, rref in zip(groups, refs, routed_refs):
         sl = slice(off, off + A.shape[0])
         # the tuner may send a size to the FP64 routine (status FP64): those
-        # results are the fused FP64 ones; the rest match the batched call
+        # results are the batched call's routed ones (the fused FP64 result,
+        # corrected for 17 <= n <= 32); the rest match the batched call
         routed = (got["status"][sl] & lufqhe_mod.ST_FP64) != 0
         for k in ("logabs", "phase", "parity"):
             a = np.ascontiguousarray(got[k][sl])
-            b = np.where(routed, fused[k], ref[k]) if mode == lufqhe_mod.MODE_MIXED else ref[k]
+            b = np.where(routed, rref[k], ref[k]) if mode == lufqhe_mod.MODE_MIXED else ref[k]
             same = (a == b) | (np.isnan(a) & np.isnan(b))
             assert same.all(), (k, A.shape[1])
     desc = plan.describe()
@@ -165,3 +167,38 @@ def test_plan_on_host_buffers(cuda, lufqhe_mod, autotune):
         assert np.array_equal(out_h.logabs.numpy()[o:o + H.shape[0]], ref["logabs"], equal_nan=True)
     plan.close()
     plan_h.close()
+
+
+def test_config4_full_plan_against_double_double(cuda, lufqhe_mod, oracle):
+    """The full config-4 batch (200000 LLL matrices, n uniform over 6..48,
+    seed 4) through an autotuned mixed plan, every result against the
+    double-double oracle: within 1e-10 (relative to max(1, |log|det||), in
+    log|det| and phase) for every n <= 32, whatever route the tuner picks;
+    n = 48, the FP64 route without a correction (FP64 LUP itself misses 1e-10
+    on about 1% of these matrices), equal to the fused FP64 kernel bit for bit."""
+    rng = np.random.default_rng(4)
+    counts = rng.multinomial(200000, [1.0 / len(SIZES)] * len(SIZES))
+    groups, off = [], 0
+    for n, c in zip(SIZES, counts):
+        A, _ = lufqhe_mod.gen_lll(int(c), n, seed=4 * 100 + n, sigma=math.sqrt(n))
+        groups.append((A, off))
+        off += int(c)
+    out = alloc(lufqhe_mod, cuda, off)
+    plan = lufqhe_mod.Plan(groups, out, mode=lufqhe_mod.MODE_MIXED, autotune=True)
+    plan.execute()
+    cuda.cuda.synchronize()
+    got = host(out)
+    plan.close()
+    for (A, o), n in zip(groups, SIZES):
+        sl = slice(o, o + A.shape[0])
+        la, ph = got["logabs"][sl], got["phase"][sl]
+        if n <= 32:
+            want, wph, _ = oracle.logdet_dd(A.cpu().numpy())
+            scale = np.maximum(1.0, np.abs(want))
+            err = np.maximum(np.abs(la - want), np.abs(np.angle(np.exp(1j * (ph - wph))))) / scale
+            assert err.max() < 1e-10, (n, float(err.max()), int((err > 1e-10).sum()))
+        else:
+            fused = host(lufqhe_mod.batch_lup_det(A, mode=lufqhe_mod.MODE_PLAIN_FP64_FUSED))
+            assert np.array_equal(la, fused["logabs"], equal_nan=True)
+            assert np.array_equal(ph, fused["phase"], equal_nan=True)
+        del A
