@@ -106,6 +106,36 @@ int lufqhe_lll_det(const void *d_z, int n, long long batch, int mode, double *d_
                    double *d_phase, int8_t *d_parity, int32_t *d_status, void *stream);
 
 /*
+ * Determinants of composite-fermion (CF) matrices built inside the
+ * factorising kernels: one configuration of np particles (host arrays phi,
+ * theta of np angles) and a batch of permutations (d_perm: batch rows of
+ * perm_stride int16, the first n of each a 1-based particle list). Row r of
+ * matrix b belongs to particle p = perm[r] - 1, with
+ *   u_p = (cos theta cos phi, cos theta sin phi), v_p = (sin theta cos phi, -sin theta sin phi),
+ *   Q = (n - 3) / 2 (n odd), a table T[p][Q+1] = (cos theta sin theta)^Q,
+ *   T[p][Q+1+j] = T[p][Q+j] u_p / v_p, T[p][Q+1-j] = T[p][Q+2-j] v_p / u_p;
+ *   columns c < n - 2: T[p][c];
+ *   column n - 2: T[p][Q+1+mu] sum_{s != r} (k1 u_p v_q + k2 u_q v_p) / (u_p v_q - u_q v_p);
+ *   column n - 1: T[p][Q+1+nu] sum_{s != r} (r1 u_p v_q + r2 u_q v_p) / (u_p v_q - u_q v_p),
+ *   q = perm[s] - 1.
+ * This is the reference's compiled-out matrix-element builder
+ * (mkMatrixElements, LU-fqhe/src/mkMatrixElements.cu:46-50, 169-358, same
+ * argument order) followed by LUCoreGPU::CALL, in FP64 and with each of the
+ * last two columns taking its own term (the reference's column masks are
+ * commented out, :251 and :285, which makes the two columns equal). Needs
+ * n odd in [3, 64], np in [n, 32767], perm_stride >= n and Q+1+mu, Q+1+nu in
+ * [0, n). A permutation entry outside 1..np, or a repeated particle, gives
+ * status LUFQHE_ST_NONFINITE for that matrix. Modes and outputs as
+ * lufqhe_batch_lup_det; d_perm and the outputs may be page-locked host memory.
+ * The tables are uploaded from pageable memory, which orders the call after
+ * the stream's earlier work; the call cannot be captured into a graph.
+ */
+int lufqhe_cf_det(const double *phi, const double *theta, int np, int n, double k1, double k2,
+                  double r1, double r2, int mu, int nu, const int16_t *d_perm, int perm_stride,
+                  long long batch, int mode, double *d_logabs, double *d_phase, int8_t *d_parity,
+                  int32_t *d_status, void *stream);
+
+/*
  * Same call on HOST buffers: the batch and the four result arrays are in host
  * memory. Replaces the copy-in / LUCoreGPU::CALL / copy-out sequence of the
  * reference's Monte Carlo loop (LU-fqhe/src/MonteCarloLoop.cu:316-329).
@@ -340,6 +370,18 @@ int lufqhe_gen_gaussian(double *d_A, int n, int lda, long long batch, unsigned l
  * z_i complex Gaussian with E|z|^2 = sigma^2 (d_z receives the z_i, may be NULL). */
 int lufqhe_gen_lll(double *d_A, double *d_z, int n, int lda, long long batch,
                    unsigned long long seed, double sigma, void *stream);
+/* The CF matrices of lufqhe_cf_det written out (the reference's makeMatrices
+ * kernel, LU-fqhe/src/mkMatrixElements.cu:295-358): matrix b at
+ * d_A + b*n*lda, row stride lda, dtype LUFQHE_C128 or LUFQHE_C64 (rounded
+ * from the FP64 entries). lufqhe_cf_det's results equal lufqhe_batch_lup_det's
+ * on the complex128 matrices bit for bit. */
+int lufqhe_gen_cf(const double *phi, const double *theta, int np, int n, double k1, double k2,
+                  double r1, double r2, int mu, int nu, const int16_t *d_perm, int perm_stride,
+                  long long batch, void *d_A, int lda, int dtype, void *stream);
+/* Host: the per-configuration tables those calls upload: uv = u[0..np) then
+ * v[0..np) (2 np complex128), tab = T (np x n complex128). */
+int lufqhe_cf_tables(const double *phi, const double *theta, int np, int n, double *uv,
+                     double *tab);
 
 /* Same generators on the host (bit-identical draws; libm's exp/sin/cos/log may
  * differ from the device's in the last place). */

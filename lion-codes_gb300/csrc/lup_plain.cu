@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "bulk_copy.cuh"
+#include "cf_source.cuh"
 #include "fp64_correct.cuh"
 #include "lup_fp64.cuh"
 
@@ -295,6 +296,13 @@ int launch_plain_lll(const double2 *Z, int n, long long batch, int arith, double
                      int status_or) {
   return launch_plain_src(LllSource{Z}, static_cast<double2 *>(nullptr), n, n, batch, arith,
                           logabs, phase, parity, status, stream, status_or);
+}
+
+int launch_plain_cf(const CfSource &src, int n, long long batch, int arith, double *logabs,
+                    double *phase, int8_t *parity, int32_t *status, cudaStream_t stream,
+                    int status_or) {
+  return launch_plain_src(src, static_cast<double2 *>(nullptr), n, n, batch, arith, logabs, phase,
+                          parity, status, stream, status_or);
 }
 
 template <class T>

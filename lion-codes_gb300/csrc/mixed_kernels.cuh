@@ -730,6 +730,13 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
 }
 
 // plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
+// Sources whose matrices are always of odd order (CF matrices, n = 2Q + 3)
+// never reach the register-tiled kernels, which exist for even n only.
+template <class S, class = void>
+struct has_even_n : std::true_type {};
+template <class S>
+struct has_even_n<S, std::void_t<decltype(S::kOddN)>> : std::false_type {};
+
 template <class Src, class PlainFn>
 int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *phase,
                      int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64,
@@ -740,14 +747,16 @@ int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *ph
   if (fp64_share_64k(n) >= 65536u)
     return plain_fp64();
   const float th2 = g_mixed_theta * g_mixed_theta;
-  switch (n) {
-    case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
-    default: break;
+  if constexpr (has_even_n<Src>::value) {
+    switch (n) {
+      case 6: return launch_mixed_tile<6>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      case 8: return launch_mixed_tile<8>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      case 12: return launch_mixed_tile<12>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      case 16: return launch_mixed_tile<16>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      case 24: return launch_mixed_tile<24>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      case 32: return launch_mixed_tile<32>(src, batch, th2, logabs, phase, parity, status, stream, inplace);
+      default: break;
+    }
   }
   const size_t per_warp = mixed_smem_per_warp(n);
   const size_t optin = device_smem_optin();

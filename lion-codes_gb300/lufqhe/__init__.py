@@ -113,6 +113,86 @@ def lll_det(z, mode: int = MODE_PLAIN_FP64, stream=None, out: DetResult | None =
     return out
 
 
+@dataclass
+class CfConfig:
+    """One composite-fermion configuration: np particle angles and the
+    parameters of the last two columns (the arguments of the reference's
+    mkMatrixElements, LU-fqhe/src/mkMatrixElements.cu:46-50)."""
+    phi: "object"
+    theta: "object"
+    k1: float
+    k2: float
+    r1: float
+    r2: float
+    mu: int
+    nu: int
+
+    def angles(self):
+        import numpy as np
+        phi = np.ascontiguousarray(self.phi, dtype=np.float64)
+        theta = np.ascontiguousarray(self.theta, dtype=np.float64)
+        if phi.ndim != 1 or phi.shape != theta.shape:
+            raise ValueError("phi and theta must be 1-D arrays of the same length")
+        return phi, theta
+
+
+def _perm_shape(perm, n):
+    import torch
+    if perm.dim() != 2 or perm.dtype != torch.int16 or not perm.is_contiguous() or \
+            not (perm.is_cuda or perm.is_pinned()):
+        raise TypeError("perm must be a contiguous (batch, stride) int16 CUDA or pinned tensor")
+    if perm.shape[1] < n:
+        raise ValueError("perm rows must hold at least n entries")
+    return perm.shape[0], perm.shape[1]
+
+
+def cf_det(cfg: CfConfig, perm, n: int, mode: int = MODE_PLAIN_FP64, stream=None,
+           out: DetResult | None = None):
+    """Determinants of the CF matrices of configuration cfg and the 1-based
+    particle lists perm[:, :n], built inside the factorising kernels."""
+    import torch
+    phi, theta = cfg.angles()
+    batch, stride = _perm_shape(perm, n)
+    if out is None:
+        dev = perm.device
+        pin = not perm.is_cuda
+        out = DetResult(*(torch.empty(batch, dtype=d, device=dev, pin_memory=pin)
+                          for d in (torch.float64, torch.float64, torch.int8, torch.int32)))
+    rc = lib().lufqhe_cf_det(phi.ctypes.data, theta.ctypes.data, phi.size, n, cfg.k1, cfg.k2,
+                             cfg.r1, cfg.r2, cfg.mu, cfg.nu, perm.data_ptr(), stride, batch, mode,
+                             out.logabs.data_ptr(), out.phase.data_ptr(), out.parity.data_ptr(),
+                             out.status.data_ptr(), _stream_ptr(stream))
+    _native.check(rc, "lufqhe_cf_det")
+    return out
+
+
+def gen_cf(cfg: CfConfig, perm, n: int, lda: int | None = None, dtype=None, stream=None):
+    """The CF matrices of cf_det written out: a (batch, n, lda) tensor."""
+    import torch
+    phi, theta = cfg.angles()
+    batch, stride = _perm_shape(perm, n)
+    lda = n if lda is None else lda
+    dtype = torch.complex128 if dtype is None else dtype
+    A = torch.zeros(batch, n, lda, dtype=dtype, device=perm.device)
+    rc = lib().lufqhe_gen_cf(phi.ctypes.data, theta.ctypes.data, phi.size, n, cfg.k1, cfg.k2,
+                             cfg.r1, cfg.r2, cfg.mu, cfg.nu, perm.data_ptr(), stride, batch,
+                             A.data_ptr(), lda, _dtype_code(A), _stream_ptr(stream))
+    _native.check(rc, "lufqhe_gen_cf")
+    return A
+
+
+def cf_tables(cfg: CfConfig, n: int):
+    """The host tables the CF calls upload: (uv (2, np), tab (np, n)) complex128."""
+    import numpy as np
+    phi, theta = cfg.angles()
+    uv = np.empty((2, phi.size), dtype=np.complex128)
+    tab = np.empty((phi.size, n), dtype=np.complex128)
+    rc = lib().lufqhe_cf_tables(phi.ctypes.data, theta.ctypes.data, phi.size, n, uv.ctypes.data,
+                                tab.ctypes.data)
+    _native.check(rc, "lufqhe_cf_tables")
+    return uv, tab
+
+
 def batch_lup_det_host(A, mode: int = MODE_PLAIN_FP64, stream=None,
                        out: DetResult | None = None) -> DetResult:
     """Determinants of a (batch, n, lda) complex128 tensor in HOST memory, results

@@ -24,6 +24,8 @@ SIGNATURES = {
     "lufqhe_batch_lup_det": (I32, [P, I32, I32, I64, I32, I32, P, P, P, P, P]),
     "lufqhe_batch_lup_det_host": (I32, [P, I32, I32, I64, I32, I32, P, P, P, P, P]),
     "lufqhe_lll_det": (I32, [P, I32, I64, I32, P, P, P, P, P]),
+    "lufqhe_cf_det": (I32, [P, P, I32, I32, F64, F64, F64, F64, I32, I32, P, I32, I64, I32, P, P,
+                            P, P, P]),
     "lufqhe_batch_lup_factor_inplace": (I32, [P, I32, I32, I64, I32, P, P, P, P, P]),
     "lufqhe_lucoregpu_call": (I32, [P, I32, I32, I32, I32, P]),
     "lufqhe_lucoregpu_call_noalloc": (I32, [P, I32, I32, I32, I32, P]),
@@ -49,6 +51,9 @@ SIGNATURES = {
     "lufqhe_read_matrices_f32": (I64, [_c.c_char_p, I32, I64, I64, I32, P]),
     "lufqhe_gen_gaussian": (I32, [P, I32, I32, I64, U64, F64, P]),
     "lufqhe_gen_lll": (I32, [P, P, I32, I32, I64, U64, F64, P]),
+    "lufqhe_gen_cf": (I32, [P, P, I32, I32, F64, F64, F64, F64, I32, I32, P, I32, I64, P, I32,
+                            I32, P]),
+    "lufqhe_cf_tables": (I32, [P, P, I32, I32, P, P]),
     "lufqhe_gen_gaussian_host": (I32, [P, I32, I32, I64, U64, F64]),
     "lufqhe_gen_lll_host": (I32, [P, P, I32, I32, I64, U64, F64]),
     "lufqhe_set_option": (I32, [I32, F64]),

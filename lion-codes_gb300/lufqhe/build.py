@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 SOURCES = ["capi.cu", "lup_plain.cu", "lup_mixed.cu", "lup_mixed_c64.cu", "gen.cu", "probe.cu", "noalloc.cu", "grouped.cu", "serve.cu", "pairsum.cu", "fileio.cu", "hostpipe.cu",
-           "host_reduce.cu"]
+           "host_reduce.cu", "cf.cu"]
 
 
 def _nvcc() -> str:
