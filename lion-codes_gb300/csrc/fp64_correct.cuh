@@ -1,5 +1,6 @@
-// Extended-precision correction of an FP64 LUP log-determinant (n <= 32, one
-// warp), for the results of the mixed mode's FP64 route.
+// Extended-precision correction of an FP64 LUP log-determinant (n <= 32 by
+// one warp, up to kCorrectMaxN by a warp group or one warp), for the results
+// of the mixed mode's FP64 route.
 //
 // FP64 LUP on ill-conditioned orbital matrices misses 1e-10 in log|det| on a
 // tail of the batch (about 1 in 10^4 matrices at n = 24, 2 in 10^3 at
@@ -147,8 +148,68 @@ __device__ __forceinline__ double2 source_entry(const LllSource &s, long long b,
 
 // The FP64 route's error on ill-conditioned orbital matrices grows with n: at
 // n <= 16 it stays two orders of magnitude inside the bound, so the small
-// register-tiled kernels carry no correction code.
+// register-tiled kernels carry no correction code. Above n = 40 the scaled
+// factors of the worst LLL matrices (z ~ CN(0, n)) are too ill-conditioned
+// for the FP32 solves: on GB300, 8192 matrices per size, the correction took
+// the results above 1e-10 from 7 to 0 at n = 33 and 38 to 2 at n = 40, but
+// only 75 to 45 at n = 48 and 120 to 119 at n = 64, at 2.5-3x the cost of
+// the factorisation; those sizes are left uncorrected.
 constexpr int kCorrectMinN = 17;
+constexpr int kCorrectMaxN = 40;
+
+// Grid of the residual sums: 2^(T - 106 + bias) for an entry whose largest
+// term is below 2^T. |R_ij| <= n^2 2^-53 2^T is n^2 2^(53 - bias) grid units,
+// so the sum read as a signed 64-bit integer keeps 3 bits of margin with
+// bias 3 for n <= 32 and bias 5 for n <= 64.
+constexpr int kGridBias32 = 3;
+constexpr int kGridBias64 = 5;
+
+// Entry p of the level order (see fp64_correct_warp, step 2): R_ij = (PA -
+// LU)_ij summed exactly modulo 2^64 on the grid, then scaled by the row and
+// column scales into F[i * lds + j].
+template <class Src>
+__device__ __forceinline__ void residual_entry(const Src &src, long long sb, int n,
+                                               const double2 *M, int lds, const int *perm,
+                                               const int *sr, const int *sc, int p, int bias,
+                                               float2 *F) {
+  int m = (int)((float)n - sqrtf((float)(n * n - p)));
+  while (m > 0 && m * (2 * n - m) > p) --m;
+  while ((m + 1) * (2 * n - m - 1) <= p) ++m;
+  const int off = p - m * (2 * n - m);
+  const int i = off < n - m ? m : m + 1 + (off - (n - m));
+  const int j = off < n - m ? m + off : m;
+  const double2 a = source_entry(src, sb, n, perm[i], j);
+  const ExactDouble ar = exact_split(a.x), ai = exact_split(a.y);
+  // exponent pass: mx = the largest e(l) + e(u) (or A's, placed like a
+  // product's), biased fields
+  int mx = max(ar.e, ai.e) + 1022;
+  for (int k = 0; k <= m; ++k) {  // k = m: the term with L_ii = 1 (i <= j) or U_jj
+    const int el = k == i ? 1023 : exp_field_c(M[i * lds + k]);
+    mx = max(mx, el + exp_field_c(M[k * lds + j]));
+  }
+  // grid unit 2^g, g = mx - 2150 + bias: a product m1 m2 2^(e1 + e2 - 2150)
+  // is shifted right by g - (e1 + e2 - 2150), A's m 2^(e - 1075) left by
+  // (e - 1075) - g
+  unsigned long long re = 0ull, im = 0ull;
+  mod_add(re, ar.m, ar.e - mx + 1075 - bias, ar.neg != 0u);
+  mod_add(im, ai.m, ai.e - mx + 1075 - bias, ai.neg != 0u);
+  for (int k = 0; k <= m; ++k) {
+    const double2 u = M[k * lds + j];
+    // L_ii = 1 (k == i, a select: the lanes of a step differ here)
+    const double2 l = k == i ? make_double2(1.0, 0.0) : M[i * lds + k];
+    const ExactDouble ur = exact_split(u.x), ui = exact_split(u.y);
+    const ExactDouble lr = exact_split(l.x), li = exact_split(l.y);
+    // re -= lr ur - li ui; im -= lr ui + li ur
+    const int r0 = mx + bias;
+    mod_mac(re, lr.m, ur.m, r0 - lr.e - ur.e, (lr.neg ^ ur.neg ^ 1u) != 0u);
+    mod_mac(re, li.m, ui.m, r0 - li.e - ui.e, (li.neg ^ ui.neg) != 0u);
+    mod_mac(im, lr.m, ui.m, r0 - lr.e - ui.e, (lr.neg ^ ui.neg ^ 1u) != 0u);
+    mod_mac(im, li.m, ur.m, r0 - li.e - ur.e, (li.neg ^ ur.neg ^ 1u) != 0u);
+  }
+  const int sh = mx - 2150 + bias - sr[i] - sc[j];
+  F[i * lds + j] = make_float2(__double2float_rn(ldexp((double)(long long)re, sh)),
+                               __double2float_rn(ldexp((double)(long long)im, sh)));
+}
 
 // Shared memory the correction borrows from its caller: F (n x lds float2),
 // ints (2n: the pivot order, then the row scale exponents) and hold (2n
@@ -202,46 +263,10 @@ __device__ __noinline__ void fp64_correct_warp(const Src src, long long sb, int 
   //    the order), 32 at a time, so the lanes of a step do equal work and
   //    stay converged (with lanes each walking their own runs, the warp had
   //    run the lanes one after another).
-  {
-    for (int p0 = 0; p0 < n * n; p0 += 32) {
-      const int p = p0 + lane;
-      if (p < n * n) {
-        int m = (int)((float)n - sqrtf((float)(n * n - p)));
-        while (m > 0 && m * (2 * n - m) > p) --m;
-        while ((m + 1) * (2 * n - m - 1) <= p) ++m;
-        const int off = p - m * (2 * n - m);
-        const int i = off < n - m ? m : m + 1 + (off - (n - m));
-        const int j = off < n - m ? m + off : m;
-        const double2 a = source_entry(src, sb, n, perm[i], j);
-        const ExactDouble ar = exact_split(a.x), ai = exact_split(a.y);
-        // exponent pass: mx = the largest e(l) + e(u) (or A's, placed like a
-        // product's), biased fields
-        int mx = max(ar.e, ai.e) + 1022;
-        for (int k = 0; k <= m; ++k) {  // k = m: the term with L_ii = 1 (i <= j) or U_jj
-          const int el = k == i ? 1023 : exp_field_c(M[i * lds + k]);
-          mx = max(mx, el + exp_field_c(M[k * lds + j]));
-        }
-        unsigned long long re = 0ull, im = 0ull;
-        mod_add(re, ar.m, ar.e - mx + 1072, ar.neg != 0u);
-        mod_add(im, ai.m, ai.e - mx + 1072, ai.neg != 0u);
-        for (int k = 0; k <= m; ++k) {
-          const double2 u = M[k * lds + j];
-          // L_ii = 1 (k == i, a select: the lanes of a step differ here)
-          const double2 l = k == i ? make_double2(1.0, 0.0) : M[i * lds + k];
-          const ExactDouble ur = exact_split(u.x), ui = exact_split(u.y);
-          const ExactDouble lr = exact_split(l.x), li = exact_split(l.y);
-          // re -= lr ur - li ui; im -= lr ui + li ur
-          mod_mac(re, lr.m, ur.m, mx + 3 - lr.e - ur.e, (lr.neg ^ ur.neg ^ 1u) != 0u);
-          mod_mac(re, li.m, ui.m, mx + 3 - li.e - ui.e, (li.neg ^ ui.neg) != 0u);
-          mod_mac(im, lr.m, ui.m, mx + 3 - lr.e - ui.e, (lr.neg ^ ui.neg ^ 1u) != 0u);
-          mod_mac(im, li.m, ur.m, mx + 3 - li.e - ur.e, (li.neg ^ ur.neg ^ 1u) != 0u);
-        }
-        const int sh = mx - 2147 - sr[i] - sc[j];
-        F[i * lds + j] = make_float2(__double2float_rn(ldexp((double)(long long)re, sh)),
-                                     __double2float_rn(ldexp((double)(long long)im, sh)));
-      }
-      __syncwarp();
-    }
+  for (int p0 = 0; p0 < n * n; p0 += 32) {
+    const int p = p0 + lane;
+    if (p < n * n) residual_entry(src, sb, n, M, lds, perm, sr, sc, p, kGridBias32, F);
+    __syncwarp();
   }
   // 3. the scaled factors in FP32, in place over M (entry q of the float2
   //    view overlaps entry q/2 of the double2 view, which an earlier chunk, or
@@ -322,6 +347,153 @@ __device__ __noinline__ void fp64_correct_warp(const Src src, long long sb, int 
     *ph += dy;
   }
   __syncwarp();
+}
+
+// Barrier of a single warp, for fp64_correct_group run by one warp.
+struct WarpBarrier {
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+};
+
+// The same correction by the nthr threads of a warp group (a multiple of 32,
+// synchronised by bar, as in lup_fp64_group), or by one warp (WarpBarrier),
+// for 32 < n <= kCorrectMaxN (n <= 64 fits its grid), on FP64 factors of
+// either routine. red: 4 floats of
+// shared scratch per warp (unused, and may be null, for one warp).
+// Returns the correction to add to (log|det|, phase), the same value in every
+// thread, or (0, 0) if a scaled quantity left float's range. The steps are
+// those of fp64_correct_warp with rows, columns and residual entries dealt
+// over the group; the column scales are reduced per warp, then across warps
+// with shared atomics.
+template <class Src, class Bar>
+__device__ __noinline__ double2 fp64_correct_group(const Src src, long long sb, int n,
+                                                   double2 *M, int lds, const CorrScratch cs,
+                                                   int tid, int nthr, Bar bar, float *red) {
+  float2 *const F = cs.F;
+  const int *perm = cs.ints;
+  int *sr = cs.ints + n;
+  float2 *rd = reinterpret_cast<float2 *>(cs.hold);
+  int *sc = reinterpret_cast<int *>(rd + n);
+  const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+  // 1. scales
+  for (int j = tid; j < n; j += nthr) sc[j] = -4000;
+  for (int i = tid; i < n; i += nthr) {
+    auto it = source_row(src, sb, n, perm[i]);
+    int er = -2000;
+    for (int j = 0; j < n; ++j) er = max(er, exp_field_c(it.next()) - 1023);
+    sr[i] = er;
+  }
+  bar.sync();
+  for (int i0 = 0; i0 < n; i0 += nthr) {
+    if (i0 + warp * 32 >= n) continue;  // warp-uniform: no row of this warp
+    const int i = i0 + tid;
+    const bool live = i < n;
+    auto it = source_row(src, sb, n, perm[live ? i : i0]);
+    const int er = live ? sr[i] : 0;
+    for (int j = 0; j < n; ++j) {
+      const int c = __reduce_max_sync(kFull, live ? exp_field_c(it.next()) - 1023 - er : -4000);
+      if (lane == 0) atomicMax(&sc[j], c);
+    }
+  }
+  bar.sync();
+  // 2. R = PA - LU exactly, scaled into F, level-dealt over the group
+  for (int p0 = 0; p0 < n * n; p0 += nthr) {
+    const int p = p0 + tid;
+    if (p < n * n)
+      residual_entry(src, sb, n, M, lds, perm, sr, sc, p, n <= 32 ? kGridBias32 : kGridBias64,
+                     F);
+    __syncwarp();
+  }
+  bar.sync();
+  // 3. the scaled factors in FP32, in place over M (reads of a chunk before
+  //    its writes, which overlap entries of this chunk or earlier ones)
+  float2 *Mf = reinterpret_cast<float2 *>(M);
+  for (int q0 = 0; q0 < n * lds; q0 += nthr) {
+    const int q = q0 + tid;
+    float2 v = make_float2(0.f, 0.f);
+    if (q < n * lds) {
+      const int i = q / lds, k = q - i * lds;
+      if (k < n) {
+        const double2 d = M[q];
+        const int sh = k < i ? sr[k] - sr[i] : -sr[i] - sc[k];
+        v = make_float2(__double2float_rn(ldexp(d.x, sh)), __double2float_rn(ldexp(d.y, sh)));
+      }
+    }
+    bar.sync();
+    if (q < n * lds) Mf[q] = v;
+    bar.sync();
+  }
+  for (int i = tid; i < n; i += nthr) {
+    const float2 d = Mf[i * lds + i];
+    const float r = 1.0f / fmaf(d.x, d.x, d.y * d.y);
+    rd[i] = make_float2(d.x * r, -d.y * r);
+  }
+  bar.sync();
+  // 4. E = U^-1 L^-1 R in the scaled frame, column j by thread j
+  for (int j = tid; j < n; j += nthr) {
+    for (int i = 1; i < n; ++i) {
+      float2 s0 = F[i * lds + j], s1 = make_float2(0.f, 0.f);
+      int k = 0;
+#pragma unroll 2
+      for (; k + 1 < i; k += 2) {
+        s0 = cf_sub_mul(s0, Mf[i * lds + k], F[k * lds + j]);
+        s1 = cf_sub_mul(s1, Mf[i * lds + k + 1], F[(k + 1) * lds + j]);
+      }
+      if (k < i) s0 = cf_sub_mul(s0, Mf[i * lds + k], F[k * lds + j]);
+      F[i * lds + j] = make_float2(s0.x + s1.x, s0.y + s1.y);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      float2 s0 = F[i * lds + j], s1 = make_float2(0.f, 0.f);
+      int k = i + 1;
+#pragma unroll 2
+      for (; k + 1 < n; k += 2) {
+        s0 = cf_sub_mul(s0, Mf[i * lds + k], F[k * lds + j]);
+        s1 = cf_sub_mul(s1, Mf[i * lds + k + 1], F[(k + 1) * lds + j]);
+      }
+      if (k < n) s0 = cf_sub_mul(s0, Mf[i * lds + k], F[k * lds + j]);
+      F[i * lds + j] = cf_mul(make_float2(s0.x + s1.x, s0.y + s1.y), rd[i]);
+    }
+  }
+  bar.sync();
+  // 5. tr E and tr E^2: per thread, per warp, then the warps in order
+  float2 t1 = make_float2(0.f, 0.f), t2 = make_float2(0.f, 0.f);
+  for (int j = tid; j < n; j += nthr) {
+    const float2 e = F[j * lds + j];
+    t1.x += e.x;
+    t1.y += e.y;
+    for (int i = 0; i < n; ++i) {
+      const float2 p = cf_mul(F[i * lds + j], F[j * lds + i]);
+      t2.x += p.x;
+      t2.y += p.y;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    t1.x += __shfl_xor_sync(kFull, t1.x, off);
+    t1.y += __shfl_xor_sync(kFull, t1.y, off);
+    t2.x += __shfl_xor_sync(kFull, t2.x, off);
+    t2.y += __shfl_xor_sync(kFull, t2.y, off);
+  }
+  float4 t = make_float4(t1.x, t1.y, t2.x, t2.y);
+  if (nw > 1) {
+    if (lane == 0) {
+      red[4 * warp] = t1.x;
+      red[4 * warp + 1] = t1.y;
+      red[4 * warp + 2] = t2.x;
+      red[4 * warp + 3] = t2.y;
+    }
+    bar.sync();
+    t = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int w = 0; w < nw; ++w) {
+      t.x += red[4 * w];
+      t.y += red[4 * w + 1];
+      t.z += red[4 * w + 2];
+      t.w += red[4 * w + 3];
+    }
+    bar.sync();
+  }
+  const double dx = (double)t.x - 0.5 * (double)t.z;
+  const double dy = (double)t.y - 0.5 * (double)t.w;
+  return (isfinite(dx) && isfinite(dy)) ? make_double2(dx, dy) : make_double2(0.0, 0.0);
 }
 
 }  // namespace lufqhe

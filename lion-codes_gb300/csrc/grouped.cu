@@ -203,13 +203,16 @@ int default_tile(int n) {
 // Warp-group form of the grouped kernel for the FP64 route at n > 32: each CTA
 // claims work items and factorises their matrices with all its threads
 // (lup_fp64_group), as the batched plain kernel does for those sizes.
-template <int ARITH>
+// CORRECT (a mixed plan's pass): the results of items with n <= nm get the
+// extended-precision correction (fp64_correct_group), as the batched mixed
+// mode's FP64 route does; its scratch (nm x (nm + 1) float2 and 2 nm ints)
+// follows the row scales.
+template <int ARITH, bool CORRECT = false>
 __global__ void __launch_bounds__(kFp64GroupWarps * 32)
     grouped_group_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter,
                          int nm, int nf, float theta2, int refine, double *__restrict__ logabs,
                          double *__restrict__ phase, int8_t *__restrict__ parity,
                          int32_t *__restrict__ status) {
-  (void)nm;
   (void)theta2;
   (void)refine;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -218,6 +221,8 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
   const int tid = threadIdx.x, nthr = blockDim.x;
   double2 *M = reinterpret_cast<double2 *>(smem_raw);
   double *hold = reinterpret_cast<double *>(M + (size_t)nf * (nf + 1));
+  float2 *F = reinterpret_cast<float2 *>(hold + 2 * nf);   // nm x (nm + 1)
+  int *ints = reinterpret_cast<int *>(F + (size_t)nm * (nm + 1));
   for (;;) {
     __syncthreads();
     if (tid == 0) item = atomicAdd(counter, 1u);
@@ -231,11 +236,14 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
       __syncthreads();
       const long long ob = w.out + j;
       int par = 0;
+      const bool correct = CORRECT && w.status_or != 0 && n <= nm;
       int st = src.load_group(w.first + j, n, M, lds, tid, nthr) ? LUFQHE_ST_NONFINITE : 0;
-      if (!st) st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par);
+      if (!st)
+        st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par, CtaBarrier(),
+                                   correct ? ints : nullptr);
       __syncthreads();
+      double la = 0.0, ph = 0.0;
       if (tid < 32) {
-        double la, ph;
         if (st == 0) {
           logdet_from_diag(M, lds, n, tid, par, &la, &ph);
         } else if (st == LUFQHE_ST_SINGULAR) {
@@ -246,18 +254,28 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
           ph = NAN;
           par = 0;
         }
-        if (tid == 0) {
-          logabs[ob] = la;
-          if (phase) phase[ob] = ph;
-          if (parity) parity[ob] = (int8_t)par;
-          if (status) status[ob] = st | w.status_or;
-        }
+      }
+      if (correct && st == 0) {
+        __syncthreads();  // the diagonal is read before the correction overwrites M
+        const double2 c = fp64_correct_group(src, w.first + j, n, M, lds,
+                                             CorrScratch{F, ints, hold}, tid, nthr, CtaBarrier(),
+                                             reinterpret_cast<float *>(red));
+        la += c.x;
+        ph += c.y;
+      }
+      if (tid == 0) {
+        logabs[ob] = la;
+        if (phase) phase[ob] = ph;
+        if (parity) parity[ob] = (int8_t)par;
+        if (status) status[ob] = st | w.status_or;
       }
     }
   }
 }
 
-GroupedKernel group_kernel_for(int mode) {
+// correct: a mixed plan's pass (its layout reserves the correction's scratch)
+GroupedKernel group_kernel_for(int mode, bool correct) {
+  if (correct) return grouped_group_kernel<ARITH_FUSED, true>;
   return mode == LUFQHE_MODE_PLAIN_FP64 ? grouped_group_kernel<ARITH_REF>
                                         : grouped_group_kernel<ARITH_FUSED>;
 }
@@ -392,10 +410,17 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
   L.smem = 0;
   if (L.nf == 0) return LUFQHE_SUCCESS;
   if (pass == 2) {
-    // one matrix per CTA of kFp64GroupWarps warps
-    GroupedKernel k = group_kernel_for(L.mode);
+    // one matrix per CTA of kFp64GroupWarps warps; a mixed plan's results
+    // with n <= kCorrectMaxN are corrected (nm: the largest such n, for the
+    // correction's scratch)
+    if (p->mode == LUFQHE_MODE_MIXED)
+      for (size_t g = 0; g < p->groups.size(); ++g)
+        if (p->groups[g].count && pass_of(p, g) == 2 && p->groups[g].n <= kCorrectMaxN)
+          L.nm = std::max(L.nm, p->groups[g].n);
+    GroupedKernel k = group_kernel_for(L.mode, L.nm > 0);
     const size_t smem =
-        (size_t)L.nf * (L.nf + 1) * sizeof(double2) + 2 * (size_t)L.nf * sizeof(double);
+        (size_t)L.nf * (L.nf + 1) * sizeof(double2) + 2 * (size_t)L.nf * sizeof(double) +
+        (size_t)L.nm * (L.nm + 1) * sizeof(float2) + 2 * (size_t)L.nm * sizeof(int);
     int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),
                         "cudaFuncSetAttribute(grouped group)");
@@ -451,7 +476,7 @@ int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
   for (int pass = 0; pass < 3 && !rc; ++pass) {
     const Launch &L = p->launch[pass];
     if (L.nitems == 0 || L.ctas == 0) continue;
-    GroupedKernel k = pass == 2 ? group_kernel_for(L.mode) : kernel_for(L.mode);
+    GroupedKernel k = pass == 2 ? group_kernel_for(L.mode, L.nm > 0) : kernel_for(L.mode);
     // a warp-group CTA takes one item at a time
     const long long want = pass == 2 ? L.nitems : (L.nitems + L.warps - 1) / L.warps;
     const int grid = (int)std::min<long long>(L.ctas, want);

@@ -149,7 +149,10 @@ __global__ void write_det_kernel(T *A, int n, int lda, long long batch,
 constexpr int kGroupWarps = kFp64GroupWarps;
 constexpr int kGroupMinN = kFp64GroupMinN;
 
-template <int ARITH, class Src, class Out = double2>
+// CORRECT: the mixed mode's FP64 route, whose log-determinants get the
+// extended-precision correction (fp64_correct_group; its scratch follows the
+// row scales in shared memory).
+template <int ARITH, class Src, class Out = double2, bool CORRECT = false>
 __global__ void __launch_bounds__(kGroupWarps * 32)
     lup_plain_group_kernel(Src src, Out *__restrict__ Aout, int n, int lda, long long batch,
                            double *__restrict__ logabs, double *__restrict__ phase,
@@ -161,11 +164,18 @@ __global__ void __launch_bounds__(kGroupWarps * 32)
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(smem_raw);
   double *hold = reinterpret_cast<double *>(M + (size_t)n * lds);
+  CorrScratch cs{};
+  if constexpr (CORRECT) {
+    float2 *F = reinterpret_cast<float2 *>(hold + 2 * n);
+    cs = CorrScratch{F, reinterpret_cast<int *>(F + (size_t)n * lds), hold};
+  }
   for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
     __syncthreads();
     int par = 0;
     int st = src.load_group(b, n, M, lds, tid, nthr) ? LUFQHE_ST_NONFINITE : 0;
-    if (!st) st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par);
+    if (!st)
+      st = lup_fp64_group<ARITH>(M, lds, hold, n, tid, nthr, red, &par, CtaBarrier(),
+                                 CORRECT ? cs.ints : nullptr);
     __syncthreads();
     if (Aout && (st == 0 || st == LUFQHE_ST_SINGULAR)) {
       Out *dst = Aout + (size_t)b * n * lda;
@@ -175,9 +185,9 @@ __global__ void __launch_bounds__(kGroupWarps * 32)
         w.next(n);
       }
     }
+    double la = 0.0, ph = 0.0;
     if (tid < 32) {
       // warp 0, with the warp routine's own summation order
-      double la, ph;
       if (st == 0) {
         logdet_from_diag(M, lds, n, tid, par, &la, &ph);
       } else if (st == LUFQHE_ST_SINGULAR) {
@@ -188,12 +198,21 @@ __global__ void __launch_bounds__(kGroupWarps * 32)
         ph = NAN;
         par = 0;
       }
-      if (tid == 0) {
-        logabs[b] = la;
-        if (phase) phase[b] = ph;
-        if (parity) parity[b] = (int8_t)par;
-        if (status) status[b] = st | status_or;
+    }
+    if constexpr (CORRECT) {
+      if (st == 0) {
+        __syncthreads();  // the diagonal is read before the correction overwrites M
+        const double2 c = fp64_correct_group(src, b, n, M, lds, cs, tid, nthr, CtaBarrier(),
+                                             reinterpret_cast<float *>(red));
+        la += c.x;
+        ph += c.y;
       }
+    }
+    if (tid == 0) {
+      logabs[b] = la;
+      if (phase) phase[b] = ph;
+      if (parity) parity[b] = (int8_t)par;
+      if (status) status[b] = st | status_or;
     }
   }
 }
@@ -214,10 +233,16 @@ int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int ar
                      double *logabs, double *phase, int8_t *parity, int32_t *status,
                      cudaStream_t stream, int status_or) {
   if (batch == 0) return LUFQHE_SUCCESS;
+  // the mixed mode's FP64 route (status_or set, no factors written back)
+  const bool correct = status_or != 0 && arith == ARITH_FUSED && Aout == nullptr &&
+                       n >= kCorrectMinN && n <= kCorrectMaxN;
+  const size_t corr_smem = (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int);
   if (n >= kGroupMinN) {
-    const size_t smem = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
-    auto kern = arith == ARITH_REF ? lup_plain_group_kernel<ARITH_REF, Src, Out>
-                                   : lup_plain_group_kernel<ARITH_FUSED, Src, Out>;
+    const size_t smem = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double) +
+                        (correct ? corr_smem : 0);
+    auto kern = correct              ? lup_plain_group_kernel<ARITH_FUSED, Src, Out, true>
+                : arith == ARITH_REF ? lup_plain_group_kernel<ARITH_REF, Src, Out>
+                                     : lup_plain_group_kernel<ARITH_FUSED, Src, Out>;
     int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),
                         "cudaFuncSetAttribute(plain group)");
@@ -240,12 +265,7 @@ int launch_plain_src(Src src, Out *Aout, int n, int lda, long long batch, int ar
     timer.stop();
     return check_cuda(cudaGetLastError(), "lup_plain_group_kernel launch");
   }
-  // the mixed mode's FP64 route (status_or set, no factors written back)
-  const bool correct = status_or != 0 && arith == ARITH_FUSED && Aout == nullptr &&
-                       n >= kCorrectMinN && n <= 32;
-  const size_t per_warp =
-      plain_smem_per_warp(n) +
-      (correct ? (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int) : 0);
+  const size_t per_warp = plain_smem_per_warp(n) + (correct ? corr_smem : 0);
   const size_t optin = device_smem_optin();
   int warps = (int)(optin / per_warp);
   if (warps > 4) warps = 4;

@@ -551,9 +551,10 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
 
 // FP64 refactorisation of matrix sb of `src` (reloaded into M), results into
 // slot b, status |= flag (FALLBACK, or FP64 for the routed share). With
-// scratch (cs, 17 <= n <= 32) the log-determinant gets the extended-precision
-// correction of fp64_correct_warp, which brings the FP64 route within the
-// mixed mode's error bound on ill-conditioned matrices.
+// scratch (cs, 17 <= n <= 40) the log-determinant gets the extended-precision
+// correction (fp64_correct_warp for n <= 32, fp64_correct_group on this one
+// warp above), which brings the FP64 route within the mixed mode's error
+// bound on ill-conditioned matrices.
 template <class Src, bool COHERENT = false>
 __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *M, int lds,
                                   double *hold, int lane, long long b, double *logabs,
@@ -563,12 +564,19 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
   __syncwarp();
   src.template load<COHERENT>(sb, n, M, lds, lane);
   int par = 0;
-  const bool correct = cs != nullptr && n >= kCorrectMinN && n <= 32;
+  const bool correct = cs != nullptr && n >= kCorrectMinN && n <= kCorrectMaxN;
   int st = lup_fp64_warp<ARITH_FUSED>(M, lds, hold, n, lane, &par, correct ? cs->ints : nullptr);
   double la, ph;
   if (st == 0) {
     logdet_from_diag(M, lds, n, lane, par, &la, &ph);
-    if (correct) fp64_correct_warp(src, sb, n, M, lds, *cs, lane, &la, &ph);
+    if (correct && n <= 32) {
+      fp64_correct_warp(src, sb, n, M, lds, *cs, lane, &la, &ph);
+    } else if (correct) {
+      const double2 c = fp64_correct_group(src, sb, n, M, lds, *cs, lane, 32, WarpBarrier(),
+                                           static_cast<float *>(nullptr));
+      la += c.x;
+      ph += c.y;
+    }
   } else if (st == LUFQHE_ST_SINGULAR) {
     la = -INFINITY;
     ph = 0.0;

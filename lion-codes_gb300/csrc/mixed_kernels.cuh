@@ -483,7 +483,8 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
   double *hold_all = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
                                                 (size_t)warps * n * lds);
   double *hold = hold_all + warp * 2 * n;
-  // n <= 32: the correction's scratch after the row scales (fallback_smem_per_warp)
+  // n <= kCorrectMaxN: the correction's scratch after the row scales
+  // (fallback_smem_per_warp)
   float2 *F_all = reinterpret_cast<float2 *>(hold_all + (size_t)warps * 2 * n);
   const CorrScratch cs{F_all + (size_t)warp * n * lds,
                        reinterpret_cast<int *>(F_all + (size_t)warps * n * lds) + warp * 2 * n,
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
     const long long b = e & ~kPendRouted;
     fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
                       (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK,
-                      n <= 32 ? &cs : nullptr);
+                      n <= kCorrectMaxN ? &cs : nullptr);
   }
 }
 
@@ -586,10 +587,10 @@ inline bool needs_counter(long long batch, long long grid_warps) {
 }
 
 // Shared memory of one warp of the FP64 pass: the matrix and its row scales;
-// for n <= 32 also the correction's float2 matrix and 2n ints.
+// for n <= kCorrectMaxN also the correction's float2 matrix and 2n ints.
 inline size_t fallback_smem_per_warp(int n) {
   size_t b = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double);
-  if (n <= 32) b += (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int);
+  if (n <= kCorrectMaxN) b += (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int);
   return b;
 }
 
