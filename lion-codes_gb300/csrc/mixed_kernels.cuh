@@ -730,7 +730,6 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   return cs.release(stream, rc);
 }
 
-// plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
 // Sources whose matrices are always of odd order (CF matrices, n = 2Q + 3)
 // never reach the register-tiled kernels, which exist for even n only.
 template <class S, class = void>
@@ -738,6 +737,7 @@ struct has_even_n : std::true_type {};
 template <class S>
 struct has_even_n<S, std::void_t<decltype(S::kOddN)>> : std::false_type {};
 
+// plain_fp64: the plain fused kernel on the same source (the all-FP64 route)
 template <class Src, class PlainFn>
 int launch_mixed_src(Src src, int n, long long batch, double *logabs, double *phase,
                      int8_t *parity, int32_t *status, cudaStream_t stream, PlainFn plain_fp64,
