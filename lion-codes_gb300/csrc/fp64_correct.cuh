@@ -79,6 +79,16 @@ __device__ __forceinline__ void mod_add(unsigned long long &acc, unsigned long l
   acc = neg ? acc - v : acc + v;
 }
 
+// x 2^e rounded to float. For -1022 <= e <= 1023 the power of two is a normal
+// double built from its bits and the product is the correctly rounded x 2^e,
+// which is ldexp's result; ldexp (a longer FP64 sequence) covers the rest.
+__device__ __forceinline__ float scale_to_float(double x, int e) {
+  const double y = (e >= -1022 && e <= 1023)
+                       ? __dmul_rn(x, __longlong_as_double((long long)(e + 1023) << 52))
+                       : ldexp(x, e);
+  return __double2float_rn(y);
+}
+
 __device__ __forceinline__ float2 cf_sub_mul(float2 s, float2 a, float2 b) {  // s - a b
   return make_float2(fmaf(a.y, b.y, fmaf(-a.x, b.x, s.x)), fmaf(-a.y, b.x, fmaf(-a.x, b.y, s.y)));
 }
@@ -207,8 +217,8 @@ __device__ __forceinline__ void residual_entry(const Src &src, long long sb, int
     mod_mac(im, li.m, ur.m, r0 - li.e - ur.e, (li.neg ^ ur.neg ^ 1u) != 0u);
   }
   const int sh = mx - 2150 + bias - sr[i] - sc[j];
-  F[i * lds + j] = make_float2(__double2float_rn(ldexp((double)(long long)re, sh)),
-                               __double2float_rn(ldexp((double)(long long)im, sh)));
+  F[i * lds + j] = make_float2(scale_to_float((double)(long long)re, sh),
+                               scale_to_float((double)(long long)im, sh));
 }
 
 // Shared memory the correction borrows from its caller: F (n x lds float2),
@@ -280,7 +290,7 @@ __device__ __noinline__ void fp64_correct_warp(const Src src, long long sb, int 
       if (k < n) {
         const double2 d = M[q];
         const int s = k < i ? sr[k] - sr[i] : -sr[i] - sc[k];
-        v = make_float2(__double2float_rn(ldexp(d.x, s)), __double2float_rn(ldexp(d.y, s)));
+        v = make_float2(scale_to_float(d.x, s), scale_to_float(d.y, s));
       }
     }
     __syncwarp();
@@ -415,7 +425,7 @@ __device__ __noinline__ double2 fp64_correct_group(const Src src, long long sb, 
       if (k < n) {
         const double2 d = M[q];
         const int sh = k < i ? sr[k] - sr[i] : -sr[i] - sc[k];
-        v = make_float2(__double2float_rn(ldexp(d.x, sh)), __double2float_rn(ldexp(d.y, sh)));
+        v = make_float2(scale_to_float(d.x, sh), scale_to_float(d.y, sh));
       }
     }
     bar.sync();
