@@ -366,16 +366,21 @@ struct WarpBarrier {
 
 // The same correction by the nthr threads of a warp group (a multiple of 32,
 // synchronised by bar, as in lup_fp64_group), or by one warp (WarpBarrier),
-// for 32 < n <= kCorrectMaxN (n <= 64 fits its grid), on FP64 factors of
-// either routine. red: 4 floats of
-// shared scratch per warp (unused, and may be null, for one warp).
-// Returns the correction to add to (log|det|, phase), the same value in every
-// thread, or (0, 0) if a scaled quantity left float's range. The steps are
-// those of fp64_correct_warp with rows, columns and residual entries dealt
-// over the group; the column scales are reduced per warp, then across warps
-// with shared atomics.
+// for n <= kCorrectMaxN (n <= 64 fits its grid), on FP64 factors of either
+// routine; for n <= 32 its result is fp64_correct_warp's bit for bit (the
+// same operations per entry and per column; the trace partials of warps
+// without a column are zero). red: 4 floats of shared scratch per warp
+// (unused, and may be null, for one warp). Returns the correction to add to
+// (log|det|, phase), the same value in every thread, or (0, 0) if a scaled
+// quantity left float's range. The steps are those of fp64_correct_warp with
+// rows, columns and residual entries dealt over the group; the column scales
+// are reduced per warp, then across warps with shared atomics. Inlined into
+// its callers: compiled out of line, its warp-group form returned wrong
+// corrections in one kernel of the library (n = 24, three warps), while the
+// same code inlined, or out of line in a module of its own, was right on the
+// same matrices.
 template <class Src, class Bar>
-__device__ __noinline__ double2 fp64_correct_group(const Src src, long long sb, int n,
+__device__ __forceinline__ double2 fp64_correct_group(const Src src, long long sb, int n,
                                                    double2 *M, int lds, const CorrScratch cs,
                                                    int tid, int nthr, Bar bar, float *red) {
   float2 *const F = cs.F;
@@ -504,6 +509,16 @@ __device__ __noinline__ double2 fp64_correct_group(const Src src, long long sb, 
   const double dx = (double)t.x - 0.5 * (double)t.z;
   const double dy = (double)t.y - 0.5 * (double)t.w;
   return (isfinite(dx) && isfinite(dy)) ? make_double2(dx, dy) : make_double2(0.0, 0.0);
+}
+
+// The one-warp form (synchronised by __syncwarp only), kept out of line: it
+// runs on a few percent of the matrices of the kernels that call it.
+template <class Src>
+__device__ __noinline__ double2 fp64_correct_one_warp(const Src src, long long sb, int n,
+                                                      double2 *M, int lds, const CorrScratch cs,
+                                                      int lane) {
+  return fp64_correct_group(src, sb, n, M, lds, cs, lane, 32, WarpBarrier(),
+                            static_cast<float *>(nullptr));
 }
 
 }  // namespace lufqhe

@@ -572,8 +572,7 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
     if (correct && n <= 32) {
       fp64_correct_warp(src, sb, n, M, lds, *cs, lane, &la, &ph);
     } else if (correct) {
-      const double2 c = fp64_correct_group(src, sb, n, M, lds, *cs, lane, 32, WarpBarrier(),
-                                           static_cast<float *>(nullptr));
+      const double2 c = fp64_correct_one_warp(src, sb, n, M, lds, *cs, lane);
       la += c.x;
       ph += c.y;
     }
