@@ -549,18 +549,39 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
   }
 }
 
+// FP64 factors left for a correction pass of their own (FacList): the
+// matrix's slot, its uncorrected result, the pivot order and L\U (row stride
+// n), in a call-local buffer of `cap` entries of `bytes` each.
+struct FacHead {
+  long long b;
+  double la, ph;
+  int par, flag;
+};
+struct FacList {
+  unsigned long long *count;
+  unsigned char *buf;
+  long long cap;
+  long long bytes;
+};
+__host__ __device__ constexpr long long fac_entry_bytes(int n) {
+  return (long long)sizeof(FacHead) + (((long long)n * 4 + 15) & ~15ll) + (long long)n * n * 16;
+}
+
 // FP64 refactorisation of matrix sb of `src` (reloaded into M), results into
 // slot b, status |= flag (FALLBACK, or FP64 for the routed share). With
 // scratch (cs, 17 <= n <= 40) the log-determinant gets the extended-precision
 // correction (fp64_correct_warp for n <= 32, fp64_correct_group on this one
 // warp above), which brings the FP64 route within the mixed mode's error
-// bound on ill-conditioned matrices.
+// bound on ill-conditioned matrices. With a list (fl, n <= 32) the factors
+// are listed instead, while it has room, for the correction pass
+// (lup_mixed_fac_correct_kernel) to finish the result.
 template <class Src, bool COHERENT = false>
 __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *M, int lds,
                                   double *hold, int lane, long long b, double *logabs,
                                   double *phase, int8_t *parity, int32_t *status,
                                   int flag = LUFQHE_ST_FALLBACK,
-                                  const CorrScratch *cs = nullptr) {
+                                  const CorrScratch *cs = nullptr,
+                                  const FacList *fl = nullptr) {
   __syncwarp();
   src.template load<COHERENT>(sb, n, M, lds, lane);
   int par = 0;
@@ -569,6 +590,21 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
   double la, ph;
   if (st == 0) {
     logdet_from_diag(M, lds, n, lane, par, &la, &ph);
+    if (correct && n <= 32 && fl) {
+      unsigned long long k = 0;
+      if (lane == 0) k = atomicAdd(fl->count, 1ull);
+      k = __shfl_sync(kFull, k, 0);
+      if (k < (unsigned long long)fl->cap) {
+        unsigned char *e = fl->buf + k * fl->bytes;
+        if (lane == 0) *reinterpret_cast<FacHead *>(e) = FacHead{b, la, ph, par, flag};
+        int *pe = reinterpret_cast<int *>(e + sizeof(FacHead));
+        for (int i = lane; i < n; i += 32) pe[i] = cs->ints[i];
+        double2 *fe = reinterpret_cast<double2 *>(e + sizeof(FacHead) + ((n * 4 + 15) & ~15));
+        for (int q = lane; q < n * n; q += 32) fe[q] = M[(q / n) * lds + q % n];
+        __syncwarp();
+        return;
+      }
+    }
     if (correct && n <= 32) {
       fp64_correct_warp(src, sb, n, M, lds, *cs, lane, &la, &ph);
     } else if (correct) {

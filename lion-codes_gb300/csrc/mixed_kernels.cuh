@@ -116,6 +116,8 @@ constexpr unsigned int kPendRouted = 0x80000000u;
 constexpr int kDeferMinN = 24;
 // Warps of the FP64 pass's CTA (one CTA per SM).
 constexpr int kFallbackMaxWarps = 20;
+// Warps of a CTA of the correction pass after the finish kernel.
+constexpr int kFacCorrectWarps = 4;
 
 // Hand matrix b to the FP64 pass (the list has room for every matrix).
 __device__ __forceinline__ void defer_fp64(CallHead *head, unsigned int *pend, long long b,
@@ -394,8 +396,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
 // after the other.
 template <int N, class Src>
 __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
-    lup_mixed_finish_kernel(Src src, const CallHead *head, const unsigned int *pend,
+    lup_mixed_finish_kernel(Src src, CallHead *head, const unsigned int *pend,
                             const unsigned char *refine, long long refine_cap, float theta2,
+                            unsigned char *fac, long long fac_cap,
                             double *__restrict__ logabs, double *__restrict__ phase,
                             int8_t *__restrict__ parity, int32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -415,6 +418,8 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   base += warps * 2 * (size_t)N * sizeof(double);
   float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
   const CorrScratch cs{F, reinterpret_cast<int *>(diag), hold};
+  // the corrections of the FP64 factorisations go to lup_mixed_fac_correct_kernel
+  const FacList fl{&head->corr_count, fac, fac_cap, fac_entry_bytes(N)};
   // 1. the FP32 pass's rejections, dealt out
   const unsigned long long listed = head->pend_count;
   const unsigned long long stride = (unsigned long long)warps * gridDim.x;
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
     const unsigned int e = pend[j];
     const long long b = e & ~kPendRouted;
     fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
-                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK, &cs);
+                      (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK, &cs, &fl);
   }
   // 2. the saved matrices, claimed; a failed refinement is refactorised here
   DeferredOut out;
@@ -453,10 +458,54 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
         out.push(lane, h.b, prod, h.exp_sum, corr, h.par, logabs, phase, parity, status);
       else
         fallback_fp64_src(src, h.b, N, M, LDS, hold, lane, h.b, logabs, phase, parity, status,
-                          LUFQHE_ST_FALLBACK, &cs);
+                          LUFQHE_ST_FALLBACK, &cs, &fl);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
+}
+
+// The corrections of the finish kernel's FP64 factorisations (n = 24, 32):
+// entry j of the list by CTA j % grid with all its warps (the inlined
+// fp64_correct_group, whose result is fp64_correct_warp's bit for bit), on the
+// listed L\U and pivot order and the source's matrix. One warp per matrix,
+// the factorisation (~92 us on a sub-partition's shared FP64 pipe) and then
+// the correction (120-177 us) on the same warp had been the finish kernel's
+// critical path.
+template <int N, class Src>
+__global__ void __launch_bounds__(kFacCorrectWarps * 32)
+    lup_mixed_fac_correct_kernel(Src src, const CallHead *head, const unsigned char *fac,
+                                 long long fac_cap, double *__restrict__ logabs,
+                                 double *__restrict__ phase, int8_t *__restrict__ parity,
+                                 int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long red[3 * kFacCorrectWarps];
+  constexpr int LDS = N + 1;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw);
+  double *hold = reinterpret_cast<double *>(M + (size_t)N * LDS);
+  float2 *F = reinterpret_cast<float2 *>(hold + 2 * N);
+  int *ints = reinterpret_cast<int *>(F + (size_t)N * LDS);
+  const CorrScratch cs{F, ints, hold};
+  const unsigned long long listed = min(head->corr_count, (unsigned long long)fac_cap);
+  for (unsigned long long j = blockIdx.x; j < listed; j += gridDim.x) {
+    const unsigned char *e = fac + j * fac_entry_bytes(N);
+    const FacHead h = *reinterpret_cast<const FacHead *>(e);
+    const int *pe = reinterpret_cast<const int *>(e + sizeof(FacHead));
+    const double2 *fe = reinterpret_cast<const double2 *>(e + sizeof(FacHead) +
+                                                          ((N * 4 + 15) & ~15));
+    __syncthreads();  // the previous entry's correction is done with the scratch
+    for (int i = tid; i < N; i += nthr) ints[i] = __ldcg(pe + i);
+    for (int q = tid; q < N * N; q += nthr) M[(q / N) * LDS + q % N] = __ldcg(fe + q);
+    __syncthreads();
+    const double2 c = fp64_correct_group(src, h.b, N, M, LDS, cs, tid, nthr, CtaBarrier(),
+                                         reinterpret_cast<float *>(red));
+    if (tid == 0) {
+      logabs[h.b] = h.la + c.x;
+      if (phase) phase[h.b] = h.ph + c.y;
+      if (parity) parity[h.b] = (int8_t)h.par;
+      if (status) status[h.b] = h.flag;
+    }
+  }
 }
 
 // The FP64 pass of the generic mixed kernel (n >= 24 without a register-tiled
@@ -672,10 +721,18 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
     corr_cap = std::max<long long>(256, (long long)(kCorrShare * (double)batch));
     corr_cap = std::min<long long>(corr_cap, batch);
   }
+  // the device path's list of FP64 factors for the correction pass (an
+  // overflow is corrected in the finish kernel itself)
+  long long fac_cap = 0;
+  if (two_pass && N >= kCorrectMinN && N <= kCorrectMaxN) {
+    fac_cap = std::max<long long>(256, (long long)(kCorrShare * (double)batch));
+    fac_cap = std::min<long long>(fac_cap, batch);
+  }
   CallState cs;
   if (two_pass || inplace || needs_counter(batch, (long long)grid * warps)) {
     rc = cs.acquire(two_pass ? (size_t)batch : 0, refine_bytes, spill_bytes, stream,
-                    (size_t)corr_cap * corr_entry_bytes<N>());
+                    inplace ? (size_t)corr_cap * corr_entry_bytes<N>()
+                            : (size_t)fac_cap * (size_t)fac_entry_bytes(N));
     if (rc) return cs.release(stream, rc);
   }
   // in-place kernels: refine_cap says whether the refinement is on
@@ -711,7 +768,8 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
       }
     }
   }
-  // the refinements and the FP64 refactorisations, side by side in one kernel
+  // the refinements and the FP64 refactorisations, side by side in one kernel,
+  // then the corrections of those refactorisations, each by a whole CTA
   if (!rc && two_pass) {
     if constexpr (N >= kDeferMinN) {
       auto fk = lup_mixed_finish_kernel<N, Src>;
@@ -721,9 +779,33 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
       if (!rc) {
         KernelTimer timer("lup_mixed_finish_kernel", N, stream);
         fk<<<grid, warps * 32, smem, stream>>>(src, cs.head, cs.pend, cs.refine, refine_cap,
-                                               theta2, logabs, phase, parity, status);
+                                               theta2, cs.corr, fac_cap, logabs, phase, parity,
+                                               status);
         timer.stop();
         rc = check_cuda(cudaGetLastError(), "lup_mixed_finish_kernel launch");
+      }
+      if (!rc && fac_cap > 0) {
+        auto xk = lup_mixed_fac_correct_kernel<N, Src>;
+        const size_t xsmem = fallback_smem_per_warp(N);
+        rc = check_cuda(cudaFuncSetAttribute(xk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)xsmem),
+                        "cudaFuncSetAttribute(mixed fac correct)");
+        int per_sm = 0;
+        if (!rc)
+          rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &per_sm, xk, kFacCorrectWarps * 32, xsmem),
+                          "occupancy(mixed fac correct)");
+        if (!rc) {
+          // the list's length is known only on the device: as many CTAs as
+          // fit, at most one per entry of its capacity
+          const long long cap = (long long)device_sm_count() * std::max(1, per_sm);
+          const int xgrid = (int)std::min<long long>(fac_cap, cap);
+          KernelTimer timer("lup_mixed_fac_correct_kernel", N, stream);
+          xk<<<xgrid, kFacCorrectWarps * 32, xsmem, stream>>>(src, cs.head, cs.corr, fac_cap,
+                                                              logabs, phase, parity, status);
+          timer.stop();
+          rc = check_cuda(cudaGetLastError(), "lup_mixed_fac_correct_kernel launch");
+        }
       }
     }
   }
