@@ -551,21 +551,29 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
 
 // FP64 factors left for a correction pass of their own (FacList): the
 // matrix's slot, its uncorrected result, the pivot order and L\U (row stride
-// n), in a call-local buffer of `cap` entries of `bytes` each.
+// n), and with `copy` the matrix itself after them (for sources the pass
+// cannot read again cheaply: a batch in host memory), in a call-local buffer
+// of `cap` entries of fac_entry_bytes(n, copy) each.
 struct FacHead {
   long long b;
   double la, ph;
   int par, flag;
 };
+__host__ __device__ constexpr long long fac_factors_offset(int n) {
+  return (long long)sizeof(FacHead) + (((long long)n * 4 + 15) & ~15ll);
+}
+__host__ __device__ constexpr long long fac_copy_offset(int n) {
+  return fac_factors_offset(n) + (long long)n * n * 16;
+}
+__host__ __device__ constexpr long long fac_entry_bytes(int n, bool copy = false) {
+  return fac_copy_offset(n) + (copy ? (long long)n * n * 16 : 0ll);
+}
 struct FacList {
   unsigned long long *count;
   unsigned char *buf;
   long long cap;
-  long long bytes;
+  int copy;
 };
-__host__ __device__ constexpr long long fac_entry_bytes(int n) {
-  return (long long)sizeof(FacHead) + (((long long)n * 4 + 15) & ~15ll) + (long long)n * n * 16;
-}
 
 // FP64 refactorisation of matrix sb of `src` (reloaded into M), results into
 // slot b, status |= flag (FALLBACK, or FP64 for the routed share). With
@@ -595,12 +603,16 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
       if (lane == 0) k = atomicAdd(fl->count, 1ull);
       k = __shfl_sync(kFull, k, 0);
       if (k < (unsigned long long)fl->cap) {
-        unsigned char *e = fl->buf + k * fl->bytes;
+        unsigned char *e = fl->buf + k * fac_entry_bytes(n, fl->copy != 0);
         if (lane == 0) *reinterpret_cast<FacHead *>(e) = FacHead{b, la, ph, par, flag};
         int *pe = reinterpret_cast<int *>(e + sizeof(FacHead));
         for (int i = lane; i < n; i += 32) pe[i] = cs->ints[i];
-        double2 *fe = reinterpret_cast<double2 *>(e + sizeof(FacHead) + ((n * 4 + 15) & ~15));
+        double2 *fe = reinterpret_cast<double2 *>(e + fac_factors_offset(n));
         for (int q = lane; q < n * n; q += 32) fe[q] = M[(q / n) * lds + q % n];
+        if (fl->copy) {
+          double2 *ce = reinterpret_cast<double2 *>(e + fac_copy_offset(n));
+          for (int q = lane; q < n * n; q += 32) ce[q] = source_entry(src, sb, n, q / n, q % n);
+        }
         __syncwarp();
         return;
       }

@@ -148,30 +148,11 @@ constexpr double kRefineShare = 0.25;
 // The host-link variant refactorises rejected matrices in place (it waits on
 // the link and has compute to spare) but hands their extended-precision
 // correction, whose latency would hold the warp off the link for the length
-// of several factorisations, to a pass of its own: the matrix (from the warp's
-// device copy) and its slot go to the call's correction list.
-template <int N>
-constexpr size_t corr_entry_bytes() {
-  return 16 + (size_t)N * N * sizeof(double2);
-}
-// Share of a batch the correction list has room for (beyond it the warp
-// corrects in place).
+// of several factorisations, to a pass of its own (the factor list with the
+// matrix from the warp's device copy, FacList); the device path's finish
+// kernel lists its factorisations the same way, without the copy. Share of a
+// batch the list has room for (beyond it the warp corrects in place):
 constexpr double kCorrShare = 0.25;
-
-template <int N>
-__device__ bool list_correction(CallHead *head, unsigned char *buf, long long cap,
-                                const double2 *own, long long b, int lane) {
-  unsigned long long k = 0;
-  if (lane == 0) k = atomicAdd(&head->corr_count, 1ull);
-  k = __shfl_sync(kFull, k, 0);
-  if (k >= (unsigned long long)cap) return false;
-  unsigned char *e = buf + k * corr_entry_bytes<N>();
-  double2 *dA = reinterpret_cast<double2 *>(e + 16);
-  for (int q = lane; q < N * N; q += 32) dA[q] = __ldcg(own + q);
-  if (lane == 0) *reinterpret_cast<long long *>(e) = b;
-  __syncwarp();
-  return true;
-}
 
 // Save a TILE_REFINE matrix; false (warp-uniform) if the buffer is full.
 template <int N>
@@ -372,12 +353,12 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
                                 tile_la_est(prod, exp_sum), corr)))
         out.push(lane, b, prod, exp_sum, corr, par, logabs, phase, parity, status);
       else if constexpr (INPLACE) {
-        const bool listed =
-            N >= kCorrectMinN && corr_list != nullptr &&
-            list_correction<N>(head, corr_list, corr_cap, own, b, lane);
+        // the factors (and the warp's copy of the matrix) are listed for the
+        // correction pass, so that no warp stops reading the link for one
+        const FacList fl{&head->corr_count, corr_list, corr_cap, 1};
         fallback_fp64_src<DenseSource, true>(DenseSource{own, N}, 0, N, M, LDS, hold, lane, b,
                                              logabs, phase, parity, status, LUFQHE_ST_FALLBACK,
-                                             listed ? nullptr : &cs);
+                                             &cs, corr_list != nullptr ? &fl : nullptr);
       }
       else
         fallback_fp64_src(src, b, N, M, LDS, hold, lane, b, logabs, phase, parity, status,
@@ -419,7 +400,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
   const CorrScratch cs{F, reinterpret_cast<int *>(diag), hold};
   // the corrections of the FP64 factorisations go to lup_mixed_fac_correct_kernel
-  const FacList fl{&head->corr_count, fac, fac_cap, fac_entry_bytes(N)};
+  const FacList fl{&head->corr_count, fac, fac_cap, 0};
   // 1. the FP32 pass's rejections, dealt out
   const unsigned long long listed = head->pend_count;
   const unsigned long long stride = (unsigned long long)warps * gridDim.x;
@@ -471,7 +452,9 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
 // the factorisation (~92 us on a sub-partition's shared FP64 pipe) and then
 // the correction (120-177 us) on the same warp had been the finish kernel's
 // critical path.
-template <int N, class Src>
+// COPY: the entries carry the matrix (the host-link variant's list), which is
+// the source of the residual instead of src.
+template <int N, class Src, bool COPY = false>
 __global__ void __launch_bounds__(kFacCorrectWarps * 32)
     lup_mixed_fac_correct_kernel(Src src, const CallHead *head, const unsigned char *fac,
                                  long long fac_cap, double *__restrict__ logabs,
@@ -488,17 +471,23 @@ __global__ void __launch_bounds__(kFacCorrectWarps * 32)
   const CorrScratch cs{F, ints, hold};
   const unsigned long long listed = min(head->corr_count, (unsigned long long)fac_cap);
   for (unsigned long long j = blockIdx.x; j < listed; j += gridDim.x) {
-    const unsigned char *e = fac + j * fac_entry_bytes(N);
+    const unsigned char *e = fac + j * fac_entry_bytes(N, COPY);
     const FacHead h = *reinterpret_cast<const FacHead *>(e);
     const int *pe = reinterpret_cast<const int *>(e + sizeof(FacHead));
-    const double2 *fe = reinterpret_cast<const double2 *>(e + sizeof(FacHead) +
-                                                          ((N * 4 + 15) & ~15));
+    const double2 *fe = reinterpret_cast<const double2 *>(e + fac_factors_offset(N));
     __syncthreads();  // the previous entry's correction is done with the scratch
     for (int i = tid; i < N; i += nthr) ints[i] = __ldcg(pe + i);
     for (int q = tid; q < N * N; q += nthr) M[(q / N) * LDS + q % N] = __ldcg(fe + q);
     __syncthreads();
-    const double2 c = fp64_correct_group(src, h.b, N, M, LDS, cs, tid, nthr, CtaBarrier(),
-                                         reinterpret_cast<float *>(red));
+    double2 c;
+    if constexpr (COPY)
+      c = fp64_correct_group(DenseSource{reinterpret_cast<const double2 *>(e + fac_copy_offset(N)),
+                                         N},
+                             0, N, M, LDS, cs, tid, nthr, CtaBarrier(),
+                             reinterpret_cast<float *>(red));
+    else
+      c = fp64_correct_group(src, h.b, N, M, LDS, cs, tid, nthr, CtaBarrier(),
+                             reinterpret_cast<float *>(red));
     if (tid == 0) {
       logabs[h.b] = h.la + c.x;
       if (phase) phase[h.b] = h.ph + c.y;
@@ -547,39 +536,6 @@ __global__ void __launch_bounds__(kFallbackMaxWarps * 32)
     fallback_fp64_src(src, b, n, M, lds, hold, lane, b, logabs, phase, parity, status,
                       (e & kPendRouted) ? LUFQHE_ST_FP64 : LUFQHE_ST_FALLBACK,
                       n <= kCorrectMaxN ? &cs : nullptr);
-  }
-}
-
-// The host-link variant's corrections: each listed matrix is refactorised from
-// its device copy (the same bits as the in-place factorisation) and its
-// log-determinant corrected; results overwrite the uncorrected ones.
-template <int N>
-__global__ void __launch_bounds__(kFallbackMaxWarps * 32)
-    lup_mixed_correct_kernel(const CallHead *head, const unsigned char *corr, long long corr_cap,
-                             double *__restrict__ logabs, double *__restrict__ phase,
-                             int8_t *__restrict__ parity, int32_t *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int LDS = N + 1;
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * N * LDS;
-  double *hold_all = reinterpret_cast<double *>(reinterpret_cast<double2 *>(smem_raw) +
-                                                (size_t)warps * N * LDS);
-  double *hold = hold_all + warp * 2 * N;
-  float2 *F_all = reinterpret_cast<float2 *>(hold_all + (size_t)warps * 2 * N);
-  const CorrScratch cs{F_all + (size_t)warp * N * LDS,
-                       reinterpret_cast<int *>(F_all + (size_t)warps * N * LDS) + warp * 2 * N,
-                       hold};
-  const unsigned long long listed = min(head->corr_count, (unsigned long long)corr_cap);
-  const unsigned long long stride = (unsigned long long)warps * gridDim.x;
-  for (unsigned long long j = (unsigned long long)warp * gridDim.x + blockIdx.x; j < listed;
-       j += stride) {
-    const unsigned char *e = corr + j * corr_entry_bytes<N>();
-    const long long b = *reinterpret_cast<const long long *>(e);
-    const double2 *A = reinterpret_cast<const double2 *>(e + 16);
-    fallback_fp64_src<DenseSource, true>(DenseSource{A, N}, 0, N, M, LDS, hold, lane, b, logabs,
-                                         phase, parity, status, LUFQHE_ST_FALLBACK, &cs);
   }
 }
 
@@ -675,6 +631,33 @@ int launch_fallback(Src src, int n, const CallHead *head, const unsigned int *pe
   return check_cuda(cudaGetLastError(), "lup_mixed_fallback_kernel launch");
 }
 
+// The correction pass over a factor list of capacity cap (its length is
+// known only on the device): as many CTAs as fit, at most one per entry.
+template <int N, class Src, bool COPY>
+int launch_fac_correct(Src src, const CallHead *head, const unsigned char *list, long long cap,
+                       double *logabs, double *phase, int8_t *parity, int32_t *status,
+                       cudaStream_t stream) {
+  auto k = lup_mixed_fac_correct_kernel<N, Src, COPY>;
+  const size_t smem = fallback_smem_per_warp(N);
+  int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
+                      "cudaFuncSetAttribute(mixed fac correct)");
+  int per_sm = 0;
+  if (!rc)
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k,
+                                                                  kFacCorrectWarps * 32, smem),
+                    "occupancy(mixed fac correct)");
+  if (rc) return rc;
+  const long long fit = (long long)device_sm_count() * std::max(1, per_sm);
+  const int grid = (int)std::min<long long>(cap, fit);
+  KernelTimer timer(COPY ? "lup_mixed_fac_correct_kernel_hostlink" : "lup_mixed_fac_correct_kernel",
+                    N, stream);
+  k<<<grid, kFacCorrectWarps * 32, smem, stream>>>(src, head, list, cap, logabs, phase, parity,
+                                                   status);
+  timer.stop();
+  return check_cuda(cudaGetLastError(), "lup_mixed_fac_correct_kernel launch");
+}
+
 template <int N, class Src>
 int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, double *phase,
                       int8_t *parity, int32_t *status, cudaStream_t stream, bool inplace) {
@@ -731,7 +714,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   CallState cs;
   if (two_pass || inplace || needs_counter(batch, (long long)grid * warps)) {
     rc = cs.acquire(two_pass ? (size_t)batch : 0, refine_bytes, spill_bytes, stream,
-                    inplace ? (size_t)corr_cap * corr_entry_bytes<N>()
+                    inplace ? (size_t)corr_cap * (size_t)fac_entry_bytes(N, true)
                             : (size_t)fac_cap * (size_t)fac_entry_bytes(N));
     if (rc) return cs.release(stream, rc);
   }
@@ -747,26 +730,9 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   }
   rc = check_cuda(cudaGetLastError(), "lup_mixed_tile_kernel launch");
   if (!rc && corr_cap > 0) {
-    if constexpr (N >= kCorrectMinN) {
-      auto ck = lup_mixed_correct_kernel<N>;
-      const size_t cper = fallback_smem_per_warp(N);
-      int cw = (int)(device_smem_optin() / cper);
-      cw = std::max(1, std::min(cw, kFallbackMaxWarps));
-      const size_t csmem = cper * cw;
-      rc = check_cuda(cudaFuncSetAttribute(ck, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)csmem),
-                      "cudaFuncSetAttribute(mixed correct)");
-      if (!rc) {
-        // one CTA per SM: the list's length is known only on the device
-        const long long want = (corr_cap + cw - 1) / cw;
-        const int cgrid = (int)std::min<long long>(want, (long long)device_sm_count());
-        KernelTimer timer("lup_mixed_correct_kernel", N, stream);
-        ck<<<cgrid, cw * 32, csmem, stream>>>(cs.head, cs.corr, corr_cap, logabs, phase, parity,
-                                              status);
-        timer.stop();
-        rc = check_cuda(cudaGetLastError(), "lup_mixed_correct_kernel launch");
-      }
-    }
+    if constexpr (kHasInplace && N >= kCorrectMinN && N <= kCorrectMaxN)
+      rc = launch_fac_correct<N, Src, true>(src, cs.head, cs.corr, corr_cap, logabs, phase,
+                                            parity, status, stream);
   }
   // the refinements and the FP64 refactorisations, side by side in one kernel,
   // then the corrections of those refactorisations, each by a whole CTA
@@ -784,29 +750,9 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
         timer.stop();
         rc = check_cuda(cudaGetLastError(), "lup_mixed_finish_kernel launch");
       }
-      if (!rc && fac_cap > 0) {
-        auto xk = lup_mixed_fac_correct_kernel<N, Src>;
-        const size_t xsmem = fallback_smem_per_warp(N);
-        rc = check_cuda(cudaFuncSetAttribute(xk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)xsmem),
-                        "cudaFuncSetAttribute(mixed fac correct)");
-        int per_sm = 0;
-        if (!rc)
-          rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, xk, kFacCorrectWarps * 32, xsmem),
-                          "occupancy(mixed fac correct)");
-        if (!rc) {
-          // the list's length is known only on the device: as many CTAs as
-          // fit, at most one per entry of its capacity
-          const long long cap = (long long)device_sm_count() * std::max(1, per_sm);
-          const int xgrid = (int)std::min<long long>(fac_cap, cap);
-          KernelTimer timer("lup_mixed_fac_correct_kernel", N, stream);
-          xk<<<xgrid, kFacCorrectWarps * 32, xsmem, stream>>>(src, cs.head, cs.corr, fac_cap,
-                                                              logabs, phase, parity, status);
-          timer.stop();
-          rc = check_cuda(cudaGetLastError(), "lup_mixed_fac_correct_kernel launch");
-        }
-      }
+      if (!rc && fac_cap > 0)
+        rc = launch_fac_correct<N, Src, false>(src, cs.head, cs.corr, fac_cap, logabs, phase,
+                                               parity, status, stream);
     }
   }
   return cs.release(stream, rc);
