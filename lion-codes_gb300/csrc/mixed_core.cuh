@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
 
 #include "lup_fp64.cuh"
 #include "fp64_correct.cuh"
@@ -552,8 +553,9 @@ __device__ __forceinline__ void emit_nonfinite(int lane, long long b, double *lo
 // FP64 factors left for a correction pass of their own (FacList): the
 // matrix's slot, its uncorrected result, the pivot order and L\U (row stride
 // n), and with `copy` the matrix itself after them (for sources the pass
-// cannot read again cheaply: a batch in host memory), in a call-local buffer
-// of `cap` entries of fac_entry_bytes(n, copy) each.
+// cannot read again cheaply: a batch in host memory, matrices built from
+// coordinates), in a call-local buffer of `cap` entries of
+// fac_entry_bytes(n, copy) each.
 struct FacHead {
   long long b;
   double la, ph;
@@ -611,7 +613,16 @@ __device__ void fallback_fp64_src(const Src &src, long long sb, int n, double2 *
         for (int q = lane; q < n * n; q += 32) fe[q] = M[(q / n) * lds + q % n];
         if (fl->copy) {
           double2 *ce = reinterpret_cast<double2 *>(e + fac_copy_offset(n));
-          for (int q = lane; q < n * n; q += 32) ce[q] = source_entry(src, sb, n, q / n, q % n);
+          if constexpr (std::is_same<Src, DenseSource>::value) {
+            for (int q = lane; q < n * n; q += 32) ce[q] = source_entry(src, sb, n, q / n, q % n);
+          } else {
+            // a row per lane, built once (entries rebuilt one at a time would
+            // repeat their row's recurrence)
+            for (int r = lane; r < n; r += 32) {
+              auto it = source_row(src, sb, n, r);
+              for (int c = 0; c < n; ++c) ce[r * n + c] = it.next();
+            }
+          }
         }
         __syncwarp();
         return;

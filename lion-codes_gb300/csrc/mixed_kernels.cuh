@@ -153,6 +153,13 @@ constexpr double kRefineShare = 0.25;
 // kernel lists its factorisations the same way, without the copy. Share of a
 // batch the list has room for (beyond it the warp corrects in place):
 constexpr double kCorrShare = 0.25;
+// Sources whose matrices the correction pass reads from a copy in the list:
+// all but a dense device batch (rows built from coordinates would be built
+// again entry by entry for the residual).
+template <class Src>
+constexpr int fac_copies() {
+  return std::is_same<Src, DenseSource>::value ? 0 : 1;
+}
 
 // Save a TILE_REFINE matrix; false (warp-uniform) if the buffer is full.
 template <int N>
@@ -400,7 +407,7 @@ __global__ void __launch_bounds__(tile_max_warps(N) * 32, tile_min_ctas(N))
   float2 *diag = reinterpret_cast<float2 *>(reinterpret_cast<int *>(base) + warp * 2 * N);
   const CorrScratch cs{F, reinterpret_cast<int *>(diag), hold};
   // the corrections of the FP64 factorisations go to lup_mixed_fac_correct_kernel
-  const FacList fl{&head->corr_count, fac, fac_cap, 0};
+  const FacList fl{&head->corr_count, fac, fac_cap, fac_copies<Src>()};
   // 1. the FP32 pass's rejections, dealt out
   const unsigned long long listed = head->pend_count;
   const unsigned long long stride = (unsigned long long)warps * gridDim.x;
@@ -715,7 +722,7 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
   if (two_pass || inplace || needs_counter(batch, (long long)grid * warps)) {
     rc = cs.acquire(two_pass ? (size_t)batch : 0, refine_bytes, spill_bytes, stream,
                     inplace ? (size_t)corr_cap * (size_t)fac_entry_bytes(N, true)
-                            : (size_t)fac_cap * (size_t)fac_entry_bytes(N));
+                            : (size_t)fac_cap * (size_t)fac_entry_bytes(N, fac_copies<Src>()));
     if (rc) return cs.release(stream, rc);
   }
   // in-place kernels: refine_cap says whether the refinement is on
@@ -751,8 +758,9 @@ int launch_mixed_tile(Src src, long long batch, float theta2, double *logabs, do
         rc = check_cuda(cudaGetLastError(), "lup_mixed_finish_kernel launch");
       }
       if (!rc && fac_cap > 0)
-        rc = launch_fac_correct<N, Src, false>(src, cs.head, cs.corr, fac_cap, logabs, phase,
-                                               parity, status, stream);
+        rc = launch_fac_correct<N, Src, fac_copies<Src>() != 0>(src, cs.head, cs.corr, fac_cap,
+                                                                logabs, phase, parity, status,
+                                                                stream);
     }
   }
   return cs.release(stream, rc);
