@@ -86,3 +86,31 @@ def test_mixed_over_host_link_special_matrices(cuda, lufqhe_mod):
         assert np.array_equal(got[k], want[k], equal_nan=True), k
     assert (got["parity"] == want["parity"]).all() and (got["status"] == want["status"]).all()
     assert got["status"][20] == lufqhe_mod.ST_NONFINITE
+
+
+@pytest.mark.parametrize("n", [24, 32])
+def test_mixed_over_host_link_every_matrix_refactorised(cuda, lufqhe_mod, oracle, n):
+    """Every matrix rejected (threshold 0): the factor lists of both paths
+    (room for a quarter of the batch) overflow, and the rest are corrected in
+    place by the warp that refactorised them; host-link results equal the
+    device entry point's bit for bit, and every one is within 1e-10 of the
+    double-double oracle."""
+    lib = lufqhe_mod.lib()
+    old = lib.lufqhe_get_option(1)
+    lib.lufqhe_set_option(1, 0.0)
+    try:
+        A, _ = lufqhe_mod.gen_lll(3000, n, seed=500 + n)
+        want = dev_dict(lufqhe_mod.batch_lup_det(A, mode=2))
+        out = lufqhe_mod.batch_lup_det_host(A.cpu().pin_memory(), mode=2)
+        cuda.cuda.synchronize()
+    finally:
+        lib.lufqhe_set_option(1, old)
+    got = host_dict(out)
+    for k in ("logabs", "phase"):
+        assert np.array_equal(got[k], want[k], equal_nan=True), k
+    assert (got["status"] == want["status"]).all()
+    assert ((got["status"] & lufqhe_mod.ST_FALLBACK) != 0).all()
+    la, ph, _ = oracle.logdet_dd(A.cpu().numpy())
+    scale = np.maximum(1.0, np.abs(la))
+    assert (np.abs(got["logabs"] - la) / scale).max() < 1e-10
+    assert (np.abs(np.angle(np.exp(1j * (got["phase"] - ph)))) / scale).max() < 1e-10
