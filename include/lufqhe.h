@@ -71,7 +71,10 @@ extern "C" {
 /* FP32 complex LUP after power-of-two equilibration, FP64-accurate residual
  * R = PA - LU (float-float on FP32 pipes), log det(I + U^-1 L^-1 R) correction,
  * FP64 log|det|/phase accumulation, and a full FP64 refactorisation for any
- * matrix whose correction norm exceeds the threshold (status FALLBACK). */
+ * matrix whose correction norm exceeds the threshold (status FALLBACK; sizes
+ * above 32 go to FP64 directly, status FP64). For 17 <= n <= 40 the FP64
+ * results get an extended-precision correction of their own (an exact
+ * residual of the FP64 factors, log det(I + E)). */
 #define LUFQHE_MODE_MIXED 2
 
 /* Largest n the batched entry points accept. */

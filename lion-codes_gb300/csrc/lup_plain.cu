@@ -27,8 +27,9 @@ constexpr int kMaxWarpsPlain = 8;
 
 // Out: element type of the in-place factors (double2, or float2 for the
 // reference's complex64 buffers). CORRECT: the mixed mode's FP64 route for
-// 17 <= n <= 32, whose log-determinants get the extended-precision correction
-// (fp64_correct_warp; its scratch follows the row scales in shared memory).
+// 17 <= n <= 32 (this warp kernel's sizes), whose log-determinants get the
+// extended-precision correction (fp64_correct_warp; its scratch follows the
+// row scales in shared memory).
 template <int ARITH, class Src, class Out = double2, bool CORRECT = false>
 __global__ void __launch_bounds__(kMaxWarpsPlain * 32)
     lup_plain_kernel(Src src, Out *__restrict__ Aout, int n, int lda,
