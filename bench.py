@@ -733,7 +733,10 @@ def run_serve(args, world, rank, local, full=True):
     rng = np.random.default_rng(seed)
     ks = np.maximum(1, np.minimum(4096, np.floor(np.exp(rng.uniform(0, np.log(4097), 200000)))))
     mean_k = float(ks.mean())
-    nreq = args.serve_requests if full else max(500, args.serve_requests // 2)
+    # the same stream length in the default line's sub-result as in the full
+    # run: with k up to 4096, a short window is dominated by the drain of its
+    # last large requests
+    nreq = args.serve_requests
 
     def offline_rate(n, mode):
         count = max(512, min(32768, int(2e8 // (16 * n * n))))
@@ -750,6 +753,7 @@ def run_serve(args, world, rank, local, full=True):
         return count / (e0.elapsed_time(e1) / 3 * 1e-3)
 
     def summary(lat, ns, el, mats, rate, capacity):
+        served_k = mats / max(1, len(lat))
         per = {}
         for n in SERVE_SIZES:
             m = ns == n
@@ -758,6 +762,7 @@ def run_serve(args, world, rank, local, full=True):
                                "p99_ms": float(np.percentile(lat[m], 99) / 1e3),
                                "requests": int(m.sum())}
         return {"rate_req_s": rate, "requests": int(len(lat)),
+                "mean_k_served": served_k, "offered_dets_s": rate * served_k,
                 "p50_ms": float(np.percentile(lat, 50) / 1e3),
                 "p99_ms": float(np.percentile(lat, 99) / 1e3),
                 "throughput_dets_s": mats / el,
@@ -783,6 +788,11 @@ def run_serve(args, world, rank, local, full=True):
 
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     result = {}
+    # determinants per request of the stream: its walkers' shapes are one fixed
+    # sequence, and a window of nreq requests sees the first hundred or so of
+    # them, whose mean k is not the population's; measured once by a stream at
+    # the population's rate, then used to set every offered load in dets/s
+    k_req = None
     for label, mode, moves in (variants if full else variants[:2]):
         rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
         batched_mix = 1.0 / float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
@@ -805,11 +815,15 @@ def run_serve(args, world, rank, local, full=True):
         runs = {"closed_loop_capacity": {"walkers": args.serve_walkers, "requests": done,
                                          "seconds": el, "dets_per_s": capacity,
                                          "requests_per_s": done / el}}
-        # the offered loads: 70% of the batched (offline) rate of the size mix,
-        # in requests/s of the mix's mean k; 70% of the closed-loop capacity;
-        # the configured 20k requests/s
-        for tag, rate, nr in (("at_70pct_offline", 0.7 * batched_mix / mean_k, nreq),
-                              ("at_70pct_capacity", 0.7 * done / el, nreq),
+        if k_req is None:
+            lat, _, _, mats = srv.run_stream(rate_hz=0.7 * batched_mix / mean_k, nrequests=nreq,
+                                             moves=100, k_min=1, k_max=4096, seed=seed)
+            k_req = mats / max(1, len(lat))
+        # the offered loads, in requests/s of the stream's determinants per
+        # request: 70% of the batched (offline) rate of the size mix; 70% of
+        # the closed-loop capacity; the configured 20k requests/s
+        for tag, rate, nr in (("at_70pct_offline", 0.7 * batched_mix / k_req, nreq),
+                              ("at_70pct_capacity", 0.7 * capacity / k_req, nreq),
                               ("at_20k_req_s", 20000.0, max(200, nreq // 4))):
             lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100, k_min=1,
                                                k_max=4096, seed=seed)
@@ -837,7 +851,8 @@ def run_serve(args, world, rank, local, full=True):
             "fraction_of_offline": r70["fraction_of_offline"],
             "fraction_of_capacity": r70["fraction_of_capacity"],
             "p99_floor_ms_whole_gpu": result["default"]["p99_floor_ms_whole_gpu"],
-            "config": workload_config("serving", world) | {"mean_k": mean_k},
+            "config": workload_config("serving", world) | {"mean_k": mean_k,
+                                                           "stream_k_per_request": k_req},
             "serving": result}
 
 
@@ -935,7 +950,7 @@ def main():
     # the reference arm factorises the whole batch every step (about 15 ms on
     # 16 cores at n = 24): short steps let OpenMP start-up and box noise skew it
     ap.add_argument("--ref-sample", type=int, default=32768)
-    ap.add_argument("--serve-requests", type=int, default=4000)
+    ap.add_argument("--serve-requests", type=int, default=6000)
     ap.add_argument("--serve-walkers", type=int, default=128,
                     help="live walkers of the closed loop that measures a server's capacity")
     ap.add_argument("--no-subconfigs", action="store_true",

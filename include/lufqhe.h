@@ -312,7 +312,7 @@ int lufqhe_plan_destroy(lufqhe_plan_t *plan);
  * move resamples particle `particle` (new z per matrix), the GPU rebuilds that
  * row of every matrix (M_ik = z^k exp(-|z|^2/4)) and recomputes the k
  * determinants. One persistent kernel per size class polls a tile ring in
- * mapped host memory (bounded waits; it exits after ~0.5 s idle and is
+ * mapped host memory (bounded waits; it exits after 0.2 s idle and is
  * relaunched on demand), so requests from many walkers share the GPU and
  * overlap without a batch boundary. Walkers are admitted against the HBM
  * budget. No counterpart in the reference, whose Monte Carlo loop re-sends
@@ -320,7 +320,10 @@ int lufqhe_plan_destroy(lufqhe_plan_t *plan);
  */
 typedef struct lufqhe_server_s lufqhe_server_t;
 /* class_n: sizes served (8, 16, 32, 64); class_sms: SMs given to each (NULL =
- * equal shares); max_k: most matrices per walker; tile: matrices per work tile.
+ * equal shares); max_k: most matrices per walker; tile: matrices per work tile
+ * for the classes n <= 16 (a larger class takes max(1, tile * 16^3 / n^3), the
+ * same factorisation work per tile, so a request's matrices spread over more
+ * warps).
  * mode: LUFQHE_MODE_MIXED or LUFQHE_MODE_PLAIN_FP64_FUSED. */
 int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_bytes, int mode,
                          const int *class_n, const int *class_sms, int nclasses, int max_k,

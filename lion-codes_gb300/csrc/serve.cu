@@ -699,8 +699,24 @@ struct SClass {
   unsigned int relaunches = 0;
   unsigned int share64k = 0;       // FP64 routing share, fixed at creation
   int moves = 0;                   // this class keeps factors and takes O(n^2) moves
+  int tile = 8;                    // matrices per tile (class_tile)
   double last_query = 0.0;         // when the loop was last seen running (host clock)
 };
+
+// Matrices per tile of class n: the server's tile for n <= 16, fewer above so
+// that a tile holds no more factorisation work (n^3) than `tile` matrices of
+// n = 16 (one at n = 32 and 64 for the default 8). A warp (or warp group)
+// works through its tile's matrices one after another, so at n = 32 a tile of
+// 8 kept a request of 8 matrices on one warp for 8 serial factorisations
+// (~1.5 ms); with one matrix per tile they run side by side. The cost is in
+// claims: each tile is a compare-and-swap on the class's claim counter, and a
+// class tops out near 1.3M claims/s (about one L2 round trip per successful
+// swap among its contenders), below the n = 32 class's factorisation rate on
+// the whole GPU but above what its share of the SMs takes in a mix.
+int class_tile(int tile, int n) {
+  const long long scaled = (long long)tile * 4096 / ((long long)n * n * n);
+  return (int)std::max(1LL, std::min((long long)tile, scaled));
+}
 
 }  // namespace
 }  // namespace lufqhe
@@ -886,6 +902,7 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     sc.share64k = mode == LUFQHE_MODE_MIXED ? fp64_share_64k(sc.n) : 0u;
     // with moves every factorisation is FP64 (its factors are kept)
     sc.moves = s->moves == 1 || (s->moves == 2 && sc.n <= kMovesAutoMaxN);
+    sc.tile = class_tile(tile, sc.n);
     const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u || sc.moves;
     const size_t optin = device_smem_optin();
     size_t used = 0;
@@ -1062,7 +1079,11 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
     return LUFQHE_ERR_BUSY;
   }
   SClass &C = s->classes[W.cls];
-  const unsigned int ntiles = (unsigned int)((W.k + s->tile - 1) / s->tile);
+  const unsigned int ntiles = (unsigned int)((W.k + C.tile - 1) / C.tile);
+  if (ntiles > kRing) {
+    set_error("lufqhe_server_submit: %u tiles exceed the class ring (%u)", ntiles, kRing);
+    return LUFQHE_ERR_INVALID_ARG;
+  }
   // ring space: tiles of the oldest in-flight request of this class bound the reuse
   unsigned int oldest = C.published;
   for (int r = 0; r < kReqSlots; ++r)
@@ -1088,7 +1109,7 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
   double2 *mats = reinterpret_cast<double2 *>(blk + lay.mats);
   double2 *z = reinterpret_cast<double2 *>(blk + lay.z);
   for (unsigned int t = 0; t < ntiles; ++t) {
-    const int first = (int)t * s->tile;
+    const int first = (int)t * C.tile;
     ServeTile T;
     T.moves = s->classes[W.cls].moves;
     T.lu = reinterpret_cast<double2 *>(blk + lay.lu) + (size_t)first * W.n * W.n;
@@ -1107,7 +1128,7 @@ extern "C" int lufqhe_server_submit(lufqhe_server_t *s, int walker_id, int parti
     T.completion = s->comp_d + slot;
     T.seq = R.seq;
     T.req_tiles = ntiles;
-    T.count = std::min(s->tile, W.k - first);
+    T.count = std::min(C.tile, W.k - first);
     T.particle = particle;
     T.build = W.built ? 0 : 1;
     s->classes[W.cls].ring_h[(C.published + t) % kRing] = T;
@@ -1188,6 +1209,42 @@ extern "C" int lufqhe_server_stats(lufqhe_server_t *s, int class_n, long long *m
   return LUFQHE_SUCCESS;
 }
 
+namespace {
+// Walker shapes for the simulated clients: n uniform over the server's
+// classes, k log-uniform in [k_min, k_max], from a generator of their own and
+// taken in order, a shape staying next until a walker of it is admitted. The
+// clients' other draws (particles, coordinates, arrival binding) depend on
+// timing, and the shapes of the walkers a window sees set the determinants it
+// asks for, so every run sees the same sequence.
+struct WalkerShapes {
+  struct Shape {
+    int n, k;
+  };
+  WalkerShapes(const lufqhe_server_s *srv, unsigned long long seed, int kmin, int kmax)
+      : s(srv), rng(seed ^ 0x5deece66dull), k_min(kmin), k_max(kmax) {}
+  Shape peek() {
+    if (!have) {
+      const int nclass = (int)s->classes.size();
+      next.n = s->classes[(int)(uni(rng) * nclass) % nclass].n;
+      const double lk = std::log((double)k_min) +
+                        uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
+      next.k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
+      have = true;
+    }
+    return next;
+  }
+  void take() { have = false; }
+
+ private:
+  const lufqhe_server_s *s;
+  std::mt19937_64 rng;
+  std::uniform_real_distribution<double> uni{0.0, 1.0};
+  int k_min, k_max;
+  Shape next{0, 0};
+  bool have = false;
+};
+}  // namespace
+
 // Simulated Monte Carlo walker stream (Poisson arrivals of move requests).
 // Walkers: k log-uniform in [k_min, k_max], n uniform over the server's
 // classes; each makes `moves` single-particle moves; a request arrives at the
@@ -1208,6 +1265,7 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
     return LUFQHE_ERR_INVALID_ARG;
   }
   std::mt19937_64 rng(seed);
+  WalkerShapes shapes(s, seed, k_min, k_max);
   std::exponential_distribution<double> gap(rate_hz);
   std::uniform_real_distribution<double> uni(0.0, 1.0);
   std::normal_distribution<double> gauss(0.0, 1.0);
@@ -1272,18 +1330,23 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
           break;
         }
       if (use < 0) {
-        const int n = s->classes[(int)(uni(rng) * nclass) % nclass].n;
-        const double lk = std::log((double)k_min) +
-                          uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
-        const int k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
+        const WalkerShapes::Shape sh = shapes.peek();
         int id = -1;
-        int rc = lufqhe_server_walker_create(s, n, k, draws(n, (size_t)2 * k * n), &id);
+        int rc = lufqhe_server_walker_create(s, sh.n, sh.k, draws(sh.n, (size_t)2 * sh.k * sh.n),
+                                             &id);
+        if (rc == LUFQHE_ERR_BUSY && act.empty()) {
+          release_tables();
+          set_error("lufqhe_server_run_stream: the HBM budget admits no walker of n=%d, k=%d",
+                    sh.n, sh.k);
+          return rc;
+        }
         if (rc == LUFQHE_ERR_BUSY) break;  // HBM budget: wait for walkers to finish
         if (rc) {
           release_tables();
           return rc;
         }
-        act.push_back({id, n, k, moves, 0, 0.0, false});
+        shapes.take();
+        act.push_back({id, sh.n, sh.k, moves, 0, 0.0, false});
         use = (int)act.size() - 1;
       }
       Active &A = act[use];
@@ -1357,9 +1420,9 @@ extern "C" long long lufqhe_server_run_closed(lufqhe_server_t *s, int walkers, l
     return LUFQHE_ERR_INVALID_ARG;
   }
   std::mt19937_64 rng(seed);
+  WalkerShapes shapes(s, seed, k_min, k_max);
   std::uniform_real_distribution<double> uni(0.0, 1.0);
   std::normal_distribution<double> gauss(0.0, 1.0);
-  const int nclass = (int)s->classes.size();
   std::vector<double> zbuf;
   auto fill = [&](int n, size_t count) -> const double * {
     zbuf.resize(count);
@@ -1367,40 +1430,50 @@ extern "C" long long lufqhe_server_run_closed(lufqhe_server_t *s, int walkers, l
     for (size_t i = 0; i < count; ++i) zbuf[i] = gauss(rng) * sig;
     return zbuf.data();
   };
+  // A walker is empty (id < 0), waiting to submit (its build or its next
+  // move), or in flight. A submit refused for want of ring space or request
+  // slots leaves the walker waiting, and the sweep goes on polling the others:
+  // ring space and slots are returned only when their requests are polled, so
+  // a client that spun on the refused submit waited for itself.
   struct W {
     int id = -1, n = 0, k = 0, left = 0;
+    bool waiting = false, build = false;
     long long ticket = 0;
   };
   std::vector<W> pop(walkers);
   // a new walker (LUFQHE_ERR_BUSY while the HBM budget is spent: tried again
   // on a later sweep, after others have retired)
   auto spawn = [&](W &w) -> int {
-    w.n = s->classes[(int)(uni(rng) * nclass) % nclass].n;
-    const double lk = std::log((double)k_min) +
-                      uni(rng) * (std::log((double)k_max + 1.0) - std::log((double)k_min));
-    w.k = std::max(k_min, std::min(k_max, (int)std::floor(std::exp(lk))));
+    const WalkerShapes::Shape sh = shapes.peek();
+    int id = -1;
+    const int rc = lufqhe_server_walker_create(s, sh.n, sh.k, fill(sh.n, (size_t)2 * sh.k * sh.n),
+                                               &id);
+    if (rc) return rc;
+    shapes.take();
+    w.id = id;
+    w.n = sh.n;
+    w.k = sh.k;
     w.left = moves;
-    w.id = -1;
-    const int rc =
-        lufqhe_server_walker_create(s, w.n, w.k, fill(w.n, (size_t)2 * w.k * w.n), &w.id);
-    if (rc) w.id = -1;
+    w.waiting = true;
+    w.build = true;
+    return LUFQHE_SUCCESS;
+  };
+  // one submit attempt: LUFQHE_ERR_BUSY leaves the walker waiting
+  auto submit = [&](W &w) -> int {
+    const int particle = w.build ? -1 : (int)(uni(rng) * w.n) % w.n;
+    const int rc = lufqhe_server_submit(s, w.id, particle,
+                                        w.build ? nullptr : fill(w.n, (size_t)2 * w.k), &w.ticket);
+    if (rc == LUFQHE_SUCCESS) w.waiting = false;
     return rc;
   };
-  auto submit = [&](W &w, bool build) -> int {
-    for (;;) {  // a full ring or slot table frees as requests complete
-      const int particle = build ? -1 : (int)(uni(rng) * w.n) % w.n;
-      const int rc = lufqhe_server_submit(s, w.id, particle,
-                                          build ? nullptr : fill(w.n, (size_t)2 * w.k), &w.ticket);
-      if (rc != LUFQHE_ERR_BUSY) return rc;
-      std::this_thread::yield();
-    }
-  };
-  // the initial builds, untimed (as many walkers as the budget admits)
+  // the initial builds, untimed (as many walkers as the budget admits), each
+  // polled until it has completed; the first moves go out in the timed loop,
+  // which polls every request it submits (first moves submitted here and left
+  // unpolled could fill the ring ahead of builds still waiting for space)
   int started = 0;
   for (W &w : pop) {
-    int rc = spawn(w);
+    const int rc = spawn(w);
     if (rc == LUFQHE_ERR_BUSY) break;
-    if (!rc) rc = submit(w, true);
     if (rc) return rc;
     ++started;
   }
@@ -1408,42 +1481,69 @@ extern "C" long long lufqhe_server_run_closed(lufqhe_server_t *s, int walkers, l
     set_error("lufqhe_server_run_closed: the HBM budget admits no walker");
     return LUFQHE_ERR_BUSY;
   }
-  for (W &w : pop) {
-    if (w.id < 0) continue;
-    int rc = lufqhe_server_poll(s, w.ticket, 60000000, nullptr, nullptr, nullptr);
-    if (!rc) rc = submit(w, false);
-    if (rc) return rc;
+  for (int built = 0; built < started;) {
+    for (W &w : pop) {
+      if (w.id < 0 || !w.build) continue;  // empty, or built
+      int rc = LUFQHE_SUCCESS;
+      if (w.waiting) {
+        rc = submit(w);
+        if (rc && rc != LUFQHE_ERR_BUSY) return rc;
+        continue;
+      }
+      rc = lufqhe_server_poll(s, w.ticket, 0, nullptr, nullptr, nullptr);
+      if (rc == LUFQHE_ERR_BUSY) continue;
+      if (rc) return rc;
+      w.build = false;  // built: its first move waits for the clock
+      w.waiting = true;
+      ++built;
+    }
   }
   long long done = 0, mats = 0, issued = started;
   const double start = now_s();
   for (;;) {
-    bool live = false;
+    bool live = false, held = false, refused = false;
     for (W &w : pop) {
       int rc = LUFQHE_SUCCESS;
       if (w.id < 0) {
         if (issued >= nrequests) continue;
         live = true;
         rc = spawn(w);
-        if (rc == LUFQHE_ERR_BUSY) continue;
-        if (!rc) rc = submit(w, true);  // a new walker's build is part of the mix
+        if (rc == LUFQHE_ERR_BUSY) {
+          refused = true;
+          continue;
+        }
         if (rc) return rc;
-        ++issued;
+        ++issued;  // its build is part of the mix
+      }
+      held = true;
+      live = true;
+      if (w.waiting) {
+        rc = submit(w);
+        if (rc && rc != LUFQHE_ERR_BUSY) return rc;
         continue;
       }
-      live = true;
       rc = lufqhe_server_poll(s, w.ticket, 0, nullptr, nullptr, nullptr);
       if (rc == LUFQHE_ERR_BUSY) continue;
       if (rc) return rc;
       ++done;
       mats += w.k;
+      w.build = false;
       if (--w.left == 0 || issued >= nrequests) {
         rc = lufqhe_server_walker_destroy(s, w.id);
         w.id = -1;
+        if (rc) return rc;
       } else {
-        rc = submit(w, false);
+        w.waiting = true;
         ++issued;
+        rc = submit(w);
+        if (rc && rc != LUFQHE_ERR_BUSY) return rc;
       }
-      if (rc) return rc;
+    }
+    if (refused && !held) {
+      const WalkerShapes::Shape sh = shapes.peek();
+      set_error("lufqhe_server_run_closed: the HBM budget admits no walker of n=%d, k=%d", sh.n,
+                sh.k);
+      return LUFQHE_ERR_BUSY;
     }
     if (!live) break;
   }

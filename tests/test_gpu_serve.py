@@ -99,6 +99,22 @@ def test_walker_stream(server):
     assert mats > 400 and elapsed > 0
 
 
+@pytest.mark.timeout(300)
+def test_closed_loop_with_more_tiles_than_the_ring(lufqhe_mod, cuda):
+    """Walkers holding more tiles than a class ring (20 walkers of 4096 n = 64
+    matrices at one matrix per tile, against 65536 tiles per ring): the closed
+    loop completes every request. A submit refused for ring space waits while
+    the other walkers' requests are polled, which returns their space."""
+    srv = lufqhe_mod.Server(8 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(64,), max_k=4096,
+                            moves=False)
+    try:
+        done, elapsed, mats = srv.run_closed(walkers=20, nrequests=40, moves=3, k_min=4096,
+                                             k_max=4096, seed=3)
+    finally:
+        srv.close()
+    assert done == 40 and mats == 40 * 4096 and elapsed > 0
+
+
 def test_idle_exit_and_relaunch(server, oracle):
     """The class loops leave after 0.2 s without work; a later request
     relaunches them and completes with the right result."""
