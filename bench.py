@@ -716,9 +716,9 @@ def run_plan(args, world, rank, local, full=True):
 def run_serve(args, world, rank, local, full=True):
     """Config 5: a Poisson stream of single-particle moves of device-resident
     walkers (k log-uniform 1..4096, n uniform over 8/16/32/64, 100 moves per
-    walker). Three servers: the default (O(n^2) moves against kept FP64
-    factors for the classes n <= 16, mixed refactorisation for the others),
-    and servers that refactorise every move, mixed and FP64. For
+    walker). Three servers: the default (every move refactorised in mixed
+    mode), one taking O(n^2) moves against kept FP64 factors for the classes
+    n <= 16, and one refactorising every move in FP64. For
     each: its capacity (the determinants/s of a saturating stream), then the
     stream at 70% of that capacity and at the configured 20k requests/s, with
     p50/p99 latency (arrival to result on the host) and throughput. The
@@ -769,10 +769,10 @@ def run_serve(args, world, rank, local, full=True):
                 "fraction_of_capacity": (mats / el) / capacity if capacity else None,
                 "per_n": per}
 
-    # the library's default server (O(n^2) moves for the classes n <= 16,
-    # mixed refactorisation above), then servers that refactorise every move
-    variants = [("default", lufqhe.MODE_MIXED, "auto"),
-                ("mixed_refactor", lufqhe.MODE_MIXED, False),
+    # the library's default server (mixed refactorisation of every move), one
+    # taking O(n^2) moves for the classes n <= 16, and FP64 refactorisation
+    variants = [("default", lufqhe.MODE_MIXED, None),
+                ("moves_n_le_16", lufqhe.MODE_MIXED, "auto"),
                 ("fp64_refactor", lufqhe.MODE_PLAIN_FP64_FUSED, False)]
     def class_rate(n, mode, moves):
         """Determinants/s of one class alone on the whole GPU, closed loop

@@ -184,7 +184,7 @@ int lib_free_async(void *p, cudaStream_t s) {
 }
 
 int g_bulk_loads = 1;
-int g_serve_moves = 2;
+int g_serve_moves = 0;
 double g_move_tol = 1e-12;
 
 bool is_device_memory(const void *p) {

@@ -729,7 +729,7 @@ struct lufqhe_server_s {
   int tile = 8;
   float theta2 = 0.01f;
   int refine = 1;  // in-place refinement of the tile path (option 5)
-  int moves = 2;   // O(n^2) moves: 0 off, 1 every class, 2 classes n <= kMovesAutoMaxN (option 8)
+  int moves = 0;   // O(n^2) moves: 0 off, 1 every class, 2 classes n <= kMovesAutoMaxN (option 8)
   std::vector<SClass> classes;
   // HBM pool with a first-fit free list
   unsigned char *pool = nullptr;

@@ -358,7 +358,7 @@ class Server:
         """moves: O(n^2) determinant-ratio moves against kept FP64 factors
         (LUFQHE_OPT_SERVE_MOVES, read at creation): True for every class,
         False for none, "auto" for the classes n <= 16; None keeps the
-        option's value (default "auto")."""
+        option's value (default False: every move refactorises)."""
         import ctypes
         self._h = None
         cn = (ctypes.c_int * len(classes))(*classes)

@@ -243,7 +243,7 @@ def test_shard_by_cost_rejects(lufqhe_mod):
     (5, [0.0, 1.0], [0.5, 2.0]),         # refinement on/off
     (6, [0.0, 1.0], [2.0]),              # kernel timing
     (7, [0.0, 1.0], [3.0]),              # bulk loads
-    (8, [0.0, 1.0, 2.0], [0.5, 3.0]),    # serving moves (2: by size)
+    (8, [0.0, 1.0, 2.0], [0.5, 3.0]),    # serving moves (0: off, 2: by size)
     (9, [1e-12, 1e-8], [0.0, 1.0, -1e-12]),  # move error bound
 ])
 def test_options_round_trip_and_validation(lufqhe_mod, opt, good, bad):

@@ -23,9 +23,12 @@ def znew_draw(rng, k, n):
     return zdraw(rng, k, n)[:, 0]
 
 
-@pytest.fixture
-def server(lufqhe_mod, cuda):
-    srv = lufqhe_mod.Server(1 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(8, 16), max_k=256)
+@pytest.fixture(params=[False, "auto"], ids=["refactor", "moves"])
+def server(request, lufqhe_mod, cuda):
+    """The default server (every move refactorises) and one taking O(n^2)
+    moves for its classes n <= 16."""
+    srv = lufqhe_mod.Server(1 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(8, 16), max_k=256,
+                            moves=request.param)
     yield srv
     srv.close()
 
