@@ -793,18 +793,36 @@ def run_serve(args, world, rank, local, full=True):
     # them, whose mean k is not the population's; measured once by a stream at
     # the population's rate, then used to set every offered load in dets/s
     k_req = None
+    # each class's share of the stream's determinants, from the same stream
+    demand = None
+
+    def shares(weight):
+        sms = np.maximum(2, np.round(nsm * weight / weight.sum())).astype(int)
+        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - nsm)
+        return list(map(int, sms))
+
     for label, mode, moves in (variants if full else variants[:2]):
         rates = {n: offline_rate(n, mode) for n in SERVE_SIZES}
         batched_mix = 1.0 / float(np.mean([1.0 / rates[n] for n in SERVE_SIZES]))
-        # SM shares per class in proportion to its measured cost per
-        # determinant when served alone (k is drawn independently of n, so
-        # every class carries the same expected number of determinants)
+        # SM shares per class in proportion to the SM time its traffic needs:
+        # its share of the stream's determinants times its measured cost per
+        # determinant when served alone
         alone = {n: class_rate(n, mode, moves) for n in SERVE_SIZES}
         cost = np.array([1.0 / alone[n] for n in SERVE_SIZES])
-        sms = np.maximum(2, np.round(nsm * cost / cost.sum())).astype(int)
-        sms[np.argmax(sms)] -= max(0, int(sms.sum()) - nsm)
-        srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES,
-                            class_sms=list(map(int, sms)), max_k=4096, tile=8, moves=moves)
+        if demand is None:
+            # one stream at the population's rate, on shares for equal demand
+            srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES,
+                                class_sms=shares(cost), max_k=4096, tile=8, moves=moves)
+            lat, ns, ks_rec, _, mats = srv.run_stream(rate_hz=0.7 * batched_mix / mean_k,
+                                                      nrequests=nreq, moves=100, k_min=1,
+                                                      k_max=4096, seed=seed)
+            srv.close()
+            k_req = mats / max(1, len(lat))
+            demand = np.array([ks_rec[ns == n].sum() for n in SERVE_SIZES], dtype=np.float64)
+            demand /= max(1.0, demand.sum())
+        sms = shares(demand * cost)
+        srv = lufqhe.Server(96 << 30, mode=mode, classes=SERVE_SIZES, class_sms=sms, max_k=4096,
+                            tile=8, moves=moves)
         # capacity: a closed loop of walkers, each moving again as soon as its
         # last move completes (the open stream's work mix: 100 moves, then a
         # new walker whose first request builds its matrices)
@@ -815,18 +833,14 @@ def run_serve(args, world, rank, local, full=True):
         runs = {"closed_loop_capacity": {"walkers": args.serve_walkers, "requests": done,
                                          "seconds": el, "dets_per_s": capacity,
                                          "requests_per_s": done / el}}
-        if k_req is None:
-            lat, _, _, mats = srv.run_stream(rate_hz=0.7 * batched_mix / mean_k, nrequests=nreq,
-                                             moves=100, k_min=1, k_max=4096, seed=seed)
-            k_req = mats / max(1, len(lat))
         # the offered loads, in requests/s of the stream's determinants per
         # request: 70% of the batched (offline) rate of the size mix; 70% of
         # the closed-loop capacity; the configured 20k requests/s
         for tag, rate, nr in (("at_70pct_offline", 0.7 * batched_mix / k_req, nreq),
                               ("at_70pct_capacity", 0.7 * capacity / k_req, nreq),
                               ("at_20k_req_s", 20000.0, max(200, nreq // 4))):
-            lat, ns, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100, k_min=1,
-                                               k_max=4096, seed=seed)
+            lat, ns, _, el, mats = srv.run_stream(rate_hz=rate, nrequests=nr, moves=100,
+                                                  k_min=1, k_max=4096, seed=seed)
             runs[tag] = summary(lat, ns, el, mats, rate, capacity) | \
                 {"fraction_of_offline": (mats / el) / batched_mix}
         srv.close()
@@ -840,7 +854,10 @@ def run_serve(args, world, rank, local, full=True):
                          "batched_offline_dets_per_s": {str(n): rates[n] for n in SERVE_SIZES},
                          "batched_offline_mix_dets_per_s": batched_mix,
                          "class_alone_dets_per_s": {str(n): alone[n] for n in SERVE_SIZES},
-                         "class_sms": list(map(int, sms)), "runs": runs,
+                         "class_sms": sms,
+                         "class_demand_share": {str(n): float(d)
+                                                for n, d in zip(SERVE_SIZES, demand)},
+                         "runs": runs,
                          "p99_floor_ms_whole_gpu": p99_floor_ms,
                          "moves_o_n2": moved, "moves_refactorised": refac}
     if rank != 0:

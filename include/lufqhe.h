@@ -346,11 +346,13 @@ int lufqhe_server_poll(lufqhe_server_t *server, long long ticket, int wait_us, d
 int lufqhe_server_destroy(lufqhe_server_t *server);
 /* Simulated walker stream: Poisson move arrivals at rate_hz, k log-uniform in
  * [k_min, k_max], n uniform over the classes, `moves` moves per walker.
- * Writes per-request latency (us, arrival to completion) and n; returns the
- * number of records, *elapsed_s the wall time, *matrices the determinants. */
+ * Walker shapes (n, k) come in the same sequence in every run. Writes
+ * per-request latency (us, arrival to completion), n and k (rec_n, rec_k may
+ * be NULL); returns the number of records, *elapsed_s the wall time,
+ * *matrices the determinants. */
 long long lufqhe_server_run_stream(lufqhe_server_t *server, double rate_hz, long long nrequests,
                                    int moves, int k_min, int k_max, unsigned long long seed,
-                                   double *lat_us, int *rec_n, long long max_records,
+                                   double *lat_us, int *rec_n, int *rec_k, long long max_records,
                                    double *elapsed_s, long long *matrices);
 /* Closed loop: `walkers` live walkers (k log-uniform in [k_min, k_max], n
  * uniform over the classes) each submit their next move when the previous one

@@ -86,11 +86,11 @@ struct ServeTile {
 };
 
 struct ClassCtl {                // device memory, one per class
-  unsigned int claimed;          // tiles claimed so far (never above published)
+  unsigned int claimed;          // tiles claimed so far (see claim_tile)
   unsigned int exited;           // warps that left the loop
   unsigned long long last_ns;    // %globaltimer of the class's latest claim
   unsigned int pub_seen;         // device mirror of the host's published count
-  unsigned int pad;
+  unsigned int ahead;            // adds that claimed a tile not yet published (see claim_tile)
   unsigned long long moved;      // moves taken by the O(n^2) path
   unsigned long long refactored; // moves that refactorised instead
   double move_tol;               // the moves' error bound
@@ -127,8 +127,20 @@ __device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int *p) {
 // thread read the host count (acquire) and raise the mirror (after a fence, so
 // a tile claimed through the mirror is ordered after the host's writes of it).
 // Idle threads back off exponentially between host reads, up to ~8 us.
+// Under a deep backlog (the mirror at least `backlog_add` tiles ahead of the
+// claims, twice the class's claimers) a tile is claimed with an add instead.
+// Every successful swap costs its contenders about one L2 round trip, so a
+// class claiming only by swaps topped out near 1.3M tiles/s, below the n = 32
+// and n = 64 classes' rates at one matrix per tile; an add always succeeds.
+// Between its reads and its add a claimer waits less than any tile takes to
+// process, so each other claimer adds at most once in that window and the
+// add lands below the published count. Should it land above (ctl->ahead
+// counts those), the claimer keeps the tile and waits for its publication.
+__device__ bool wait_published(const unsigned int *published, const unsigned int *stop,
+                               ClassCtl *ctl, unsigned int t);
+
 __device__ bool claim_tile(const unsigned int *published, const unsigned int *stop, ClassCtl *ctl,
-                           unsigned int &idx) {
+                           unsigned int backlog_add, unsigned int &idx) {
   const unsigned long long t0 = global_ns();
   volatile unsigned int *claimed = &ctl->claimed;
   unsigned int backoff = 128;
@@ -136,6 +148,14 @@ __device__ bool claim_tile(const unsigned int *published, const unsigned int *st
     const unsigned int c = *claimed;
     const unsigned int p = ld_acquire_gpu(&ctl->pub_seen);
     if ((int)(p - c) > 0) {
+      if (p - c >= backlog_add) {
+        const unsigned int t = atomicAdd(&ctl->claimed, 1u);
+        atomicMax(&ctl->last_ns, global_ns());
+        idx = t;
+        if ((int)(p - t) > 0) return true;
+        atomicAdd(&ctl->ahead, 1u);
+        return wait_published(published, stop, ctl, t);
+      }
       if (atomicCAS(&ctl->claimed, c, c + 1u) == c) {
         idx = c;
         atomicMax(&ctl->last_ns, global_ns());
@@ -164,6 +184,36 @@ __device__ bool claim_tile(const unsigned int *published, const unsigned int *st
   }
 }
 
+
+// A tile claimed by an add ahead of its publication: wait until the host has
+// published it (raising the mirror as claim_tile does). Bounded: the server
+// stopping, or kTicketWaitNs without the publication, gives up; the tile is
+// then never processed and its request's poll times out on the host.
+constexpr unsigned long long kTicketWaitNs = 10000000000ull;  // 10 s
+
+__device__ bool wait_published(const unsigned int *published, const unsigned int *stop,
+                               ClassCtl *ctl, unsigned int t) {
+  const unsigned long long t0 = global_ns();
+  unsigned int backoff = 128;
+  for (;;) {
+    const unsigned int p = ld_acquire_gpu(&ctl->pub_seen);
+    if ((int)(p - t) > 0) return true;
+    const unsigned int ph = ld_acquire_sys(published);
+    if ((int)(ph - p) > 0) {
+      __threadfence();
+      unsigned int old = p;
+      while ((int)(ph - old) > 0) {  // raise the mirror (wrap-safe)
+        const unsigned int prev = atomicCAS(&ctl->pub_seen, old, ph);
+        if (prev == old) break;
+        old = prev;
+      }
+      continue;
+    }
+    if (ld_acquire_sys(stop) || global_ns() - t0 > kTicketWaitNs) return false;
+    __nanosleep(backoff);
+    backoff = backoff < 8192u ? 2u * backoff : 8192u;
+  }
+}
 
 // Apply the move to the tile's matrices: z_particle <- znew, then rebuild that
 // row (lane j handles matrix j); with t.build every row of every matrix is
@@ -297,7 +347,8 @@ __global__ void __launch_bounds__(serve_max_warps(NC) * 32, 1)
     // claim the next published tile; give up when the class has been idle
     unsigned int idx = 0;
     int give_up = 0;
-    if (lane == 0) give_up = claim_tile(published, stop, ctl, idx) ? 0 : 1;
+    if (lane == 0)
+      give_up = claim_tile(published, stop, ctl, 2u * gridDim.x * (unsigned int)warps, idx) ? 0 : 1;
     idx = __shfl_sync(kFull, idx, 0);
     give_up = __shfl_sync(kFull, give_up, 0);
     if (give_up) {
@@ -461,7 +512,8 @@ __global__ void __launch_bounds__(kServeGroupsMax * kFp64GroupWarps * 32, 1)
   for (;;) {
     if (tid == 0) {
       unsigned int idx = 0;
-      const bool go = claim_tile(published, stop, ctl, idx);
+      const bool go =
+          claim_tile(published, stop, ctl, 2u * gridDim.x * (unsigned int)groups, idx);
       go_s[g] = go;
       if (go) {
         // the ring lives in mapped host memory: read it uncached, word by word
@@ -1252,12 +1304,13 @@ struct WalkerShapes {
 // still running, when that move completes. Walkers are admitted against the HBM
 // budget (a walker that does not fit waits for one to finish). Per request the
 // latency from its arrival to its completion is written to lat_us (capacity
-// max_records), and the request's n to rec_n. Returns the number recorded;
+// max_records), and the request's n and k to rec_n and rec_k (either may be
+// null). Returns the number recorded;
 // *elapsed_s gets the wall time and *matrices the determinants computed.
 extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz,
                                               long long nrequests, int moves, int k_min, int k_max,
                                               unsigned long long seed, double *lat_us, int *rec_n,
-                                              long long max_records, double *elapsed_s,
+                                              int *rec_k, long long max_records, double *elapsed_s,
                                               long long *matrices) {
   if (!s || rate_hz <= 0 || nrequests < 1 || moves < 1 || k_min < 1 || k_max < k_min ||
       k_max > s->max_k) {
@@ -1373,6 +1426,7 @@ extern "C" long long lufqhe_server_run_stream(lufqhe_server_t *s, double rate_hz
           if (recorded < max_records) {
             lat_us[recorded] = (done - A.arrival) * 1e6;
             if (rec_n) rec_n[recorded] = A.n;
+            if (rec_k) rec_k[recorded] = A.k;
           }
           ++recorded;
           mats += A.k;

@@ -423,14 +423,15 @@ class Server:
         import numpy as np
         lat = np.empty(nrequests)
         ns = np.empty(nrequests, np.int32)
+        ks = np.empty(nrequests, np.int32)
         el = ctypes.c_double()
         mats = ctypes.c_longlong()
         r = lib().lufqhe_server_run_stream(self._h, rate_hz, nrequests, moves, k_min, k_max, seed,
-                                           lat.ctypes.data, ns.ctypes.data, nrequests,
-                                           ctypes.byref(el), ctypes.byref(mats))
+                                           lat.ctypes.data, ns.ctypes.data, ks.ctypes.data,
+                                           nrequests, ctypes.byref(el), ctypes.byref(mats))
         if r < 0:
             _native.check(int(r), "lufqhe_server_run_stream")
-        return lat[:r], ns[:r], el.value, mats.value
+        return lat[:r], ns[:r], ks[:r], el.value, mats.value
 
     def run_closed(self, walkers: int, nrequests: int, moves: int = 100, k_min: int = 1,
                    k_max: int = 4096, seed: int = 5):

@@ -45,7 +45,7 @@ SIGNATURES = {
     "lufqhe_server_submit": (I32, [P, I32, I32, P, P]),
     "lufqhe_server_poll": (I32, [P, I64, I32, P, P, P]),
     "lufqhe_server_destroy": (I32, [P]),
-    "lufqhe_server_run_stream": (I64, [P, F64, I64, I32, I32, I32, U64, P, P, I64, P, P]),
+    "lufqhe_server_run_stream": (I64, [P, F64, I64, I32, I32, I32, U64, P, P, P, I64, P, P]),
     "lufqhe_server_run_closed": (I64, [P, I32, I64, I32, I32, I32, U64, P, P]),
     "lufqhe_server_stats": (I32, [P, I32, P, P]),
     "lufqhe_read_matrices_f32": (I64, [_c.c_char_p, I32, I64, I64, I32, P]),

@@ -95,10 +95,11 @@ def test_hbm_admission(lufqhe_mod, cuda):
 
 
 def test_walker_stream(server):
-    lat, ns, elapsed, mats = server.run_stream(rate_hz=5000, nrequests=400, moves=10, k_min=1,
-                                               k_max=256, seed=7)
+    lat, ns, ks, elapsed, mats = server.run_stream(rate_hz=5000, nrequests=400, moves=10,
+                                                   k_min=1, k_max=256, seed=7)
     assert len(lat) == 400 and np.isfinite(lat).all() and (lat > 0).all()
     assert set(np.unique(ns)) <= {8, 16}
+    assert ((ks >= 1) & (ks <= 256)).all() and ks.sum() == mats
     assert mats > 400 and elapsed > 0
 
 
