@@ -955,6 +955,12 @@ extern "C" int lufqhe_server_create(lufqhe_server_t **server, size_t hbm_budget_
     // with moves every factorisation is FP64 (its factors are kept)
     sc.moves = s->moves == 1 || (s->moves == 2 && sc.n <= kMovesAutoMaxN);
     sc.tile = class_tile(tile, sc.n);
+    if ((max_k + sc.tile - 1) / sc.tile > (int)kRing) {
+      set_error("lufqhe_server_create: max_k=%d needs more than the %u tiles of class n=%d's ring",
+                max_k, kRing, sc.n);
+      rc = LUFQHE_ERR_INVALID_ARG;
+      break;
+    }
     const bool fp64_only = mode != LUFQHE_MODE_MIXED || sc.share64k >= 65536u || sc.moves;
     const size_t optin = device_smem_optin();
     size_t used = 0;

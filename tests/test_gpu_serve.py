@@ -119,6 +119,13 @@ def test_closed_loop_with_more_tiles_than_the_ring(lufqhe_mod, cuda):
     assert done == 40 and mats == 40 * 4096 and elapsed > 0
 
 
+def test_max_k_beyond_a_class_ring_is_refused(lufqhe_mod, cuda):
+    """At one matrix per tile (n = 64) a walker of 70000 matrices would need
+    more tiles than the class ring holds: creation refuses it."""
+    with pytest.raises(RuntimeError, match="ring"):
+        lufqhe_mod.Server(1 << 30, mode=lufqhe_mod.MODE_MIXED, classes=(64,), max_k=70000)
+
+
 def test_idle_exit_and_relaunch(server, oracle):
     """The class loops leave after 0.2 s without work; a later request
     relaunches them and completes with the right result."""
