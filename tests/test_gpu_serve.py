@@ -191,6 +191,35 @@ def test_large_class_matches_batched_fp64_bits(lufqhe_mod, cuda, mode):
         srv.close()
 
 
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_default_server_matches_batched_mixed_bits(lufqhe_mod, cuda, n):
+    """The default server (every move refactorised in mixed mode; one matrix
+    per tile at n = 32, eight below) gives the batched mixed path's bits on
+    the same matrices, for a walker's first request and after a move: log|det|,
+    phase and status, FP64 refactorisations and their corrections included."""
+    import torch
+    mixed = lufqhe_mod.MODE_MIXED
+    srv = lufqhe_mod.Server(1 << 30, mode=mixed, classes=(n,), max_k=512)
+    try:
+        rng = np.random.default_rng(20 + n)
+        z = zdraw(rng, 300, n)
+        w = srv.walker(z)
+        for particle in (-1, n // 2):
+            if particle >= 0:
+                znew = znew_draw(rng, 300, n)
+                la, ph, st = srv.result(srv.submit(w, particle, znew), 300)
+                z[:, particle] = znew
+            else:
+                la, ph, st = srv.result(srv.submit(w, -1), 300)
+            ref = lufqhe_mod.lll_det(torch.from_numpy(z).cuda(), mode=mixed)
+            assert np.array_equal(la, ref.logabs.cpu().numpy())
+            assert np.array_equal(ph, ref.phase.cpu().numpy())
+            assert (st == ref.status.cpu().numpy()).all()
+        srv.destroy_walker(w)
+    finally:
+        srv.close()
+
+
 @pytest.mark.parametrize("n,tol", [(8, 1e-10), (16, 1e-10), (32, None), (64, None)])
 def test_moves_against_double_double(lufqhe_mod, cuda, oracle, n, tol):
     """O(n^2) moves (kept FP64 factors, determinant lemma, Woodbury over the
