@@ -28,10 +28,24 @@
 
 namespace lufqhe {
 
+// The plan's correction passes (lup_mixed.cu, where the correction kernel is
+// built): corrections of the FP64 factorisations listed for size n, each
+// entry with its matrix; head is the list's zeroed header block.
+int launch_listed_corrections(int n, const void *head, const unsigned char *list, long long cap,
+                              double *logabs, double *phase, int8_t *parity, int32_t *status,
+                              cudaStream_t stream);
+size_t listed_count_offset();
+size_t head_bytes();
+
 
 namespace {
 
 using namespace mixed;
+
+// Sizes whose FP64 factorisations a mixed plan lists for its correction pass
+// (the register-tiled sizes the correction kernel is built for): lists is an
+// array of kListMaxN + 1 FacLists indexed by n.
+constexpr int kListMaxN = 32;
 
 struct WorkItem {
   const double2 *A;  // group base
@@ -72,15 +86,17 @@ template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int nm, int lane,
                                float theta2, bool refine, unsigned int share64k, int status_or,
-                               DeferredOut &out, double *logabs, double *phase, int8_t *parity,
-                               int32_t *status) {
+                               const FacList *fl, DeferredOut &out, double *logabs, double *phase,
+                               int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
-  // a group on the FP32 path has F and 2n ints (n <= nm) for the correction
+  // a group on the FP32 path has F and 2n ints (n <= nm) for the correction;
+  // with a list (fl) its FP64 factorisations are listed for the plan's
+  // correction pass instead, while the list has room
   const CorrScratch cs{F, er, hold};
   if (MODE == LUFQHE_MODE_MIXED && route_fp64(src, share64k)) {
-    fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
-                  LUFQHE_ST_FP64, &cs);
+    fallback_fp64_src(DenseSource{src, lda}, 0, n, M, lds, hold, lane, ob, logabs, phase, parity,
+                      status, LUFQHE_ST_FP64, &cs, fl);
     return;
   }
   if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
@@ -112,8 +128,8 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
     if (ok)
       out.push(lane, ob, prod, exp_sum, corr, par, logabs, phase, parity, status);
     else
-      fallback_fp64(src, n, lda, M, lds, hold, lane, ob, logabs, phase, parity, status,
-                    LUFQHE_ST_FALLBACK, &cs);
+      fallback_fp64_src(DenseSource{src, lda}, 0, n, M, lds, hold, lane, ob, logabs, phase,
+                        parity, status, LUFQHE_ST_FALLBACK, &cs, fl);
   } else {
     // a mixed plan's FP64 route (status_or set) gets the correction where the
     // batched mixed mode does; its pass reserves the scratch (nm >= n)
@@ -150,7 +166,8 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nm,
                    int nf,
                    float theta2, int refine, double *__restrict__ logabs, double *__restrict__ phase,
-                   int8_t *__restrict__ parity, int32_t *__restrict__ status) {
+                   int8_t *__restrict__ parity, int32_t *__restrict__ status,
+                   const FacList *__restrict__ lists) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
@@ -171,11 +188,15 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     it = __shfl_sync(kFull, it, 0);
     if (it >= (unsigned int)nitems) break;
     const WorkItem w = items[it];
+    // the plan's factor list for this size (lists[n].count null: none)
+    const FacList *fl = nullptr;
+    if (MODE == LUFQHE_MODE_MIXED && lists && w.n <= kListMaxN && lists[w.n].count)
+      fl = lists + w.n;
     for (int j = 0; j < w.count; ++j) {
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, out,
+                           ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, fl, out,
                            logabs, phase, parity, status);
     }
   }
@@ -183,7 +204,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
 }
 
 using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, int,
-                               double *, double *, int8_t *, int32_t *);
+                               double *, double *, int8_t *, int32_t *, const FacList *);
 
 GroupedKernel kernel_for(int mode) {
   switch (mode) {
@@ -212,9 +233,10 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
     grouped_group_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter,
                          int nm, int nf, float theta2, int refine, double *__restrict__ logabs,
                          double *__restrict__ phase, int8_t *__restrict__ parity,
-                         int32_t *__restrict__ status) {
+                         int32_t *__restrict__ status, const FacList *__restrict__ lists) {
   (void)theta2;
   (void)refine;
+  (void)lists;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long red[3 * kFp64GroupWarps];
   __shared__ unsigned int item;
@@ -329,6 +351,18 @@ struct lufqhe_plan_s {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cap_stream = nullptr;
   std::string report;
+  // a mixed plan's factor lists (n = 24 and 32): the FP64 factorisations of
+  // its FP32-path groups, corrected after the passes by a whole CTA each, as
+  // in the batched mixed mode (a warp correcting its own in place had made
+  // the plan's warp pass 1.9 times the batched calls' time). d_lists is the
+  // device array by n that the grouped kernel reads.
+  struct PlanList {
+    int n = 0;
+    unsigned char *head = nullptr, *buf = nullptr;
+    long long cap = 0;
+  };
+  std::vector<PlanList> lists;
+  lufqhe::mixed::FacList *d_lists = nullptr;
 };
 
 namespace {
@@ -473,6 +507,8 @@ int configure_launch(lufqhe_plan_s *p, int warps) {
 int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
   int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 3 * sizeof(unsigned int), s),
                       "memset(counter)");
+  for (const auto &l : p->lists)
+    if (!rc) rc = check_cuda(cudaMemsetAsync(l.head, 0, head_bytes(), s), "memset(list head)");
   for (int pass = 0; pass < 3 && !rc; ++pass) {
     const Launch &L = p->launch[pass];
     if (L.nitems == 0 || L.ctas == 0) continue;
@@ -485,10 +521,55 @@ int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
     k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
                                                        p->refine,
-                                                       p->logabs, p->phase, p->parity, p->status);
+                                                       p->logabs, p->phase, p->parity, p->status,
+                                                       p->d_lists);
     timer.stop();
     rc = check_cuda(cudaGetLastError(), "grouped_kernel launch");
   }
+  for (const auto &l : p->lists)
+    if (!rc)
+      rc = launch_listed_corrections(l.n, l.head, l.buf, l.cap, p->logabs, p->phase, p->parity,
+                                     p->status, s);
+  return rc;
+}
+
+// A mixed plan's factor lists: for n = 24 and 32, room for kPlanListShare of
+// the plan's matrices of that size (the FP32 path rejects 4-5% of n = 24 and
+// ~18% of n = 32 LLL matrices); a factorisation beyond it is corrected in
+// place by its warp.
+constexpr double kPlanListShare = 0.3;
+
+int alloc_lists(lufqhe_plan_s *p) {
+  if (p->mode != LUFQHE_MODE_MIXED) return LUFQHE_SUCCESS;
+  std::vector<mixed::FacList> host(kListMaxN + 1, mixed::FacList{nullptr, nullptr, 0, 0});
+  for (int n : {24, 32}) {
+    long long count = 0;
+    for (const auto &G : p->groups)
+      if (G.n == n) count += G.count;
+    const long long cap = (long long)std::ceil(kPlanListShare * (double)count);
+    if (cap < 1) continue;
+    lufqhe_plan_s::PlanList l;
+    l.n = n;
+    l.cap = cap;
+    int rc = check_cuda(cudaMalloc(&l.head, head_bytes()), "cudaMalloc(list head)");
+    if (!rc)
+      rc = check_cuda(cudaMalloc(&l.buf, (size_t)cap * mixed::fac_entry_bytes(n, true)),
+                      "cudaMalloc(factor list)");
+    if (rc) {
+      if (l.head) cudaFree(l.head);
+      return rc;
+    }
+    p->lists.push_back(l);
+    host[n] = mixed::FacList{
+        reinterpret_cast<unsigned long long *>(l.head + listed_count_offset()), l.buf, cap, 1};
+  }
+  if (p->lists.empty()) return LUFQHE_SUCCESS;
+  int rc = check_cuda(cudaMalloc(&p->d_lists, host.size() * sizeof(mixed::FacList)),
+                      "cudaMalloc(lists)");
+  if (!rc)
+    rc = check_cuda(cudaMemcpy(p->d_lists, host.data(), host.size() * sizeof(mixed::FacList),
+                               cudaMemcpyHostToDevice),
+                    "copy(lists)");
   return rc;
 }
 
@@ -619,6 +700,11 @@ void destroy_plan(lufqhe_plan_s *p) {
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->d_items) cudaFree(p->d_items);
   if (p->d_counter) cudaFree(p->d_counter);
+  for (const auto &l : p->lists) {
+    cudaFree(l.head);
+    cudaFree(l.buf);
+  }
+  if (p->d_lists) cudaFree(p->d_lists);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
 }
@@ -679,6 +765,7 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   if (!rc)
     rc = check_cuda(cudaMalloc(&p->d_counter, 3 * sizeof(unsigned int)), "cudaMalloc(counter)");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sync(plan inputs)");
+  if (!rc) rc = alloc_lists(p);
   if (!rc && (flags & LUFQHE_PLAN_AUTOTUNE) && p->total > 0) rc = autotune(p, p->cap_stream);
   if (!rc) rc = build_items(p, p->cap_stream);
   if (!rc && !(flags & LUFQHE_PLAN_AUTOTUNE)) {
@@ -719,7 +806,7 @@ extern "C" int lufqhe_plan_describe(const lufqhe_plan_t *plan, char *buf, size_t
     return LUFQHE_ERR_INVALID_ARG;
   }
   // the report is one JSON object: add the kernels one execution launches
-  int kernels = 0;
+  int kernels = (int)plan->lists.size();  // the correction passes
   for (const Launch &L : plan->launch) kernels += (L.nitems > 0 && L.ctas > 0) ? 1 : 0;
   std::string r = plan->report;
   const size_t close = r.rfind('}');

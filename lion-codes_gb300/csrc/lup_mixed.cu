@@ -2,6 +2,8 @@
 // lowest-Landau-level entry points, the precision policy and the options.
 // The method and its kernels are described in mixed_kernels.cuh.
 
+#include <cstddef>
+
 #include "mixed_kernels.cuh"
 
 namespace lufqhe {
@@ -63,6 +65,30 @@ int launch_mixed(const double2 *A, int n, int lda, long long batch, double *loga
       },
       inplace);
 }
+
+// A mixed plan's correction pass: the FP64 factorisations its grouped kernel
+// listed for size n, each entry with its matrix (the plan's groups have no
+// common source). head is the list's header block (kHeadBytes, zeroed before
+// the plan's passes); the corrections are those of the batched mixed mode, on
+// a whole CTA per entry.
+int launch_listed_corrections(int n, const void *head, const unsigned char *list, long long cap,
+                              double *logabs, double *phase, int8_t *parity, int32_t *status,
+                              cudaStream_t stream) {
+  const CallHead *h = static_cast<const CallHead *>(head);
+  switch (n) {
+    case 24:
+      return launch_fac_correct<24, DenseSource, true>(DenseSource{nullptr, 24}, h, list, cap,
+                                                       logabs, phase, parity, status, stream);
+    case 32:
+      return launch_fac_correct<32, DenseSource, true>(DenseSource{nullptr, 32}, h, list, cap,
+                                                       logabs, phase, parity, status, stream);
+    default:
+      set_error("listed corrections: n=%d has no correction pass", n);
+      return LUFQHE_ERR_UNSUPPORTED_N;
+  }
+}
+size_t listed_count_offset() { return offsetof(CallHead, corr_count); }
+size_t head_bytes() { return kHeadBytes; }
 
 int launch_mixed_lll(const double2 *Z, int n, long long batch, double *logabs, double *phase,
                      int8_t *parity, int32_t *status, cudaStream_t stream) {
