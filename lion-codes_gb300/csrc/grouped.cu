@@ -47,6 +47,28 @@ using namespace mixed;
 // array of kListMaxN + 1 FacLists indexed by n.
 constexpr int kListMaxN = 32;
 
+// A matrix that a mixed plan's warp pass sends to FP64 (rejected by the FP32
+// path, or routed), for the plan's pending pass.
+struct PendEntry {
+  const double2 *A;  // the matrix
+  long long ob;      // its output index
+  int n, lda, flag, pad;
+};
+
+// A mixed plan's device extras, passed to its kernels by value: the factor
+// lists by n, and the pending FP64 refactorisations of its n >= kPlanDeferMinN
+// matrices (pend null: each is refactorised by the warp that rejected it).
+struct PlanAux {
+  const FacList *lists;
+  PendEntry *pend;
+  unsigned int *pend_count;
+  unsigned int pend_cap;
+};
+
+// Sizes whose FP64 refactorisations a mixed plan leaves to its pending pass
+// (as the batched mixed mode leaves them to its finish kernel from n = 24).
+constexpr int kPlanDeferMinN = 24;
+
 struct WorkItem {
   const double2 *A;  // group base
   long long first;   // first matrix of the tile within the group
@@ -82,21 +104,42 @@ __host__ __device__ inline WarpLayout warp_layout(int nm, int nf) {
   return L;
 }
 
+// FP64 refactorisation of a matrix of a mixed plan's warp pass: appended to
+// the pending list when the plan has one for this size and it has room, else
+// done here (its factors listed for the correction pass when fl has room).
+__device__ void plan_fp64(const double2 *src, int n, int lda, long long ob, double2 *M,
+                          double *hold, int lane, int flag, const CorrScratch &cs,
+                          const FacList *fl, const PlanAux &aux, double *logabs, double *phase,
+                          int8_t *parity, int32_t *status) {
+  // (the pending pass's shared memory holds the plan's largest n <= kListMaxN)
+  if (aux.pend && n >= kPlanDeferMinN && n <= kListMaxN) {
+    unsigned int k = 0;
+    if (lane == 0) k = atomicAdd(aux.pend_count, 1u);
+    k = __shfl_sync(kFull, k, 0);
+    if (k < aux.pend_cap) {
+      if (lane == 0) aux.pend[k] = PendEntry{src, ob, n, lda, flag, 0};
+      return;
+    }
+  }
+  fallback_fp64_src(DenseSource{src, lda}, 0, n, M, n + 1, hold, lane, ob, logabs, phase, parity,
+                    status, flag, &cs, fl);
+}
+
 template <int MODE>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int nm, int lane,
                                float theta2, bool refine, unsigned int share64k, int status_or,
-                               const FacList *fl, DeferredOut &out, double *logabs, double *phase,
-                               int8_t *parity, int32_t *status) {
+                               const FacList *fl, const PlanAux &aux, DeferredOut &out,
+                               double *logabs, double *phase, int8_t *parity, int32_t *status) {
   const int lds = n + 1;
   double2 *M = reinterpret_cast<double2 *>(HL);
   // a group on the FP32 path has F and 2n ints (n <= nm) for the correction;
-  // with a list (fl) its FP64 factorisations are listed for the plan's
-  // correction pass instead, while the list has room
+  // a mixed plan defers its FP64 refactorisations and lists their factors for
+  // its correction pass, while its lists have room
   const CorrScratch cs{F, er, hold};
   if (MODE == LUFQHE_MODE_MIXED && route_fp64(src, share64k)) {
-    fallback_fp64_src(DenseSource{src, lda}, 0, n, M, lds, hold, lane, ob, logabs, phase, parity,
-                      status, LUFQHE_ST_FP64, &cs, fl);
+    plan_fp64(src, n, lda, ob, M, hold, lane, LUFQHE_ST_FP64, cs, fl, aux, logabs, phase, parity,
+              status);
     return;
   }
   if (load_matrix_fp64(src, n, lda, M, lds, lane)) {
@@ -128,8 +171,8 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
     if (ok)
       out.push(lane, ob, prod, exp_sum, corr, par, logabs, phase, parity, status);
     else
-      fallback_fp64_src(DenseSource{src, lda}, 0, n, M, lds, hold, lane, ob, logabs, phase,
-                        parity, status, LUFQHE_ST_FALLBACK, &cs, fl);
+      plan_fp64(src, n, lda, ob, M, hold, lane, LUFQHE_ST_FALLBACK, cs, fl, aux, logabs, phase,
+                parity, status);
   } else {
     // a mixed plan's FP64 route (status_or set) gets the correction where the
     // batched mixed mode does; its pass reserves the scratch (nm >= n)
@@ -166,8 +209,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nm,
                    int nf,
                    float theta2, int refine, double *__restrict__ logabs, double *__restrict__ phase,
-                   int8_t *__restrict__ parity, int32_t *__restrict__ status,
-                   const FacList *__restrict__ lists) {
+                   int8_t *__restrict__ parity, int32_t *__restrict__ status, PlanAux aux) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5;
@@ -190,21 +232,21 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     const WorkItem w = items[it];
     // the plan's factor list for this size (lists[n].count null: none)
     const FacList *fl = nullptr;
-    if (MODE == LUFQHE_MODE_MIXED && lists && w.n <= kListMaxN && lists[w.n].count)
-      fl = lists + w.n;
+    if (MODE == LUFQHE_MODE_MIXED && aux.lists && w.n <= kListMaxN && aux.lists[w.n].count)
+      fl = aux.lists + w.n;
     for (int j = 0; j < w.count; ++j) {
       __syncwarp();
       const long long b = w.first + j;
       process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
-                           ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, fl, out,
-                           logabs, phase, parity, status);
+                           ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, fl, aux,
+                           out, logabs, phase, parity, status);
     }
   }
   out.flush(lane, logabs, phase, parity, status);
 }
 
 using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, int,
-                               double *, double *, int8_t *, int32_t *, const FacList *);
+                               double *, double *, int8_t *, int32_t *, PlanAux);
 
 GroupedKernel kernel_for(int mode) {
   switch (mode) {
@@ -233,10 +275,10 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
     grouped_group_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter,
                          int nm, int nf, float theta2, int refine, double *__restrict__ logabs,
                          double *__restrict__ phase, int8_t *__restrict__ parity,
-                         int32_t *__restrict__ status, const FacList *__restrict__ lists) {
+                         int32_t *__restrict__ status, PlanAux aux) {
   (void)theta2;
   (void)refine;
-  (void)lists;
+  (void)aux;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long red[3 * kFp64GroupWarps];
   __shared__ unsigned int item;
@@ -292,6 +334,45 @@ __global__ void __launch_bounds__(kFp64GroupWarps * 32)
         if (status) status[ob] = st | w.status_or;
       }
     }
+  }
+}
+
+// A mixed plan's pending pass: the FP64 refactorisations its warp pass left
+// (n >= kPlanDeferMinN), one warp per matrix, in shared memory sized for the
+// largest of them (the matrix, row scales, and the correction's scratch)
+// rather than the warp pass's FP32-path layout and registers. Each
+// factorisation is listed for the correction pass while its size's list has
+// room, else corrected here.
+constexpr int kPendWarps = 4;
+
+__host__ __device__ inline size_t pending_warp_bytes(int n) {
+  const size_t b = (size_t)n * (n + 1) * sizeof(double2) + 2 * (size_t)n * sizeof(double) +
+                   (size_t)n * (n + 1) * sizeof(float2) + 2 * (size_t)n * sizeof(int);
+  return (b + 15) & ~(size_t)15;
+}
+
+__global__ void __launch_bounds__(kPendWarps * 32)
+    grouped_pending_kernel(PlanAux aux, int nmax, double *__restrict__ logabs,
+                           double *__restrict__ phase, int8_t *__restrict__ parity,
+                           int32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  unsigned char *base = smem_raw + (size_t)warp * pending_warp_bytes(nmax);
+  double2 *M = reinterpret_cast<double2 *>(base);
+  double *hold = reinterpret_cast<double *>(M + (size_t)nmax * (nmax + 1));
+  float2 *F = reinterpret_cast<float2 *>(hold + 2 * nmax);
+  int *ints = reinterpret_cast<int *>(F + (size_t)nmax * (nmax + 1));
+  const CorrScratch cs{F, ints, hold};
+  const unsigned int listed = min(*aux.pend_count, aux.pend_cap);
+  const unsigned int stride = (unsigned int)(gridDim.x * warps);
+  for (unsigned int j = blockIdx.x * warps + warp; j < listed; j += stride) {
+    const PendEntry e = aux.pend[j];
+    const FacList *fl = nullptr;
+    if (aux.lists && e.n <= kListMaxN && aux.lists[e.n].count) fl = aux.lists + e.n;
+    fallback_fp64_src(DenseSource{e.A, e.lda}, 0, e.n, M, e.n + 1, hold, lane, e.ob, logabs,
+                      phase, parity, status, e.flag, &cs, fl);
   }
 }
 
@@ -363,6 +444,12 @@ struct lufqhe_plan_s {
   };
   std::vector<PlanList> lists;
   lufqhe::mixed::FacList *d_lists = nullptr;
+  // its pending FP64 refactorisations (n = 24..32) and their pass's launch
+  lufqhe::PendEntry *d_pend = nullptr;
+  unsigned int *d_pend_count = nullptr;
+  unsigned int pend_cap = 0;
+  int pend_nmax = 0, pend_ctas = 0;
+  size_t pend_smem = 0;
 };
 
 namespace {
@@ -504,11 +591,18 @@ int configure_launch(lufqhe_plan_s *p, int warps) {
   return rc;
 }
 
+PlanAux aux_of(const lufqhe_plan_s *p) {
+  return PlanAux{p->d_lists, p->d_pend, p->d_pend_count, p->pend_cap};
+}
+
 int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
   int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 3 * sizeof(unsigned int), s),
                       "memset(counter)");
   for (const auto &l : p->lists)
     if (!rc) rc = check_cuda(cudaMemsetAsync(l.head, 0, head_bytes(), s), "memset(list head)");
+  if (!rc && p->d_pend_count)
+    rc = check_cuda(cudaMemsetAsync(p->d_pend_count, 0, sizeof(unsigned int), s),
+                    "memset(pending count)");
   for (int pass = 0; pass < 3 && !rc; ++pass) {
     const Launch &L = p->launch[pass];
     if (L.nitems == 0 || L.ctas == 0) continue;
@@ -522,9 +616,16 @@ int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
                                                        p->refine,
                                                        p->logabs, p->phase, p->parity, p->status,
-                                                       p->d_lists);
+                                                       aux_of(p));
     timer.stop();
     rc = check_cuda(cudaGetLastError(), "grouped_kernel launch");
+  }
+  if (!rc && p->pend_cap) {
+    KernelTimer timer("grouped_pending_kernel", p->pend_nmax, s);
+    grouped_pending_kernel<<<p->pend_ctas, kPendWarps * 32, p->pend_smem, s>>>(
+        aux_of(p), p->pend_nmax, p->logabs, p->phase, p->parity, p->status);
+    timer.stop();
+    rc = check_cuda(cudaGetLastError(), "grouped_pending_kernel launch");
   }
   for (const auto &l : p->lists)
     if (!rc)
@@ -563,14 +664,43 @@ int alloc_lists(lufqhe_plan_s *p) {
     host[n] = mixed::FacList{
         reinterpret_cast<unsigned long long *>(l.head + listed_count_offset()), l.buf, cap, 1};
   }
-  if (p->lists.empty()) return LUFQHE_SUCCESS;
-  int rc = check_cuda(cudaMalloc(&p->d_lists, host.size() * sizeof(mixed::FacList)),
-                      "cudaMalloc(lists)");
+  int rc = LUFQHE_SUCCESS;
+  if (!p->lists.empty()) {
+    rc = check_cuda(cudaMalloc(&p->d_lists, host.size() * sizeof(mixed::FacList)),
+                    "cudaMalloc(lists)");
+    if (!rc)
+      rc = check_cuda(cudaMemcpy(p->d_lists, host.data(), host.size() * sizeof(mixed::FacList),
+                                 cudaMemcpyHostToDevice),
+                      "copy(lists)");
+  }
+  // the pending list: room for kPlanListShare of the matrices with
+  // kPlanDeferMinN <= n <= 32 (the FP32 path's sizes that defer)
+  long long count = 0;
+  for (const auto &G : p->groups)
+    if (G.n >= kPlanDeferMinN && G.n <= kListMaxN) {
+      count += G.count;
+      p->pend_nmax = std::max(p->pend_nmax, G.n);
+    }
+  const long long cap = (long long)std::ceil(kPlanListShare * (double)count);
+  if (rc || cap < 1) return rc;
+  rc = check_cuda(cudaMalloc(&p->d_pend, (size_t)cap * sizeof(PendEntry)), "cudaMalloc(pending)");
   if (!rc)
-    rc = check_cuda(cudaMemcpy(p->d_lists, host.data(), host.size() * sizeof(mixed::FacList),
-                               cudaMemcpyHostToDevice),
-                    "copy(lists)");
-  return rc;
+    rc = check_cuda(cudaMalloc(&p->d_pend_count, sizeof(unsigned int)), "cudaMalloc(pending count)");
+  if (rc) return rc;
+  p->pend_smem = kPendWarps * pending_warp_bytes(p->pend_nmax);
+  rc = check_cuda(cudaFuncSetAttribute(grouped_pending_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)p->pend_smem),
+                  "cudaFuncSetAttribute(pending)");
+  int per_sm = 0;
+  if (!rc)
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &per_sm, grouped_pending_kernel, kPendWarps * 32, p->pend_smem),
+                    "occupancy(pending)");
+  if (rc) return rc;
+  p->pend_ctas = device_sm_count() * std::max(1, per_sm);
+  p->pend_cap = (unsigned int)cap;
+  return LUFQHE_SUCCESS;
 }
 
 // Time one launch (ms) after one warm-up launch.
@@ -705,6 +835,8 @@ void destroy_plan(lufqhe_plan_s *p) {
     cudaFree(l.buf);
   }
   if (p->d_lists) cudaFree(p->d_lists);
+  if (p->d_pend) cudaFree(p->d_pend);
+  if (p->d_pend_count) cudaFree(p->d_pend_count);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
 }
@@ -806,7 +938,8 @@ extern "C" int lufqhe_plan_describe(const lufqhe_plan_t *plan, char *buf, size_t
     return LUFQHE_ERR_INVALID_ARG;
   }
   // the report is one JSON object: add the kernels one execution launches
-  int kernels = (int)plan->lists.size();  // the correction passes
+  // the pending and correction passes
+  int kernels = (int)plan->lists.size() + (plan->pend_cap ? 1 : 0);
   for (const Launch &L : plan->launch) kernels += (L.nitems > 0 && L.ctas > 0) ? 1 : 0;
   std::string r = plan->report;
   const size_t close = r.rfind('}');
