@@ -392,7 +392,9 @@ GroupedKernel group_kernel_for(int mode, bool correct) {
 //  2. the warp-group kernel over the FP64-route groups with n > 32 (fused
 //     arithmetic for a mixed plan, the plan's arithmetic for a plain one).
 // Groups routed to FP64 need neither the FP32 path's shared memory nor its
-// registers, and get the plain kernels' occupancy.
+// registers, and get the plain kernels' occupancy. After the passes a mixed
+// plan runs its pending pass (grouped_pending_kernel) and the correction
+// passes of its factor lists.
 struct Launch {
   int mode = LUFQHE_MODE_MIXED;
   int nm = 0, nf = 1;  // warp_layout of the pass
