@@ -298,7 +298,11 @@ typedef struct lufqhe_plan_s lufqhe_plan_t;
 int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *groups, int ngroups, int mode,
                        double *d_logabs, double *d_phase, int8_t *d_parity, int32_t *d_status,
                        int flags, void *stream);
-/* Replay the captured graph on `stream` (asynchronous). */
+/* Replay the captured graph on `stream` (asynchronous). A plan's work
+ * counters and lists (a mixed plan's pending FP64 refactorisations and factor
+ * lists) are its own device memory, reset by each execution: executions of
+ * one plan must not overlap on the GPU (order them on one stream); different
+ * plans may run side by side. */
 int lufqhe_plan_execute(lufqhe_plan_t *plan, void *stream);
 /* The same work as lufqhe_plan_execute, launched directly instead of via the graph. */
 int lufqhe_plan_launch_direct(lufqhe_plan_t *plan, void *stream);
