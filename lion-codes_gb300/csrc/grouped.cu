@@ -69,6 +69,13 @@ struct PlanAux {
 // (as the batched mixed mode leaves them to its finish kernel from n = 24).
 constexpr int kPlanDeferMinN = 24;
 
+// A plan's passes (see Launch), and the largest n of a mixed plan's small
+// pass: its own build of the grouped kernel, whose register-tiled cases stop
+// at n = 16, takes under 128 registers and runs two 8-warp CTAs per SM where
+// the build with the n = 24 and 32 cases (190 registers) runs one.
+constexpr int kPlanPasses = 4;
+constexpr int kSmallPassMaxN = 16;
+
 struct WorkItem {
   const double2 *A;  // group base
   long long first;   // first matrix of the tile within the group
@@ -125,7 +132,7 @@ __device__ void plan_fp64(const double2 *src, int n, int lda, long long ob, doub
                     status, flag, &cs, fl);
 }
 
-template <int MODE>
+template <int MODE, bool SMALL = false>
 __device__ void process_matrix(const double2 *src, int n, int lda, long long ob, float4 *HL,
                                float2 *F, double *hold, int *er, int *ec, int nm, int lane,
                                float theta2, bool refine, unsigned int share64k, int status_or,
@@ -156,8 +163,15 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
       case 8: ok = mixed_factor_tile<8>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
       case 12: ok = mixed_factor_tile<12>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
       case 16: ok = mixed_factor_tile<16>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
-      case 24: ok = mixed_factor_tile<24>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
-      case 32: ok = mixed_factor_tile<32>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine); break;
+      // (never reached in the small pass, n <= kSmallPassMaxN)
+      case 24:
+        if constexpr (SMALL) ok = false;
+        else ok = mixed_factor_tile<24>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine);
+        break;
+      case 32:
+        if constexpr (SMALL) ok = false;
+        else ok = mixed_factor_tile<32>(HL, F, er, ec, lane, theta2, prod, exp_sum, corr, par, refine);
+        break;
       default: {
         MixedSmem S;
         S.SC = HL;
@@ -204,8 +218,8 @@ __device__ void process_matrix(const double2 *src, int n, int lda, long long ob,
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
+template <int MODE, bool SMALL = false>
+__global__ void __launch_bounds__(kMaxWarpsMixed * 32, SMALL ? 2 : 1)
     grouped_kernel(const WorkItem *__restrict__ items, int nitems, unsigned int *counter, int nm,
                    int nf,
                    float theta2, int refine, double *__restrict__ logabs, double *__restrict__ phase,
@@ -237,7 +251,7 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
     for (int j = 0; j < w.count; ++j) {
       __syncwarp();
       const long long b = w.first + j;
-      process_matrix<MODE>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
+      process_matrix<MODE, SMALL>(w.A + (size_t)b * w.n * w.lda, w.n, w.lda, w.out + j, HL, F, hold, er,
                            ec, nm, lane, theta2, refine != 0, w.share64k, w.status_or, fl, aux,
                            out, logabs, phase, parity, status);
     }
@@ -248,11 +262,12 @@ __global__ void __launch_bounds__(kMaxWarpsMixed * 32, 1)
 using GroupedKernel = void (*)(const WorkItem *, int, unsigned int *, int, int, float, int,
                                double *, double *, int8_t *, int32_t *, PlanAux);
 
-GroupedKernel kernel_for(int mode) {
+GroupedKernel kernel_for(int mode, bool small = false) {
   switch (mode) {
     case LUFQHE_MODE_PLAIN_FP64: return grouped_kernel<LUFQHE_MODE_PLAIN_FP64>;
     case LUFQHE_MODE_PLAIN_FP64_FUSED: return grouped_kernel<LUFQHE_MODE_PLAIN_FP64_FUSED>;
-    default: return grouped_kernel<LUFQHE_MODE_MIXED>;
+    default:
+      return small ? grouped_kernel<LUFQHE_MODE_MIXED, true> : grouped_kernel<LUFQHE_MODE_MIXED>;
   }
 }
 
@@ -390,7 +405,9 @@ GroupedKernel group_kernel_for(int mode, bool correct) {
 //  1. (mixed plans) the plain fused kernel over the groups with n <= 32 that
 //     the precision policy sends to FP64;
 //  2. the warp-group kernel over the FP64-route groups with n > 32 (fused
-//     arithmetic for a mixed plan, the plan's arithmetic for a plain one).
+//     arithmetic for a mixed plan, the plan's arithmetic for a plain one);
+//  3. (mixed plans) the small build of the mixed kernel over the FP32-path
+//     groups with n <= kSmallPassMaxN, at twice pass 0's occupancy.
 // Groups routed to FP64 need neither the FP32 path's shared memory nor its
 // registers, and get the plain kernels' occupancy. After the passes a mixed
 // plan runs its pending pass (grouped_pending_kernel) and the correction
@@ -424,7 +441,7 @@ struct lufqhe_plan_s {
   // per-group tile size and FP64 share (1/65536) chosen by the tuner
   std::vector<int> tile;
   std::vector<unsigned int> share;
-  Launch launch[3];
+  Launch launch[kPlanPasses];
   // device state
   WorkItem *d_items = nullptr;
   unsigned int *d_counter = nullptr;
@@ -461,7 +478,8 @@ namespace {
 int pass_of(const lufqhe_plan_s *p, size_t g) {
   const bool fp64 = p->mode != LUFQHE_MODE_MIXED || p->share[g] >= 65536u;
   if (fp64 && p->groups[g].n >= kFp64GroupMinN) return 2;
-  return p->mode == LUFQHE_MODE_MIXED && fp64 ? 1 : 0;
+  if (p->mode == LUFQHE_MODE_MIXED && fp64) return 1;
+  return p->mode == LUFQHE_MODE_MIXED && p->groups[g].n <= kSmallPassMaxN ? 3 : 0;
 }
 
 int build_items(lufqhe_plan_s *p, cudaStream_t s) {
@@ -469,7 +487,7 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return p->groups[a].n > p->groups[b].n; });
-  std::vector<WorkItem> items[3];
+  std::vector<WorkItem> items[kPlanPasses];
   for (int g : order) {
     const lufqhe_group_t &G = p->groups[g];
     const int T = p->tile[g];
@@ -482,13 +500,14 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
       w.count = (int)std::min<long long>(T, G.count - f);
       w.n = G.n;
       w.lda = G.lda;
-      w.share64k = p->mode == LUFQHE_MODE_MIXED && pass == 0 ? p->share[g] : 0u;
-      w.status_or = p->mode == LUFQHE_MODE_MIXED && pass > 0 ? LUFQHE_ST_FP64 : 0;
+      const bool fp32_path = pass == 0 || pass == 3;
+      w.share64k = p->mode == LUFQHE_MODE_MIXED && fp32_path ? p->share[g] : 0u;
+      w.status_or = p->mode == LUFQHE_MODE_MIXED && !fp32_path ? LUFQHE_ST_FP64 : 0;
       items[pass].push_back(w);
     }
   }
   std::vector<WorkItem> all;
-  for (int q = 0; q < 3; ++q) {
+  for (int q = 0; q < kPlanPasses; ++q) {
     p->launch[q].first = (int)all.size();
     p->launch[q].nitems = (int)items[q].size();
     all.insert(all.end(), items[q].begin(), items[q].end());
@@ -515,7 +534,8 @@ int build_items(lufqhe_plan_s *p, cudaStream_t s) {
 // without groups is left empty.
 int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
   Launch &L = p->launch[pass];
-  L.mode = pass > 0 && p->mode == LUFQHE_MODE_MIXED ? LUFQHE_MODE_PLAIN_FP64_FUSED : p->mode;
+  L.mode = (pass == 1 || pass == 2) && p->mode == LUFQHE_MODE_MIXED ? LUFQHE_MODE_PLAIN_FP64_FUSED
+                                                                    : p->mode;
   L.nm = 0;
   L.nf = 0;
   for (size_t g = 0; g < p->groups.size(); ++g) {
@@ -562,7 +582,7 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
     L.ctas = device_sm_count() * per_sm;
     return LUFQHE_SUCCESS;
   }
-  GroupedKernel k = kernel_for(L.mode);
+  GroupedKernel k = kernel_for(L.mode, pass == 3);
   const size_t per_warp = warp_layout(L.nm, L.nf).total;
   const size_t optin = device_smem_optin();
   int w = std::min<int>(warps, (int)(optin / per_warp));
@@ -589,7 +609,7 @@ int configure_pass(lufqhe_plan_s *p, int pass, int warps) {
 
 int configure_launch(lufqhe_plan_s *p, int warps) {
   int rc = 0;
-  for (int pass = 0; pass < 3 && !rc; ++pass) rc = configure_pass(p, pass, warps);
+  for (int pass = 0; pass < kPlanPasses && !rc; ++pass) rc = configure_pass(p, pass, warps);
   return rc;
 }
 
@@ -598,21 +618,23 @@ PlanAux aux_of(const lufqhe_plan_s *p) {
 }
 
 int launch_once(lufqhe_plan_s *p, cudaStream_t s) {
-  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, 3 * sizeof(unsigned int), s),
+  int rc = check_cuda(cudaMemsetAsync(p->d_counter, 0, kPlanPasses * sizeof(unsigned int), s),
                       "memset(counter)");
   for (const auto &l : p->lists)
     if (!rc) rc = check_cuda(cudaMemsetAsync(l.head, 0, head_bytes(), s), "memset(list head)");
   if (!rc && p->d_pend_count)
     rc = check_cuda(cudaMemsetAsync(p->d_pend_count, 0, sizeof(unsigned int), s),
                     "memset(pending count)");
-  for (int pass = 0; pass < 3 && !rc; ++pass) {
+  for (int pass = 0; pass < kPlanPasses && !rc; ++pass) {
     const Launch &L = p->launch[pass];
     if (L.nitems == 0 || L.ctas == 0) continue;
-    GroupedKernel k = pass == 2 ? group_kernel_for(L.mode, L.nm > 0) : kernel_for(L.mode);
+    GroupedKernel k =
+        pass == 2 ? group_kernel_for(L.mode, L.nm > 0) : kernel_for(L.mode, pass == 3);
     // a warp-group CTA takes one item at a time
     const long long want = pass == 2 ? L.nitems : (L.nitems + L.warps - 1) / L.warps;
     const int grid = (int)std::min<long long>(L.ctas, want);
-    static const char *names[3] = {"grouped_kernel", "grouped_kernel_fp64", "grouped_group_kernel"};
+    static const char *names[kPlanPasses] = {"grouped_kernel", "grouped_kernel_fp64",
+                                             "grouped_group_kernel", "grouped_kernel_small"};
     KernelTimer timer(names[pass], L.nf, s);
     k<<<std::max(1, grid), L.warps * 32, L.smem, s>>>(p->d_items + L.first, L.nitems,
                                                        p->d_counter + pass, L.nm, L.nf, p->theta2,
@@ -785,7 +807,8 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   for (int w : {2, 4, 8}) {
     rc = configure_launch(p, w);
     if (rc) return rc;
-    if (p->launch[0].warps != w && p->launch[1].warps != w) continue;  // does not fit
+    if (p->launch[0].warps != w && p->launch[1].warps != w && p->launch[3].warps != w)
+      continue;  // does not fit
     float ms = 0.0f;
     rc = time_launch(p, s, &ms);
     if (rc) return rc;
@@ -801,8 +824,9 @@ int autotune(lufqhe_plan_s *p, cudaStream_t s) {
   if (rc) return rc;
   snprintf(line, sizeof(line),
            "}, \"chosen_warps\": %d, \"ctas\": %d, \"fp64_pass_ctas\": %d, "
-           "\"group_pass_ctas\": %d}",
-           p->launch[0].warps, p->launch[0].ctas, p->launch[1].ctas, p->launch[2].ctas);
+           "\"group_pass_ctas\": %d, \"small_pass_ctas\": %d}",
+           p->launch[0].warps, p->launch[0].ctas, p->launch[1].ctas, p->launch[2].ctas,
+           p->launch[3].ctas);
   p->report += line;
   return LUFQHE_SUCCESS;
 }
@@ -897,7 +921,8 @@ extern "C" int lufqhe_plan_create(lufqhe_plan_t **plan, const lufqhe_group_t *gr
   int rc = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking),
                       "cudaStreamCreate(plan)");
   if (!rc)
-    rc = check_cuda(cudaMalloc(&p->d_counter, 3 * sizeof(unsigned int)), "cudaMalloc(counter)");
+    rc = check_cuda(cudaMalloc(&p->d_counter, kPlanPasses * sizeof(unsigned int)),
+                    "cudaMalloc(counter)");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sync(plan inputs)");
   if (!rc) rc = alloc_lists(p);
   if (!rc && (flags & LUFQHE_PLAN_AUTOTUNE) && p->total > 0) rc = autotune(p, p->cap_stream);
