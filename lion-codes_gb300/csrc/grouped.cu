@@ -12,8 +12,13 @@
 //
 // A plan (lufqhe_plan_create) fixes the groups and output buffers, chooses the
 // tile sizes and the warps per CTA with an autotuner that times candidate
-// launches on the plan's own data, and captures "reset counter + persistent
-// kernel" in a CUDA graph that lufqhe_plan_execute replays.
+// launches on the plan's own data, and captures its launch in a CUDA graph
+// that lufqhe_plan_execute replays:
+//  - the counter and list resets;
+//  - its passes, each a persistent kernel (see Launch);
+//  - for a mixed plan, the pending FP64 refactorisations of its n = 24..32
+//    matrices and the correction passes of their listed factors, as the
+//    batched mixed mode runs them.
 
 #include <algorithm>
 #include <cmath>
